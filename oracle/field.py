@@ -1,0 +1,343 @@
+"""float64 torch restatement of the neural-SDF field, NeuS rendering and losses.
+
+TEST INFRASTRUCTURE ONLY -- the checker, never the product path.
+
+Each function states the reference lines it follows.  Parameters travel as a
+plain dict of tensors (layout described in ``init_params``); autograd in
+float64 provides the reference gradients.  The hash-grid encoder is the numpy
+restatement in ``oracle/hashgrid.py`` wrapped as an autograd function.
+"""
+import math
+
+import numpy as np
+import torch
+import torch.nn.functional as F
+
+from . import hashgrid as hg
+
+
+# ---------------------------------------------------------------------------
+# configuration (plain dict; mirrors projects/neuralangelo/configs/base.yaml:38-115)
+
+def make_config(n_levels=16, n_features=8, log2_hashmap_size=22, base_resolution=32,
+                per_level_scale=None, max_resolution=2048, active_levels=None,
+                sdf_hidden=256, rgb_hidden=256, rgb_layers=4, app_dim=0, n_images=0,
+                softplus_beta=100.0, out_bias=0.5, inside_out=False, s_var_init=3.0,
+                anneal_end=0.1, taps=6, vol_range=(-2.0, 2.0), sh_levels=3):
+    if per_level_scale is None:
+        # modules.py:39-41
+        per_level_scale = float(np.exp((np.log(max_resolution) - np.log(base_resolution)) / (n_levels - 1)))
+    return dict(n_levels=n_levels, n_features=n_features, log2_hashmap_size=log2_hashmap_size,
+                base_resolution=base_resolution, per_level_scale=per_level_scale,
+                active_levels=n_levels if active_levels is None else active_levels,
+                sdf_hidden=sdf_hidden, rgb_hidden=rgb_hidden, rgb_layers=rgb_layers, app_dim=app_dim,
+                n_images=n_images, softplus_beta=softplus_beta, out_bias=out_bias, inside_out=inside_out,
+                s_var_init=s_var_init, anneal_end=anneal_end, taps=taps, vol_range=vol_range,
+                sh_levels=sh_levels)
+
+
+def eps_resolutions(cfg):
+    """modules.py:52-54: resolutions[l] = floor(r_min * growth^l) + 1 (used only for eps)."""
+    g = cfg['per_level_scale']
+    return [int(np.floor(cfg['base_resolution'] * g ** lv).astype(int)) + 1 for lv in range(cfg['n_levels'])]
+
+
+def normal_eps(cfg, anneal_levels):
+    """modules.py:102-107: eps = 1 / resolutions[anneal_levels - 1]."""
+    return 1.0 / eps_resolutions(cfg)[anneal_levels - 1]
+
+
+# ---------------------------------------------------------------------------
+# hash-grid encoder as a float64 autograd function
+
+class _HashGridFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, table, layout, active):
+        xn = x.detach().to(torch.float32).cpu().numpy()
+        out = hg.encode(xn, table.detach().cpu().numpy(), layout, active)
+        ctx.save_for_backward(x)
+        ctx.layout, ctx.active, ctx.dtype = layout, active, table.dtype
+        return torch.from_numpy(out).to(table.dtype)
+
+    @staticmethod
+    def backward(ctx, d_out):
+        (x,) = ctx.saved_tensors
+        g = hg.encode_backward(x.detach().to(torch.float32).cpu().numpy(),
+                               d_out.detach().cpu().numpy(), ctx.layout, ctx.active)
+        return None, torch.from_numpy(g.reshape(-1)).to(ctx.dtype), None, None
+
+
+def hashgrid(x01, table, layout, active=None):
+    """x01 [...,3] in [0,1] -> [..., L*F]; the table gradient flows, dx does not
+    (numerical-gradient mode never asks for it)."""
+    shp = x01.shape[:-1]
+    out = _HashGridFn.apply(x01.reshape(-1, 3), table, layout, active)
+    return out.reshape(*shp, out.shape[-1])
+
+
+# ---------------------------------------------------------------------------
+# parameters
+
+def weight_norm(v, g):
+    """torch.nn.utils.weight_norm(dim=0): W = g * v / ||v||_row (mlp.py:42-43, nerf_util.py:177-178)."""
+    return v * (g / v.norm(dim=1, keepdim=True))
+
+
+def rgb_layer_dims(cfg):
+    """modules.py:186-202: input = [x 3, SH 16, normal 3, feat, app] -> hidden*layers -> 3."""
+    sh = (cfg['sh_levels'] + 1) ** 2
+    d_in = 6 + sh + cfg['sdf_hidden'] + cfg['app_dim']
+    return [d_in] + [cfg['rgb_hidden']] * cfg['rgb_layers'] + [3]
+
+
+def init_params(cfg, seed=0, enc_perturb=1e-2, table_scale=1e-4, dtype=torch.float64):
+    """Seeded parameters with the reference's initialisation.
+
+    Geometric init (mlp.py:71-84) zeroes the encoding columns of SDF layer 0, so
+    the table gradient would be exactly zero; a seeded N(0, enc_perturb) is
+    added to those columns so table-gradient parity is meaningful.
+    Layout (all float64 unless dtype says otherwise):
+      table [n_entries*F] ~ U(-table_scale, table_scale)
+      sdf.l0.{v,g,b}: v [H, 3+L*F]; sdf.l1.{v,g,b}: v [H,H]; sdf.head.{w,b}: w [1,H]
+      rgb.l{i}.{v,g,b} for each colour layer; s_var (scalar); app [n_images, app_dim]
+    """
+    gen = torch.Generator().manual_seed(seed)
+    L, Fd = cfg['n_levels'], cfg['n_features']
+    layout = hg.level_layout(L, Fd, cfg['log2_hashmap_size'], cfg['base_resolution'], cfg['per_level_scale'])
+    H = cfg['sdf_hidden']
+    p = {}
+    p['table'] = (torch.rand(layout['n_entries'] * Fd, generator=gen, dtype=torch.float64) * 2 - 1) * table_scale
+    d0 = 3 + L * Fd
+    # layer 0: N(0, sqrt(2/k_out)), encoding columns zero (mlp.py:72-75), then perturbed
+    v0 = torch.randn(H, d0, generator=gen, dtype=torch.float64) * math.sqrt(2.0 / H)
+    v0[:, 3:] = torch.randn(H, d0 - 3, generator=gen, dtype=torch.float64) * enc_perturb
+    v1 = torch.randn(H, H, generator=gen, dtype=torch.float64) * math.sqrt(2.0 / H)
+    for name, v in (('sdf.l0', v0), ('sdf.l1', v1)):
+        p[name + '.v'] = v
+        p[name + '.g'] = v.norm(dim=1, keepdim=True).clone()   # weight_norm init: g = ||v||
+        p[name + '.b'] = torch.zeros(H, dtype=torch.float64)
+    # SDF head: N(sqrt(pi/k_in), 1e-4), bias -out_bias (mlp.py:79-84)
+    sgn = -1.0 if cfg['inside_out'] else 1.0
+    p['sdf.head.w'] = sgn * (math.sqrt(math.pi / H) + 1e-4 * torch.randn(1, H, generator=gen, dtype=torch.float64))
+    p['sdf.head.b'] = sgn * torch.full((1,), -cfg['out_bias'], dtype=torch.float64)
+    dims = rgb_layer_dims(cfg)
+    for i, (k_in, k_out) in enumerate(zip(dims[:-1], dims[1:])):
+        bound = 1.0 / math.sqrt(k_in)                  # torch.nn.Linear default init
+        v = (torch.rand(k_out, k_in, generator=gen, dtype=torch.float64) * 2 - 1) * bound
+        b = (torch.rand(k_out, generator=gen, dtype=torch.float64) * 2 - 1) * bound
+        if i == len(dims) - 2:
+            b = torch.zeros_like(b)                    # nerf_util.py:182-183
+        p[f'rgb.l{i}.v'] = v
+        p[f'rgb.l{i}.g'] = v.norm(dim=1, keepdim=True).clone()
+        p[f'rgb.l{i}.b'] = b
+    p['s_var'] = torch.tensor(cfg['s_var_init'], dtype=torch.float64)
+    if cfg['app_dim'] > 0:
+        p['app'] = torch.randn(cfg['n_images'], cfg['app_dim'], generator=gen, dtype=torch.float64)
+    return {k: v.to(dtype) for k, v in p.items()}, layout
+
+
+# ---------------------------------------------------------------------------
+# field
+
+def softplus(x, beta):
+    """torch.nn.functional.softplus(beta, threshold=20) (misc.py:92-107 via base.yaml:46-48)."""
+    return F.softplus(x, beta=beta)
+
+
+def sdf_mlp(p, cfg, enc_in, with_feat):
+    """MLPforNeuralSDF.forward (mlp.py:55-69) for layer_dims [3+LF, H, H]:
+    h0 = softplus(W0 in + b0); sdf = w_head h0 + b_head; feat = softplus(W1 h0 + b1)."""
+    beta = cfg['softplus_beta']
+    W0 = weight_norm(p['sdf.l0.v'], p['sdf.l0.g'])
+    h0 = softplus(enc_in @ W0.t() + p['sdf.l0.b'], beta)
+    sdf = h0 @ p['sdf.head.w'].t() + p['sdf.head.b']
+    feat = None
+    if with_feat:
+        W1 = weight_norm(p['sdf.l1.v'], p['sdf.l1.g'])
+        feat = softplus(h0 @ W1.t() + p['sdf.l1.b'], beta)
+    return sdf, feat
+
+
+def encode(p, cfg, layout, pts):
+    """NeuralSDF.encode (modules.py:76-95): normalise by the volume range, hash-grid,
+    coarse-to-fine mask (implemented by not evaluating masked levels), cat [x, enc]."""
+    vmin, vmax = cfg['vol_range']
+    x01 = (pts - vmin) / (vmax - vmin)
+    enc = hashgrid(x01, p['table'], layout, cfg['active_levels'])
+    return torch.cat([pts, enc], dim=-1)
+
+
+def neural_sdf(p, cfg, layout, pts, with_feat=True):
+    return sdf_mlp(p, cfg, encode(p, cfg, layout, pts), with_feat)
+
+
+def tap_offsets(cfg, eps):
+    """Tap displacement vectors, modules.py:134-143 (6 taps) / :158-166 (4 taps)."""
+    if cfg['taps'] == 6:
+        return [(eps, 0, 0), (-eps, 0, 0), (0, eps, 0), (0, -eps, 0), (0, 0, eps), (0, 0, -eps)]
+    e = eps / np.sqrt(3)
+    return [(e, -e, -e), (-e, -e, e), (-e, e, -e), (e, e, e)]
+
+
+def compute_gradients(p, cfg, layout, pts, eps, sdf_centre, training=True):
+    """NeuralSDF.compute_gradients, numerical mode (modules.py:131-178).
+
+    6 taps: g_i = (f(x+e_i) - f(x-e_i)) / 2eps; H_ii = (f+ + f- - 2 sdf) / eps^2
+    where sdf is the caller's (post-overwrite) centre value (model.py:163-166).
+    """
+    dt = pts.dtype
+    if cfg['taps'] == 6:
+        fs = []
+        for d in range(3):
+            e = torch.zeros(3, dtype=dt)
+            e[d] = eps
+            fs.append((neural_sdf(p, cfg, layout, pts + e, False)[0],
+                       neural_sdf(p, cfg, layout, pts - e, False)[0]))
+        grad = torch.cat([(fp - fm) / (2 * eps) for fp, fm in fs], dim=-1)
+        hess = torch.cat([(fp + fm - 2 * sdf_centre) / (eps ** 2) for fp, fm in fs], dim=-1) if training else None
+        return grad, hess
+    e = eps / np.sqrt(3)
+    ks = [torch.tensor(k, dtype=dt) for k in ((1, -1, -1), (-1, -1, 1), (-1, 1, -1), (1, 1, 1))]
+    sd = [neural_sdf(p, cfg, layout, pts + k * e, False)[0] for k in ks]
+    grad = sum(k * s for k, s in zip(ks, sd)) / (4.0 * e)
+    hess = None
+    if training:
+        hxx = ((sd[0] + sd[1] + sd[2] + sd[3]) / 2.0 - 2 * sdf_centre) / e ** 2
+        hess = torch.cat([hxx, hxx, hxx], dim=-1) / 3.0
+    return grad, hess
+
+
+_SH_C0 = 0.28209479177387814
+_SH_C1 = 0.4886025119029199
+_SH_C2 = (1.0925484305920792, -1.0925484305920792, 0.31539156525252005, -1.0925484305920792, 0.5462742152960396)
+_SH_C3 = (-0.5900435899266435, 2.890611442640554, -0.4570457994644658, 0.3731763325901154,
+          -0.4570457994644658, 1.445305721320277, -0.5900435899266435)
+
+
+def spherical_harmonics(d):
+    """Degree-3 real SH basis (projects/neuralangelo/utils/spherical_harmonics.py:47-84).
+    The coefficients are the standard real-SH normalisation constants.  The
+    reference stores the basis in a tensor of the default dtype (float32,
+    spherical_harmonics.py:49), so each value is rounded to float32 once."""
+    x, y, z = d.unbind(-1)
+    xx, yy, zz = x * x, y * y, z * z
+    xy, yz, xz = x * y, y * z, x * z
+    return torch.stack([
+        torch.full_like(x, _SH_C0),
+        -_SH_C1 * y, _SH_C1 * z, -_SH_C1 * x,
+        _SH_C2[0] * xy, _SH_C2[1] * yz, _SH_C2[2] * (2.0 * zz - xx - yy), _SH_C2[3] * xz, _SH_C2[4] * (xx - yy),
+        _SH_C3[0] * y * (3 * xx - yy), _SH_C3[1] * xy * z, _SH_C3[2] * y * (4 * zz - xx - yy),
+        _SH_C3[3] * z * (2 * zz - 3 * xx - 3 * yy), _SH_C3[4] * x * (4 * zz - xx - yy),
+        _SH_C3[5] * z * (xx - yy), _SH_C3[6] * x * (xx - 3 * yy)], dim=-1).to(torch.float32).to(d.dtype)
+
+
+def neural_rgb(p, cfg, pts, normals, rays_unit, feats, app):
+    """NeuralRGB.forward (modules.py:209-220) with MLPwithSkipConnection (nerf_util.py:187-196):
+    input [x, SH(d), n, feat, app], ReLU hidden layers, sigmoid output."""
+    parts = [pts, spherical_harmonics(rays_unit), normals, feats]
+    if app is not None:
+        parts.append(app)
+    h = torch.cat(parts, dim=-1)
+    n = cfg['rgb_layers'] + 1
+    for i in range(n):
+        W = weight_norm(p[f'rgb.l{i}.v'], p[f'rgb.l{i}.g'])
+        h = h @ W.t() + p[f'rgb.l{i}.b']
+        if i != n - 1:
+            h = torch.relu(h)
+    return torch.sigmoid(h)
+
+
+# ---------------------------------------------------------------------------
+# rendering
+
+def intersect_with_sphere(center, ray_unit, radius=1.0):
+    """nerf_util.py:199-205."""
+    ctc = (center * center).sum(dim=-1, keepdim=True)
+    ctv = (center * ray_unit).sum(dim=-1, keepdim=True)
+    b2_minus_4ac = ctv ** 2 - (ctc - radius ** 2)
+    return -ctv - b2_minus_4ac.sqrt(), -ctv + b2_minus_4ac.sqrt()
+
+
+def dist_bounds(center, ray_unit):
+    """Model.get_dist_bounds (model.py:207-213): near.relu_(); misses get near=1, far=1.2."""
+    near, far = intersect_with_sphere(center, ray_unit)
+    near = near.clamp(min=0)
+    outside = near.isnan()
+    near = torch.where(outside, torch.ones_like(near), near)
+    far = torch.where(outside, torch.full_like(far, 1.2), far)
+    return near, far, outside
+
+
+def iter_cos(true_cos, progress, anneal_end):
+    """Model._get_iter_cos (model.py:294-298)."""
+    a = min(progress / anneal_end, 1.0)
+    return -(torch.relu(-true_cos * 0.5 + 0.5) * (1.0 - a) + torch.relu(-true_cos) * a)
+
+
+def neus_alphas(ray_unit, sdfs, grads, dists, far, s_var, progress, anneal_end, eps=1e-5):
+    """Model.compute_neus_alphas (model.py:275-292).
+    ray_unit [R,3], sdfs [R,N], grads [R,N,3], dists [R,N], far [R,1] -> alphas [R,N]."""
+    inv_s = s_var.exp()
+    true_cos = (ray_unit[:, None, :] * grads).sum(dim=-1)
+    ic = iter_cos(true_cos, progress, anneal_end)
+    d = torch.cat([dists, far], dim=1)
+    intv = d[:, 1:] - d[:, :-1]
+    est_prev = sdfs - ic * intv * 0.5
+    est_next = sdfs + ic * intv * 0.5
+    prev_cdf = torch.sigmoid(est_prev * inv_s)
+    next_cdf = torch.sigmoid(est_next * inv_s)
+    return ((prev_cdf - next_cdf) / (prev_cdf + eps)).clamp(0.0, 1.0)
+
+
+def compositing_weights(alphas):
+    """render.alpha_compositing_weights (render.py:87-99): w_i = a_i * prod_{j<i}(1 - a_j)."""
+    front = torch.cat([torch.zeros_like(alphas[:, :1]), alphas[:, :-1]], dim=1)
+    return alphas * torch.cumprod(1 - front, dim=1)
+
+
+def eikonal_loss(grads, outside):
+    """misc.py:74-80 (mean over every sample, outside rays contribute 0)."""
+    err = ((grads.norm(dim=-1) - 1.0) ** 2).nan_to_num(nan=0.0, posinf=0.0, neginf=0.0)
+    return (err * (~outside).to(err.dtype)).mean()
+
+
+def curvature_loss(hess, outside):
+    """misc.py:83-89."""
+    lap = hess.sum(dim=-1).abs().nan_to_num(nan=0.0, posinf=0.0, neginf=0.0)
+    return (lap * (~outside).to(lap.dtype)).mean()
+
+
+def render_step(p, cfg, layout, batch, eps, progress, w_eik, w_curv, training=True):
+    """One training forward of Model.render_rays_object + render_rays + Trainer._compute_loss
+    (model.py:124-190, trainer.py:40-52), background disabled.
+
+    batch: center [R,3], ray_unit [R,3], dists [R,N], far [R,1], outside [R,1] (bool),
+           target [R,3], app_idx [R] (or None).  Returns a dict of outputs incl. 'loss'.
+    """
+    c, d, dists = batch['center'], batch['ray_unit'], batch['dists']
+    R, N = dists.shape
+    pts = c[:, None, :] + d[:, None, :] * dists[..., None]                # camera.py:314-320
+    sdf, feat = neural_sdf(p, cfg, layout, pts, with_feat=True)
+    outside = batch['outside']
+    out_val = 1000.0 * (-1 if cfg['inside_out'] else 1)                   # model.py:33
+    sdf = torch.where(outside[:, None, :].expand_as(sdf), torch.full_like(sdf, out_val), sdf)  # model.py:163
+    grads, hess = compute_gradients(p, cfg, layout, pts, eps, sdf, training)
+    normals = F.normalize(grads, dim=-1)
+    rays = d[:, None, :].expand_as(pts)
+    app = None
+    if cfg['app_dim'] > 0:
+        app = p['app'][batch['app_idx']][:, None, :].expand(R, N, cfg['app_dim'])
+    rgbs = neural_rgb(p, cfg, pts, normals, rays, feat, app)
+    alphas = neus_alphas(d, sdf[..., 0], grads, dists, batch['far'], p['s_var'], progress, cfg['anneal_end'])
+    weights = compositing_weights(alphas)
+    rgb = (rgbs * weights[..., None]).sum(dim=1)
+    l_render = (rgb - batch['target']).abs().mean() * 3.0                  # trainer.py:43
+    out_mask = outside.expand(R, N)
+    l_eik = eikonal_loss(grads, out_mask)
+    loss = l_render + w_eik * l_eik
+    l_curv = None
+    if hess is not None and w_curv:
+        l_curv = curvature_loss(hess, out_mask)
+        loss = loss + w_curv * l_curv
+    return dict(loss=loss, l_render=l_render, l_eik=l_eik, l_curv=l_curv, rgb=rgb, rgbs=rgbs,
+                sdf=sdf[..., 0], feat=feat, grads=grads, hess=hess, alphas=alphas, weights=weights)
