@@ -1,0 +1,330 @@
+"""Benchmark: SDF samples/s for one training forward+backward of the full neural-SDF
+field (16 levels x 8 features, T=2^22, 32->2048, 8 levels active; SDF MLP 256;
+colour MLP 4x256 with a 16-dim appearance embedding over 100 images) on
+16384 rays x 128 samples, seeded synthetic rays and colours.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--mode fused|plain]
+
+Prints ONE JSON line (rank 0).  ``value`` is the device-resident throughput of
+the selected mode (default: the fused path when built, else the plain FP32
+drop-in), ``e2e`` the same step through the public API with the batch copied
+from pinned host memory and the loss read back every step.  Under torchrun
+every rank runs an independent replica (the path has no exchange step on one
+node in this build: replicas only) and ``value`` sums the ranks' samples over
+the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+R_RAYS, N_SAMPLES, ACTIVE = 16384, 128, 8
+METRIC = "SDF samples/s fwd+bwd (full field, 16384 rays x 128 samples)"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--mode", default="auto", choices=["auto", "fused", "plain"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-plain", action="store_true", help="skip the plain FP32 denominator (profiling runs)")
+    p.add_argument("--rays", type=int, default=R_RAYS)
+    p.add_argument("--samples", type=int, default=N_SAMPLES)
+    return p.parse_args()
+
+
+# --------------------------------------------------------------------------- CPU baseline
+
+def cpu_port_sample(rays=64, samples=N_SAMPLES, steps=1, warmup=1):
+    """Time the CPU restatement of the reference path (oracle, float32 torch on the
+    host cores + numpy hash grid) on a bounded sample of the same workload."""
+    import torch
+    from oracle import field as of
+    from neuralangelo_gb300.workloads import full_field_iteration, make_rays
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    cfg = of.make_config(active_levels=ACTIVE, app_dim=16, n_images=100)
+    params, layout = of.init_params(cfg, seed=0, dtype=torch.float32)
+    params = {k: v.requires_grad_(True) for k, v in params.items()}
+    b = make_rays(rays, samples, seed=0, n_images=100)
+    it = full_field_iteration(ACTIVE)
+    eps = of.normal_eps(cfg, ACTIVE)
+    w_curv = 5e-4 / (cfg['per_level_scale'] ** (ACTIVE - 1))
+    times = []
+    for i in range(warmup + steps):
+        t0 = time.perf_counter()
+        out = of.render_step(params, cfg, layout, b, eps, it / 500000, 0.1, w_curv)
+        out['loss'].backward()
+        dt = time.perf_counter() - t0
+        if i >= warmup:
+            times.append(dt)
+        for v in params.values():
+            v.grad = None
+    t = statistics.median(times)
+    return dict(value=rays * samples / t, unit="samples/s", cores=threads, kind="port",
+                sample=f"{rays} rays x {samples} samples of the same field, float32, oracle restatement "
+                       f"(torch CPU + numpy hash grid), median of {steps} after {warmup} warm-up",
+                seconds_per_step=t)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cb = cpu_port_sample(steps=max(1, min(args.steps, 3)), warmup=1)
+    line = dict(metric=METRIC, value=cb["value"], unit="samples/s", n_gpus=args.gpus, steps=args.steps,
+                warmup=args.warmup, ms_per_step=cb["seconds_per_step"] * 1e3, higher_is_better=True,
+                scaling="weak", vs_baseline=None, dtype="f32", data="synthetic",
+                config=dict(workload="full field, 16384 rays x 128 samples (CPU sample: 64 rays)",
+                            parallelism="host cores"),
+                impl="reference", cpu_baseline=cb,
+                e2e=dict(value=cb["value"], unit="samples/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------- clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f".clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        if not sm:
+            return None
+        return dict(sm_mhz=statistics.median(sm), sm_max_mhz=max(mx), reasons=sorted(reasons), samples=len(sm))
+
+
+# --------------------------------------------------------------------------- GPU arm
+
+def make_plain(device, seed=0):
+    import torch
+    from neuralangelo_gb300.config import field_config
+    from neuralangelo_gb300.model import FieldModel
+    from neuralangelo_gb300.workloads import full_field_iteration, init_field_params
+    torch.manual_seed(seed)
+    model = FieldModel(field_config("full")).to(device)
+    init_field_params(model, seed)
+    model.schedule(full_field_iteration(ACTIVE))
+    assert model.neural_sdf.active_levels == ACTIVE
+    return model
+
+
+def step_plain(model, batch):
+    model.zero_grad(set_to_none=True)
+    out = model.render_step(batch)
+    out["loss"].backward()
+    return out["loss"]
+
+
+def time_steps(fn, steps, warmup, barrier):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    barrier()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    barrier()
+    return a.elapsed_time(b) / steps
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    device = f"cuda:{local}"
+    torch.cuda.set_device(device)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t)
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from neuralangelo_gb300 import _lib
+    from neuralangelo_gb300.workloads import encoder_bytes_per_sample, flops_per_sample, make_rays
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    R, N = args.rays, args.samples
+    n_samples = R * N
+    host_batch = make_rays(R, N, seed=rank, n_images=100)
+    batch = {k: v.to(device) for k, v in host_batch.items()}
+    pinned = {k: v.pin_memory() for k, v in host_batch.items()}
+    h2d = sum(v.numel() * v.element_size() for v in pinned.values())
+
+    model = make_plain(device)
+    fused = None
+    if args.mode in ("auto", "fused"):
+        from neuralangelo_gb300.fused import FusedField
+        fused = FusedField(model)
+    mode = "fused" if fused is not None else "plain"
+
+    def step_fused(b, compute_loss=False):
+        model.zero_grad(set_to_none=True)
+        return fused.step(b, compute_loss=compute_loss)
+
+    def measure(fn, steps, warmup):
+        _lib.TIMER.reset()
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        _lib.TIMER.enabled = True
+        ms_ = time_steps(fn, steps, 0, barrier)
+        _lib.TIMER.enabled = False
+        torch.cuda.synchronize()
+        return ms_, _lib.TIMER.summary()
+
+    # the plain FP32 drop-in (the denominator of the fused speed-up)
+    plain_ms = float("nan")
+    if not args.no_plain or fused is None:
+        plain_ms, plain_k = measure(lambda: step_plain(model, batch), max(2, args.steps // 2), args.warmup)
+        plain_ms = max_over_ranks(plain_ms)
+    clocks = ClockSampler(local)
+    clocks.start()
+    if fused is not None:
+        ms, ksum = measure(lambda: step_fused(batch), args.steps, args.warmup)
+    else:
+        ms, ksum = measure(lambda: step_plain(model, batch), args.steps, args.warmup)
+    clock = clocks.stop()
+    ms = max_over_ranks(ms)
+    value = world * n_samples / (ms * 1e-3)
+
+    # end to end through the public API: H2D of the batch, step, D2H of the loss
+    def e2e_step():
+        b = {k: v.to(device, non_blocking=True) for k, v in pinned.items()}
+        if fused is not None:
+            return step_fused(b, compute_loss=True)["loss"]
+        return float(step_plain(model, b).detach().cpu())
+
+    e2e_ms = time_steps(e2e_step, max(1, args.steps // 2), 1, barrier)
+    e2e_ms = max_over_ranks(e2e_ms)
+
+    # per-kernel algorithmic work (bytes, flops) of one launch, for the roofline
+    F, A, H = 8, ACTIVE, 256
+    enc_read = A * 8 * F * (2 if mode == "fused" else 4)
+    work = {
+        "gbsdf_hashgrid_fwd": (n_samples * (A * 8 * F * 4 + 16 * F * 4 + 12), 0),
+        "gbsdf_hashgrid_bwd": (n_samples * (A * 8 * F * 8 + 16 * F * 4), 0),
+        "gbsdf_field_fwd": (n_samples * (7 * enc_read + H * 2 + 48 * 2 + 28 + 12), n_samples * 7 * 2 * 64 * H),
+        "gbsdf_field_bwd": (n_samples * (7 * enc_read + 7 * A * 8 * F * 8 + 7 * H * 2 + 7 * 80 * 2 + H * 2 + 64 + 64),
+                            n_samples * 7 * 3 * 2 * 64 * H),
+    }
+    dom = max(ksum.items(), key=lambda kv: kv[1][1]) if ksum else None
+    roof = None
+    if dom is not None:
+        name, (calls, tot_ms) = dom
+        per_launch_ms = tot_ms / calls
+        if name in work:
+            by, fl = work[name]
+            ach = by / (per_launch_ms * 1e-3) / 1e9
+            roof = dict(kernel=name, bound="hbm", achieved=round(ach, 1), peak=hbm_peak, unit="GB/s",
+                        frac=round(ach / hbm_peak, 4), traffic=None, per_launch_ms=round(per_launch_ms, 4),
+                        algorithmic_bytes_per_launch=by, flops_per_launch=fl,
+                        tensor_tflops=round(fl / (per_launch_ms * 1e-3) / 1e12, 2),
+                        launches_per_step=calls / args.steps,
+                        peak_source="MEASURED_PEAKS.json hbm_gbs (burst, of measured)")
+    launches = int(sum(c for c, _ in ksum.values()) / args.steps)
+    cb = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = cpu_port_sample()
+        cb.pop("seconds_per_step", None)
+    if rank == 0:
+        line = dict(metric=METRIC, value=round(value, 1), unit="samples/s", n_gpus=world, steps=args.steps,
+                    warmup=args.warmup, ms_per_step=round(ms, 3), higher_is_better=True, scaling="weak",
+                    vs_baseline=None, dtype="f32" if mode == "plain" else "f16", data="synthetic",
+                    plain_fp32=(dict(value=round(world * n_samples / (plain_ms * 1e-3), 1), unit="samples/s",
+                                     ms_per_step=round(plain_ms, 3)) if plain_ms == plain_ms else None),
+                    speedup_vs_plain=round(plain_ms / ms, 3) if plain_ms == plain_ms else None,
+                    config=dict(workload=f"full field L16 F8 T2^22 (8 active), {R} rays x {N} samples, mode={mode}",
+                                rays=R, samples_per_ray=N, active_levels=ACTIVE, mode=mode,
+                                l2="inputs larger than L2 (1.46 GB table)", parallelism="replicas"),
+                    e2e=dict(value=round(world * n_samples / (e2e_ms * 1e-3), 1), unit="samples/s",
+                             h2d_bytes_per_step=h2d, d2h_bytes_per_step=32 if fused is not None else 4,
+                             ms_per_step=round(e2e_ms, 3)),
+                    roofline=roof, cpu_baseline=cb, gpu_launches=launches, clocks=clock,
+                    flops_per_sample=flops_per_sample(model.cfg, ACTIVE),
+                    encoder_bytes_per_sample=encoder_bytes_per_sample(ACTIVE, 8, 4),
+                    kernel_ms_per_step={k: round(v[1] / args.steps, 4) for k, v in ksum.items()})
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

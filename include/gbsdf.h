@@ -1,0 +1,261 @@
+/*
+ * gbsdf -- C ABI of the GB300 (sm_103a) neural-SDF field and volume-rendering path.
+ *
+ * Every entry point takes plain pointers to DEVICE memory (unless stated),
+ * element counts, and the CUDA stream to run on (passed as void*; NULL = the
+ * legacy default stream).  Nothing synchronises implicitly; nothing allocates
+ * device memory: scratch buffers are passed in by the caller and their sizes are
+ * reported by the *_workspace_size() queries.  Every call returns a status
+ * (GBSDF_OK = 0); gbsdf_last_error() returns a thread-local message for the
+ * last failing call on the calling thread.  Exceptions never cross this ABI.
+ *
+ * Reference interfaces replaced (paths inside NVlabs/neuralangelo):
+ *   hash grid ............ tcnn.Encoding(3, {"otype": "HashGrid", ...})
+ *                          projects/neuralangelo/utils/modules.py:42-50 (built), :84-86 (called)
+ *   NeuS alpha ........... Model.compute_neus_alphas  projects/neuralangelo/model.py:275-298
+ *   compositing .......... render.alpha_compositing_weights / composite
+ *                          projects/nerf/utils/render.py:87-112
+ *   fused field step ..... NeuralSDF.forward + compute_gradients + NeuralRGB.forward +
+ *                          compute_neus_alphas + compositing + Trainer._compute_loss and
+ *                          their autograd backward (modules.py:68-220, model.py:158-190,
+ *                          trainer.py:40-52, misc.py:74-89)
+ *   lattice SDF + MC ..... extract_mesh / LatticeGrid / marching_cubes
+ *                          projects/neuralangelo/utils/mesh.py:25-49, 68-101, 119-133
+ *   importance sampler ... Model.sample_dists_hierarchical + nerf_util.sample_dists_from_pdf
+ *                          projects/neuralangelo/model.py:250-267, projects/nerf/utils/nerf_util.py:41-68
+ */
+#ifndef GBSDF_H
+#define GBSDF_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBSDF_OK               0
+#define GBSDF_ERR_ARG          1   /* bad pointer, size, stride or alignment */
+#define GBSDF_ERR_UNSUPPORTED  2   /* configuration the kernels are not built for */
+#define GBSDF_ERR_CUDA         3   /* a CUDA runtime call failed */
+#define GBSDF_ERR_TIMEOUT      4   /* a bounded device-side wait ran out */
+
+#define GBSDF_MAX_LEVELS 32
+
+#define GBSDF_F32 0
+#define GBSDF_F16 1
+
+/* Level table of a multi-resolution hash grid (tcnn "HashGrid" semantics).
+ * Filled by gbsdf_grid_init; read-only for every other call. */
+typedef struct gbsdf_grid {
+    int32_t  n_levels;            /* L */
+    int32_t  n_features;          /* F: 1, 2, 4 or 8 */
+    int32_t  log2_hashmap_size;   /* T = 2^log2_hashmap_size entries max per level */
+    int32_t  base_resolution;
+    float    per_level_scale;
+    float    scale[GBSDF_MAX_LEVELS];        /* position scale of each level */
+    uint32_t resolution[GBSDF_MAX_LEVELS];   /* grid points per axis */
+    uint32_t size[GBSDF_MAX_LEVELS];         /* entries in the level */
+    uint32_t hashed[GBSDF_MAX_LEVELS];       /* 1 = spatial hash, 0 = dense */
+    uint64_t offset[GBSDF_MAX_LEVELS + 1];   /* first entry of each level; offset[L] = total */
+} gbsdf_grid;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int gbsdf_version(void);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* gbsdf_last_error(void);
+
+/* Number of CUDA devices visible (0 without a GPU); never fails. */
+int gbsdf_device_count(void);
+
+/* Fill a level table.  Replaces the level setup inside tcnn's GridEncoding that
+ * modules.py:42-50 configures (n_levels, n_features_per_level,
+ * log2_hashmap_size, base_resolution, per_level_scale).  Host-only. */
+int gbsdf_grid_init(gbsdf_grid* grid, int n_levels, int n_features, int log2_hashmap_size,
+                    int base_resolution, float per_level_scale);
+
+/* Hash-grid forward.  Replaces tcnn.Encoding.forward (modules.py:85).
+ * x       [M,3] float32 positions in grid units [0,1] (modules.py:82-83)
+ * table   [offset[L], F] entries, dtype GBSDF_F32 or GBSDF_F16
+ * out     [M, L*F] level-major, dtype out_dtype; levels >= active_levels are
+ *         written as 0 (the coarse-to-fine mask of modules.py:91-93). */
+int gbsdf_hashgrid_fwd(const gbsdf_grid* grid, int active_levels, const float* x, int64_t M,
+                       const void* table, int table_dtype, void* out, int out_dtype, void* stream);
+
+/* Hash-grid backward.  Replaces the autograd backward of tcnn.Encoding
+ * (the dL/dparams path; numerical-gradient mode never needs dL/dx).
+ * d_out   [M, L*F] float32 ; d_table [offset[L], F] float32, ACCUMULATED into. */
+int gbsdf_hashgrid_bwd(const gbsdf_grid* grid, int active_levels, const float* x, int64_t M,
+                       const float* d_out, float* d_table, void* stream);
+
+/* Absolute entry index of each (point, active level, corner), int64 [M, A, 8].
+ * Exposes the index computation for bit-exact parity checks. */
+int gbsdf_hashgrid_indices(const gbsdf_grid* grid, int active_levels, const float* x, int64_t M,
+                           int64_t* indices, void* stream);
+
+/* NeuS alpha, forward.  Replaces Model.compute_neus_alphas (model.py:275-292)
+ * with _get_iter_cos (model.py:294-298).
+ * ray_unit [R,3], sdf [R,N], grad [R,N,3], dists [R,N], far [R] (float32);
+ * s_var: device pointer to the scalar log inverse standard deviation (model.py:64);
+ * alpha [R,N] out. */
+int gbsdf_neus_alpha_fwd(int64_t R, int64_t N, const float* ray_unit, const float* sdf, const float* grad,
+                         const float* dists, const float* far, const float* s_var, float progress,
+                         float anneal_end, float* alpha, void* stream);
+
+/* NeuS alpha, backward: d_alpha [R,N] -> d_sdf [R,N], d_grad [R,N,3] (written),
+ * d_s_var [1] (accumulated). */
+int gbsdf_neus_alpha_bwd(int64_t R, int64_t N, const float* ray_unit, const float* sdf, const float* grad,
+                         const float* dists, const float* far, const float* s_var, float progress,
+                         float anneal_end, const float* d_alpha, float* d_sdf, float* d_grad, float* d_s_var,
+                         void* stream);
+
+/* Compositing weights w_i = a_i * prod_{j<i}(1-a_j), forward, FP32 log-space
+ * transmittance.  Replaces render.alpha_compositing_weights (render.py:87-99).
+ * alpha [R,N] -> weights [R,N]. */
+int gbsdf_composite_weights_fwd(int64_t R, int64_t N, const float* alpha, float* weights, void* stream);
+
+/* Backward of the compositing weights: d_weights [R,N] -> d_alpha [R,N]. */
+int gbsdf_composite_weights_bwd(int64_t R, int64_t N, const float* alpha, const float* d_weights,
+                                float* d_alpha, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Fused dense layer on the tcgen05 tensor cores (fp16 operands, fp32 accumulate):
+ *     Y[:, 0:N] = epi(X[:, 0:K] * W^T + bias ; G)
+ * Replaces one torch.nn.Linear + activation of the SDF feature layer
+ * (projects/neuralangelo/utils/mlp.py:55-69) and of the colour MLP
+ * (projects/nerf/utils/nerf_util.py:187-196), forward or input-gradient:
+ *   epi 0 identity, 1 relu, 2 softplus(beta)           (forward; bias added)
+ *   epi 3 acc*[G>0], 4 acc*(1-exp(-beta*G))             (backward through the
+ *         previous layer's activation; G = its stored output; bias ignored)
+ * X [M, ldx] fp16, W [N, K] fp16 row-major, bias [N] fp32 (may be NULL),
+ * G [M, ldg] fp16, Y [M, ldy] fp16 (fp32 when y_f32 != 0).  K % 16 == 0,
+ * K <= 320, N % 64 == 0, ldx/ldg/ldy % 8 == 0, 16-byte aligned bases.  err:
+ * optional device int set non-zero when a bounded device wait runs out. */
+int gbsdf_dense(int64_t M, int K, int N, const void* X, int ldx, const void* W, const float* bias,
+                const void* G, int ldg, void* Y, int ldy, int y_f32, int epi, float beta, int* err, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Fused SDF field (hash grid + SDF layer 0 + head + 6 numerical-gradient taps).
+ * Replaces NeuralSDF.forward / compute_gradients (modules.py:68-95, 131-156),
+ * MLPforNeuralSDF layer 0 and head (mlp.py:55-69), the outside overwrite
+ * (model.py:163) and builds NeuralRGB's input tail (modules.py:209-213).
+ * Samples are a flat array; ray of sample s = s / S (S > 0) or sample_ray[s].
+ * fp16 tensors are passed as void*.  Field meanings are documented in
+ * neuralangelo_gb300/csrc/field.cu. */
+typedef struct gbsdf_field_args {
+    int64_t Ns;
+    int32_t S;
+    int32_t pad0;
+    const int32_t* sample_ray;
+    const float* center;
+    const float* ray_unit;
+    const float* dists;
+    const uint8_t* outside;
+    const int32_t* app_idx;
+    gbsdf_grid grid;
+    int32_t active;
+    int32_t K0;
+    const void* table;       /* fp16 [entries, F] */
+    const void* w0e;         /* fp16 [256, K0] */
+    const void* w0eT;        /* fp16 [K0, 256] */
+    const float* w0x;        /* [256, 3] */
+    const float* b0;         /* [256] */
+    const float* whead;      /* [256] */
+    const float* bhead;      /* [1] */
+    float beta, eps, two_eps, eps2, outside_val;
+    int32_t pad1;
+    void* xc;                /* fp16 [Ns, ldxc] colour input; columns >= 256 written by the forward */
+    int32_t ldxc;
+    int32_t app_dim;
+    const float* app_table;  /* [n_images, app_dim] */
+    float* sdf;              /* [Ns] */
+    float* grad;             /* [Ns, 3] */
+    float* hess;             /* [Ns, 3] */
+    void* h0c;               /* fp16 [Ns, 256] */
+    const float* d_sdf;      /* [Ns]    backward inputs, loss-scaled */
+    const float* d_grad;     /* [Ns, 3] */
+    const float* d_hess;     /* [Ns, 3] */
+    const float* d_xc;       /* [Ns, ld_dxc] gradient of the colour-input tail */
+    int32_t ld_dxc;
+    int32_t normal_col;
+    const float* d_h0c;      /* [Ns, 256] gradient of the centre layer-0 activation */
+    float* d_table;          /* [entries, F] accumulated */
+    void* d_pre0;            /* fp16 [7 Ns, 256] */
+    void* x0ext;             /* fp16 [7 Ns, K0 + 16] */
+    float* d_whead;          /* [256] accumulated */
+    float* d_bhead;          /* [1] accumulated */
+    int32_t* err;            /* device flag for timed-out waits */
+} gbsdf_field_args;
+
+size_t gbsdf_field_args_size(void);
+int gbsdf_field_fwd(const gbsdf_field_args* args, void* stream);
+int gbsdf_field_bwd(const gbsdf_field_args* args, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Fused per-ray rendering forward + backward: NeuS alpha (model.py:275-298),
+ * FP32 log-space transmittance and compositing (render.py:87-112), the L1
+ * colour, eikonal and curvature losses (trainer.py:40-52, misc.py:74-89) and
+ * their gradients with respect to every per-sample input, one warp per ray.
+ * Ray r owns samples [ray_offsets[r], ray_offsets[r+1]) (or [r S, r S + S)). */
+typedef struct gbsdf_render_args {
+    int64_t R;
+    int32_t S;
+    int32_t pad0;
+    const int64_t* ray_offsets;  /* [R + 1] when S == 0 */
+    const float* ray_unit;       /* [R, 3] */
+    const float* dists;          /* [Ns] */
+    const float* far;            /* [R] */
+    const uint8_t* outside;      /* [R] */
+    const float* target;         /* [R, 3] */
+    const float* s_var;          /* [1] */
+    const float* sdf;            /* [Ns] */
+    const float* grad;           /* [Ns, 3] */
+    const float* hess;           /* [Ns, 3] */
+    const float* rgbs;           /* [Ns, 3] */
+    float anneal;                /* min(progress / anneal_end, 1) */
+    float w_render, w_eik, w_curv;
+    float l1_scale;              /* d L1 / d rgb = l1_scale * sign (3 / (3 R) for the reference) */
+    float mean_scale;            /* 1 / (number of samples in the eikonal/curvature means) */
+    float loss_scale;            /* multiplies every gradient output */
+    int32_t pad1;
+    float* rgb;                  /* [R, 3] out */
+    float* weights;              /* [Ns] out (may be NULL) */
+    float* d_rgbs;               /* [Ns, 3] out */
+    float* d_sdf;                /* [Ns] out */
+    float* d_grad;               /* [Ns, 3] out */
+    float* d_hess;               /* [Ns, 3] out */
+    float* d_s_var;              /* [1] accumulated */
+    double* loss_sums;           /* [4] accumulated: l1 sum, eikonal sum, curvature sum, (unused) */
+    int32_t* err;                /* device flag: 2 = a ray longer than 512 samples was skipped */
+} gbsdf_render_args;
+
+size_t gbsdf_render_args_size(void);
+int gbsdf_render_fused(const gbsdf_render_args* args, void* stream);
+
+/* Last colour layer (H -> 3, sigmoid) forward: rgbs = sigmoid(Y W^T + b).
+ * Replaces the last Linear + sigmoid of NeuralRGB (modules.py:215, nerf_util.py:187-196).
+ * Y fp16 [Ns, ldy] (hidden width H <= 256, H % 8 == 0), W [3, H] fp32, b [3]. */
+int gbsdf_rgb_head_fwd(int64_t Ns, const void* Y, int ldy, int H, const float* W, const float* b, float* rgbs,
+                       void* stream);
+
+/* Its backward: d_rgbs [Ns,3] -> d_pre [Ns, 8] fp16 (columns 0-2, rest 0),
+ * dZ = (d_pre W) * [Y > 0] fp16 [Ns, H], d_b [3] accumulated. */
+int gbsdf_rgb_head_bwd(int64_t Ns, const void* Y, int ldy, int H, const float* W, const float* rgbs,
+                       const float* d_rgbs, void* d_pre, void* dZ, float* d_b, void* stream);
+
+/* Appearance-embedding gradient: d_app[app_idx[r]] += sum over ray r's samples of
+ * d_xc[s, col0 : col0 + app_dim] (fp32). */
+int gbsdf_app_grad(int64_t R, int32_t S, const int64_t* ray_offsets, const int32_t* app_idx, const void* d_xc,
+                   int ld_dxc, int col0, int app_dim, float* d_app, void* stream);
+
+/* Weight gradient dW [N, K] = alpha * dZ[M, N]^T X[M, K] + beta * dW (fp16 in,
+ * fp32 out; cuBLAS).  dW of every MLP layer of the fused step. */
+int gbsdf_gemm_wgrad(int64_t M, int N, int K, const void* dZ, int ldz, const void* X, int ldx, float* dW,
+                     int ldw, float alpha, float beta, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBSDF_H */

@@ -1,0 +1,106 @@
+// Shared device helpers for the gbsdf kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "../../include/gbsdf.h"
+
+namespace gbsdf {
+
+// ---------------------------------------------------------------------------
+// error reporting (thread-local message, defined in capi.cu)
+void set_error(const char* fmt, ...);
+void clear_error();
+
+#define GBSDF_CHECK_ARG(cond, ...)            \
+    do {                                      \
+        if (!(cond)) {                        \
+            ::gbsdf::set_error(__VA_ARGS__);  \
+            return GBSDF_ERR_ARG;             \
+        }                                     \
+    } while (0)
+
+int launch_status(const char* what);   // checks cudaGetLastError after a launch
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+
+// ---------------------------------------------------------------------------
+// hash-grid level arithmetic, shared by every kernel that evaluates the field.
+// Follows tiny-cuda-nn's HashGrid (the encoder behind modules.py:42-50):
+// position p = fma(scale, x, 0.5); corner = floor(p); frac = p - corner; the
+// corner index is dense (x + y*res + z*res^2) or the XOR prime hash, modulo the
+// level size.  The per-level scale arrives precomputed in gbsdf_grid.scale.
+
+struct LevelDesc {
+    float scale;
+    uint32_t res;
+    uint32_t size;
+    uint32_t hashed;
+    uint64_t offset;
+};
+
+__device__ __forceinline__ LevelDesc level_desc(const gbsdf_grid& g, int l) {
+    LevelDesc d;
+    d.scale = g.scale[l];
+    d.res = g.resolution[l];
+    d.size = g.size[l];
+    d.hashed = g.hashed[l];
+    d.offset = g.offset[l];
+    return d;
+}
+
+__device__ __forceinline__ void grid_pos(float scale, float x, uint32_t& base, float& frac) {
+    const float p = __fmaf_rn(scale, x, 0.5f);
+    const float f = floorf(p);
+    base = (uint32_t)(int)f;
+    frac = __fsub_rn(p, f);
+}
+
+__device__ __forceinline__ uint32_t grid_index(const LevelDesc& d, uint32_t cx, uint32_t cy, uint32_t cz) {
+    uint32_t idx;
+    if (d.hashed) {
+        idx = (cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u);
+    } else {
+        idx = cx + cy * d.res + cz * (d.res * d.res);
+    }
+    return idx % d.size;
+}
+
+// Corner c (0..7) selects +1 in dimension d when bit d of c is set.
+__device__ __forceinline__ float corner_weight(int c, float fx, float fy, float fz) {
+    const float wx = (c & 1) ? fx : __fsub_rn(1.0f, fx);
+    const float wy = (c & 2) ? fy : __fsub_rn(1.0f, fy);
+    const float wz = (c & 4) ? fz : __fsub_rn(1.0f, fz);
+    return __fmul_rn(__fmul_rn(wx, wy), wz);
+}
+
+// Normalisation of a world point into the grid's unit cube, as NeuralSDF.encode
+// does it (modules.py:82-83): (p - vmin) / (vmax - vmin) with range [-2, 2].
+__device__ __forceinline__ float to_unit(float p) { return __fmul_rn(__fadd_rn(p, 2.0f), 0.25f); }
+
+// ---------------------------------------------------------------------------
+// numerics shared with the reference's activations
+
+// torch.nn.functional.softplus(x, beta, threshold=20)
+__device__ __forceinline__ float softplus_beta(float x, float beta) {
+    const float bx = x * beta;
+    return bx > 20.0f ? x : log1pf(expf(bx)) / beta;
+}
+// d softplus / dx = sigmoid(beta*x) (1 above the threshold)
+__device__ __forceinline__ float softplus_grad(float x, float beta) {
+    const float bx = x * beta;
+    return bx > 20.0f ? 1.0f : 1.0f / (1.0f + expf(-bx));
+}
+__device__ __forceinline__ float sigmoidf_(float x) { return 1.0f / (1.0f + expf(-x)); }
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace gbsdf

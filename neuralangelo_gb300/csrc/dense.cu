@@ -1,0 +1,213 @@
+// Generic fused dense layer on tcgen05:  Y = epi(X * W^T + b ; G)
+//
+// Forward layers:  epi = relu / softplus(beta) / identity
+// Backward (dX):   X = dZ, W = W^T of the forward layer, epi multiplies by the
+//                  derivative of the previous layer's activation read from G
+//                  (G = that layer's stored output): relu' = [G > 0],
+//                  softplus' = 1 - exp(-beta G).
+// These are the colour-MLP layers of NeuralRGB (projects/neuralangelo/utils/
+// modules.py:199-220 via projects/nerf/utils/nerf_util.py:158-196) and the SDF
+// feature layer (utils/mlp.py:55-69), forward and input-gradient.
+#include "dense.cuh"
+
+namespace gbsdf {
+
+enum DenseEpi : int {
+    EPI_IDENTITY = 0,
+    EPI_RELU = 1,
+    EPI_SOFTPLUS = 2,
+    EPI_DRELU = 3,      // y = acc * [G > 0]
+    EPI_DSOFTPLUS = 4,  // y = acc * (1 - exp(-beta * G))
+};
+
+struct DenseParams {
+    int64_t M;
+    int K;
+    int N_total;
+    int n_split;
+    const __half* X;
+    int ldx;
+    const __half* W;
+    const float* bias;
+    const __half* G;
+    int ldg;
+    void* Y;
+    int ldy;
+    int y_f32;
+    int epi;
+    float beta;
+    int* err;
+};
+
+template <int N_TILE>
+__global__ void __launch_bounds__(DENSE_THREADS, 1) k_dense(DenseParams p) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* w_s = smem;                                              // [N_TILE x K]
+    uint8_t* a_s = w_s + (size_t)N_TILE * p.K * 2;                    // [128 x K]
+    float* bias_s = reinterpret_cast<float*>(a_s + (size_t)TILE_M * p.K * 2);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(bias_s + N_TILE);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ns = blockIdx.x % p.n_split;
+    const int group = blockIdx.x / p.n_split, ngroups = gridDim.x / p.n_split;
+    const int n0 = ns * N_TILE;
+
+    // resident weight slice and bias
+    stage_rows_kmajor(w_s, p.W, n0, p.N_total, p.K, p.K, tid, DENSE_THREADS, N_TILE);
+    for (int i = tid; i < N_TILE; i += DENSE_THREADS) bias_s[i] = p.bias ? p.bias[n0 + i] : 0.0f;
+    if (tid == 0) {
+        umma::mbar_init(mbar, 1);
+        umma::fence_mbar_init();
+    }
+    if (warp == 0) {
+        umma::tmem_alloc(tslot, N_TILE);
+        umma::tmem_relinquish();
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint32_t idesc = umma::idesc_f16(TILE_M, N_TILE);
+    const uint32_t a_addr = umma::smem_u32(a_s), w_addr = umma::smem_u32(w_s);
+    const int64_t ntiles = (p.M + TILE_M - 1) / TILE_M;
+    uint32_t phase = 0;
+    bool ok = true;
+
+    const int q = warp & 3;                 // TMEM lane quadrant of this warp
+    const int half = warp >> 2;             // which half of the columns this warp reads
+    const int row = q * 32 + lane;
+    constexpr int COLS_PER_WARP = N_TILE / 2;
+
+    for (int64_t t = group; t < ntiles && ok; t += ngroups) {
+        const int64_t m0 = t * TILE_M;
+        stage_rows_kmajor(a_s, p.X, m0, p.M, p.ldx, p.K, tid, DENSE_THREADS);
+        cp_async_wait_all();
+        umma::fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            umma::fence_after_sync();
+            issue_tile_mma(tmem, a_addr, w_addr, p.K, idesc);
+            umma::mma_commit(mbar);
+        }
+        ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
+        phase ^= 1u;
+        if (!ok) {
+            flag_timeout(p.err, 1);
+            break;
+        }
+        umma::fence_after_sync();
+        const int64_t grow = m0 + row;
+        const bool live = grow < p.M;
+#pragma unroll 1
+        for (int c0 = half * COLS_PER_WARP; c0 < (half + 1) * COLS_PER_WARP; c0 += 32) {
+            float v[32];
+            umma::tmem_ld32(umma::taddr(tmem, q * 32, c0), v);
+            if (!live) continue;
+            if (p.epi == EPI_DRELU || p.epi == EPI_DSOFTPLUS) {
+                const __half* gp = p.G + grow * (int64_t)p.ldg + n0 + c0;
+#pragma unroll
+                for (int j = 0; j < 32; j += 8) {
+                    float g[8];
+                    load_half8(gp + j, g);
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const float d = (p.epi == EPI_DRELU) ? (g[i] > 0.0f ? 1.0f : 0.0f)
+                                                             : (1.0f - expf(-p.beta * g[i]));
+                        v[j + i] *= d;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const float z = v[j] + bias_s[c0 + j];
+                    v[j] = (p.epi == EPI_RELU) ? fmaxf(z, 0.0f) : (p.epi == EPI_SOFTPLUS) ? softplus_beta(z, p.beta) : z;
+                }
+            }
+            if (p.y_f32) {
+                float* yp = reinterpret_cast<float*>(p.Y) + grow * (int64_t)p.ldy + n0 + c0;
+#pragma unroll
+                for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4*>(yp + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+            } else {
+                __half* yp = reinterpret_cast<__half*>(p.Y) + grow * (int64_t)p.ldy + n0 + c0;
+#pragma unroll
+                for (int j = 0; j < 32; j += 8) store_half8(yp + j, v + j);
+            }
+        }
+        umma::fence_before_sync();
+        __syncthreads();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, N_TILE);
+}
+
+static int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <int N_TILE>
+static int launch_dense(const DenseParams& p, cudaStream_t s) {
+    const size_t smem = (size_t)N_TILE * p.K * 2 + (size_t)TILE_M * p.K * 2 + N_TILE * 4 + 16;
+    if (smem > 227 * 1024) {
+        set_error("dense layer K=%d N_TILE=%d needs %zu B of shared memory", p.K, N_TILE, smem);
+        return GBSDF_ERR_UNSUPPORTED;
+    }
+    cudaFuncSetAttribute(k_dense<N_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int64_t ntiles = (p.M + TILE_M - 1) / TILE_M;
+    int64_t groups = sm_count() / p.n_split;
+    if (groups < 1) groups = 1;
+    if (groups > ntiles) groups = ntiles;
+    k_dense<N_TILE><<<(unsigned)(groups * p.n_split), DENSE_THREADS, smem, s>>>(p);
+    return launch_status("dense");
+}
+
+int dense_launch(const DenseParams& p, int n_tile, cudaStream_t s) {
+    switch (n_tile) {
+        case 64: return launch_dense<64>(p, s);
+        case 128: return launch_dense<128>(p, s);
+        case 256: return launch_dense<256>(p, s);
+        default: set_error("unsupported n_tile %d", n_tile); return GBSDF_ERR_UNSUPPORTED;
+    }
+}
+
+}  // namespace gbsdf
+
+using namespace gbsdf;
+
+// Y[:, 0:N] = epi(X[:, 0:K] * W^T + b ; G), fp16 in/out, fp32 accumulate.
+// K multiple of 16 (<= 320), N multiple of 64; leading dimensions multiples of 8.
+extern "C" int gbsdf_dense(int64_t M, int K, int N, const void* X, int ldx, const void* W, const float* bias,
+                           const void* G, int ldg, void* Y, int ldy, int y_f32, int epi, float beta, int* err,
+                           void* stream) {
+    clear_error();
+    GBSDF_CHECK_ARG(M >= 0 && K > 0 && N > 0, "bad sizes");
+    if (M == 0) return GBSDF_OK;
+    GBSDF_CHECK_ARG(X && W && Y, "NULL pointer");
+    GBSDF_CHECK_ARG(K % 16 == 0 && K <= 320, "K=%d must be a multiple of 16 and <= 320", K);
+    GBSDF_CHECK_ARG(N % 64 == 0 && N <= 512, "N=%d must be a multiple of 64 and <= 512", N);
+    GBSDF_CHECK_ARG(ldx % 8 == 0 && ldy % 8 == 0 && ldx >= K && ldy >= N, "leading dimensions");
+    GBSDF_CHECK_ARG(aligned(X, 16) && aligned(W, 16) && aligned(Y, 16), "X, W, Y must be 16-byte aligned");
+    GBSDF_CHECK_ARG(epi >= 0 && epi <= 4, "bad epilogue %d", epi);
+    if (epi == EPI_DRELU || epi == EPI_DSOFTPLUS) {
+        GBSDF_CHECK_ARG(G != nullptr && ldg % 8 == 0 && ldg >= N && aligned(G, 16), "gate matrix G");
+    }
+    DenseParams p;
+    p.M = M; p.K = K; p.N_total = N;
+    p.X = (const __half*)X; p.ldx = ldx; p.W = (const __half*)W; p.bias = bias;
+    p.G = (const __half*)G; p.ldg = ldg; p.Y = Y; p.ldy = ldy; p.y_f32 = y_f32 ? 1 : 0; p.epi = epi; p.beta = beta;
+    p.err = err;
+    // largest N tile whose weight slice + A tile fit in shared memory
+    int n_tile = 256;
+    while (n_tile > 64 && ((size_t)n_tile * K * 2 + (size_t)TILE_M * K * 2 + 2048 > 227 * 1024 || N % n_tile != 0))
+        n_tile >>= 1;
+    p.n_split = N / n_tile;
+    return dense_launch(p, n_tile, as_stream(stream));
+}

@@ -1,0 +1,693 @@
+// Fused neural-SDF field kernels (hash grid + SDF layer 0 + head + numerical
+// gradient taps) on tcgen05, forward and backward.
+//
+// Reference path: NeuralSDF.forward / sdf / compute_gradients (6 taps)
+// (projects/neuralangelo/utils/modules.py:68-95, 131-156), MLPforNeuralSDF
+// layer 0 + SDF head (utils/mlp.py:55-69), the outside overwrite
+// (projects/neuralangelo/model.py:163) and the input of NeuralRGB
+// (modules.py:209-220: x, SH(view dir), normalize(gradient), feature, appearance).
+//
+// Tile = 18 samples x 7 evaluations (centre + 6 taps) = 126 rows (+2 zero rows)
+// of a 128-row tcgen05 tile.  Row r holds evaluation e = r / 18 of sample r % 18:
+// e = 0 centre, 1 +x, 2 -x, 3 +y, 4 -y, 5 +z, 6 -z.  The hash-grid features of
+// the active levels are gathered straight into the shared-memory A tile
+// (fp16, K-major core-matrix layout); W0's encoding columns are resident; the
+// three position columns, bias, softplus and the SDF head run in fp32 in the
+// epilogue, so SDF values and the tap differences keep fp32 accuracy.
+#include "dense.cuh"
+
+namespace gbsdf {
+
+constexpr int SPT = 18;          // samples per tile
+constexpr int EVALS = 7;
+constexpr int FIELD_THREADS = 256;
+constexpr int HID = 256;         // SDF hidden width (base.yaml:41)
+
+typedef gbsdf_field_args FieldParams;   // layout and field meanings: include/gbsdf.h
+
+__device__ __forceinline__ int ray_of(const FieldParams& p, int64_t s) {
+    return p.S > 0 ? (int)(s / p.S) : p.sample_ray[s];
+}
+
+// float32 centre point c + d t (camera.py:314-320: one multiply, one add)
+__device__ __forceinline__ void sample_point(const FieldParams& p, int64_t s, float* x) {
+    const int r = ray_of(p, s);
+    const float t = p.dists[s];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) x[i] = __fadd_rn(p.center[3 * r + i], __fmul_rn(p.ray_unit[3 * r + i], t));
+}
+
+// evaluation position: the reference adds a float32 [eps,0,0]-style vector (modules.py:135-143)
+__device__ __forceinline__ void eval_point(const float* c, int e, float eps, float* x) {
+    x[0] = c[0]; x[1] = c[1]; x[2] = c[2];
+    if (e > 0) {
+        const int d = (e - 1) >> 1;
+        x[d] = (e & 1) ? __fadd_rn(x[d], eps) : __fsub_rn(x[d], eps);
+    }
+}
+
+// Gather the active levels of one (row, level) pair into the A tile.
+template <int F>
+__device__ __forceinline__ void gather_level(const FieldParams& p, const float* xu, int l, float* out) {
+    const LevelDesc d = level_desc(p.grid, l);
+    uint32_t bx, by, bz;
+    float fx, fy, fz;
+    grid_pos(d.scale, xu[0], bx, fx);
+    grid_pos(d.scale, xu[1], by, fy);
+    grid_pos(d.scale, xu[2], bz, fz);
+#pragma unroll
+    for (int f = 0; f < F; ++f) out[f] = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const uint32_t idx = grid_index(d, bx + (c & 1), by + ((c >> 1) & 1), bz + ((c >> 2) & 1));
+        const float w = corner_weight(c, fx, fy, fz);
+        const __half* row = (const __half*)p.table + (d.offset + idx) * F;
+        float v[F];
+        if constexpr (F == 8) {
+            load_half8(row, v);
+        } else if constexpr (F == 4) {
+            const uint2 u = __ldg(reinterpret_cast<const uint2*>(row));
+            const __half2* h = reinterpret_cast<const __half2*>(&u);
+            const float2 a = __half22float2(h[0]), b = __half22float2(h[1]);
+            v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+        } else {
+#pragma unroll
+            for (int f = 0; f < F; ++f) v[f] = __half2float(row[f]);
+        }
+#pragma unroll
+        for (int f = 0; f < F; ++f) out[f] = fmaf(w, v[f], out[f]);
+    }
+}
+
+template <int F>
+__device__ __forceinline__ void write_tile_features(uint8_t* a_s, int row, int l, int K0, const float* v) {
+    const uint32_t off = umma::kmajor_offset(row, l * F, K0);
+    if constexpr (F == 8) {
+        store_half8(reinterpret_cast<__half*>(a_s + off), v);
+    } else if constexpr (F == 4) {
+        __half2 h[2] = {__floats2half2_rn(v[0], v[1]), __floats2half2_rn(v[2], v[3])};
+        *reinterpret_cast<uint2*>(a_s + off) = *reinterpret_cast<const uint2*>(h);
+    } else {
+#pragma unroll
+        for (int f = 0; f < F; ++f) reinterpret_cast<__half*>(a_s + off)[f] = __float2half_rn(v[f]);
+    }
+}
+
+// Stage the encoder features of one tile (126 rows) into the A tile.
+template <int F>
+__device__ void stage_encoding(const FieldParams& p, int64_t s0, uint8_t* a_s, __half* x0ext_tile_rows) {
+    const int pairs = SPT * EVALS * p.active;
+    for (int i = threadIdx.x; i < pairs; i += blockDim.x) {
+        const int row = i / p.active, l = i % p.active;
+        const int e = row / SPT, sl = row % SPT;
+        const int64_t s = s0 + sl;
+        float v[F];
+        if (s < p.Ns) {
+            float c[3], x[3], xu[3];
+            sample_point(p, s, c);
+            eval_point(c, e, p.eps, x);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) xu[k] = to_unit(x[k]);
+            gather_level<F>(p, xu, l, v);
+        } else {
+#pragma unroll
+            for (int f = 0; f < F; ++f) v[f] = 0.0f;
+        }
+        write_tile_features<F>(a_s, row, l, p.K0, v);
+        (void)x0ext_tile_rows;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// forward
+
+template <int F>
+__global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int K0 = p.K0;
+    uint8_t* w_s = smem;                                        // [256 x K0]
+    uint8_t* a_s = w_s + HID * K0 * 2;                          // [128 x K0]
+    float* w0x_s = reinterpret_cast<float*>(a_s + TILE_M * K0 * 2);   // [256*3]
+    float* b0_s = w0x_s + HID * 3;
+    float* wh_s = b0_s + HID;
+    float* part_s = wh_s + HID;                                 // [2][128] partial head sums
+    float* sdf_s = part_s + 2 * TILE_M;                         // [7][18]
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sdf_s + EVALS * SPT + 2);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    stage_rows_kmajor(w_s, (const __half*)p.w0e, 0, HID, K0, K0, tid, FIELD_THREADS, HID);
+    for (int i = tid; i < HID * 3; i += FIELD_THREADS) w0x_s[i] = p.w0x[i];
+    for (int i = tid; i < HID; i += FIELD_THREADS) {
+        b0_s[i] = p.b0[i];
+        wh_s[i] = p.whead[i];
+    }
+    for (int i = tid; i < TILE_M * K0 / 8; i += FIELD_THREADS)
+        reinterpret_cast<uint4*>(a_s)[i] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        umma::mbar_init(mbar, 1);
+        umma::fence_mbar_init();
+    }
+    if (warp == 0) {
+        umma::tmem_alloc(tslot, HID);
+        umma::tmem_relinquish();
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint32_t idesc = umma::idesc_f16(TILE_M, HID);
+    const uint32_t a_addr = umma::smem_u32(a_s), w_addr = umma::smem_u32(w_s);
+    const float bhead = p.bhead[0];
+    const int64_t ntiles = (p.Ns + SPT - 1) / SPT;
+    const int q = warp & 3, half = warp >> 2;
+    const int row = q * 32 + lane;
+    const int e_row = row / SPT, sl_row = row % SPT;
+    uint32_t phase = 0;
+
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int64_t s0 = t * SPT;
+        stage_encoding<F>(p, s0, a_s, nullptr);
+        umma::fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            umma::fence_after_sync();
+            issue_tile_mma(tmem, a_addr, w_addr, K0, idesc);
+            umma::mma_commit(mbar);
+        }
+        const bool ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
+        phase ^= 1u;
+        if (!ok) {
+            flag_timeout(p.err, 1);
+            break;
+        }
+        umma::fence_after_sync();
+        // epilogue: pre = acc + W0x x + b0 ; h = softplus ; partial head dot
+        const int64_t s = s0 + sl_row;
+        const bool live = row < SPT * EVALS && s < p.Ns;
+        float x[3] = {0.f, 0.f, 0.f};
+        if (live) {
+            float c[3];
+            sample_point(p, s, c);
+            eval_point(c, e_row, p.eps, x);
+        }
+        float part = 0.0f;
+#pragma unroll 1
+        for (int c0 = half * 128; c0 < half * 128 + 128; c0 += 32) {
+            float v[32];
+            umma::tmem_ld32(umma::taddr(tmem, q * 32, c0), v);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const int n = c0 + j;
+                float z = v[j] + w0x_s[3 * n] * x[0] + w0x_s[3 * n + 1] * x[1] + w0x_s[3 * n + 2] * x[2] + b0_s[n];
+                const float h = softplus_beta(z, p.beta);
+                v[j] = h;
+                part = fmaf(wh_s[n], h, part);
+            }
+            if (live && e_row == 0) {
+                __half* dst = (__half*)p.h0c + s * HID + c0;
+#pragma unroll
+                for (int j = 0; j < 32; j += 8) store_half8(dst + j, v + j);
+            }
+        }
+        part_s[half * TILE_M + row] = part;
+        umma::fence_before_sync();
+        __syncthreads();
+        if (tid < SPT * EVALS) {
+            sdf_s[tid] = part_s[tid] + part_s[TILE_M + tid] + bhead;
+        }
+        __syncthreads();
+        // per-sample: gradient, Hessian diagonal, outside overwrite, colour-input columns
+        if (tid < SPT) {
+            const int64_t ss = s0 + tid;
+            if (ss < p.Ns) {
+                const int r = ray_of(p, ss);
+                const bool out = p.outside && p.outside[r];
+                const float fc = out ? p.outside_val : sdf_s[tid];
+                float g[3], hh[3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const float fp = sdf_s[(1 + 2 * d) * SPT + tid], fm = sdf_s[(2 + 2 * d) * SPT + tid];
+                    g[d] = __fdiv_rn(__fsub_rn(fp, fm), p.two_eps);
+                    hh[d] = __fdiv_rn(__fsub_rn(__fadd_rn(fp, fm), __fmul_rn(2.0f, fc)), p.eps2);
+                }
+                p.sdf[ss] = fc;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    p.grad[3 * ss + d] = g[d];
+                    p.hess[3 * ss + d] = hh[d];
+                }
+                if (p.xc) {
+                    // NeuralRGB input tail (modules.py:209-213): x, SH(d), normalize(g), app
+                    float c[3];
+                    sample_point(p, ss, c);
+                    const float* dv = p.ray_unit + 3 * r;
+                    const float dx = dv[0], dy = dv[1], dz = dv[2];
+                    const float xx = dx * dx, yy = dy * dy, zz = dz * dz;
+                    float col[48];
+#pragma unroll
+                    for (int k = 0; k < 48; ++k) col[k] = 0.0f;
+                    col[0] = c[0]; col[1] = c[1]; col[2] = c[2];
+                    // real spherical-harmonic basis, degree <= 3 (spherical_harmonics.py:47-84)
+                    col[3] = 0.28209479177387814f;
+                    col[4] = -0.4886025119029199f * dy;
+                    col[5] = 0.4886025119029199f * dz;
+                    col[6] = -0.4886025119029199f * dx;
+                    col[7] = 1.0925484305920792f * dx * dy;
+                    col[8] = -1.0925484305920792f * dy * dz;
+                    col[9] = 0.31539156525252005f * (2.0f * zz - xx - yy);
+                    col[10] = -1.0925484305920792f * dx * dz;
+                    col[11] = 0.5462742152960396f * (xx - yy);
+                    col[12] = -0.5900435899266435f * dy * (3.0f * xx - yy);
+                    col[13] = 2.890611442640554f * dx * dy * dz;
+                    col[14] = -0.4570457994644658f * dy * (4.0f * zz - xx - yy);
+                    col[15] = 0.3731763325901154f * dz * (2.0f * zz - 3.0f * xx - 3.0f * yy);
+                    col[16] = -0.4570457994644658f * dx * (4.0f * zz - xx - yy);
+                    col[17] = 1.445305721320277f * dz * (xx - yy);
+                    col[18] = -0.5900435899266435f * dx * (xx - 3.0f * yy);
+                    const float nrm = fmaxf(sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]), 1e-12f);
+                    col[19] = g[0] / nrm; col[20] = g[1] / nrm; col[21] = g[2] / nrm;
+                    if (p.app_table && p.app_dim > 0) {
+                        const float* a = p.app_table + (int64_t)p.app_idx[r] * p.app_dim;
+                        for (int k = 0; k < p.app_dim && k < 26; ++k) col[22 + k] = a[k];
+                    }
+                    __half* dst = (__half*)p.xc + ss * (int64_t)p.ldxc + HID;
+                    const int ncol = p.ldxc - HID;
+                    for (int k = 0; k < ncol; k += 8) store_half8(dst + k, col + k);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, HID);
+}
+
+// ---------------------------------------------------------------------------
+// backward
+
+// Scatter d_enc of one (sample, level) over its 7 evaluations, merging the
+// evaluations that land in the same cell (the taps are eps apart, so coarse
+// levels almost always share all 8 corners) before the vector atomics.
+template <int F>
+__device__ __forceinline__ void scatter_sample_level(const FieldParams& p, const float* c, int l,
+                                                     const float* denc_s, int sl) {
+    const LevelDesc d = level_desc(p.grid, l);
+    uint32_t pidx[8];
+    float pacc[8][F];
+    bool have = false;
+    for (int e = 0; e < EVALS; ++e) {
+        const int row = e * SPT + sl;
+        const float* dv = denc_s + row * p.K0 + l * F;
+        float x[3], xu[3];
+        eval_point(c, e, p.eps, x);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) xu[k] = to_unit(x[k]);
+        uint32_t bx, by, bz;
+        float fx, fy, fz;
+        grid_pos(d.scale, xu[0], bx, fx);
+        grid_pos(d.scale, xu[1], by, fy);
+        grid_pos(d.scale, xu[2], bz, fz);
+        uint32_t idx[8];
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc) idx[cc] = grid_index(d, bx + (cc & 1), by + ((cc >> 1) & 1), bz + ((cc >> 2) & 1));
+        bool same = have;
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc) same = same && (idx[cc] == pidx[cc]);
+        if (have && !same) {
+#pragma unroll
+            for (int cc = 0; cc < 8; ++cc) {
+                float* dst = p.d_table + (d.offset + pidx[cc]) * F;
+                if constexpr (F == 8) {
+                    atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[cc][0], pacc[cc][1], pacc[cc][2], pacc[cc][3]));
+                    atomicAdd(reinterpret_cast<float4*>(dst) + 1, make_float4(pacc[cc][4], pacc[cc][5], pacc[cc][6], pacc[cc][7]));
+                } else if constexpr (F == 4) {
+                    atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[cc][0], pacc[cc][1], pacc[cc][2], pacc[cc][3]));
+                } else {
+#pragma unroll
+                    for (int f = 0; f < F; ++f) atomicAdd(dst + f, pacc[cc][f]);
+                }
+            }
+        }
+        if (!same) {
+#pragma unroll
+            for (int cc = 0; cc < 8; ++cc) {
+                pidx[cc] = idx[cc];
+#pragma unroll
+                for (int f = 0; f < F; ++f) pacc[cc][f] = 0.0f;
+            }
+            have = true;
+        }
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc) {
+            const float w = corner_weight(cc, fx, fy, fz);
+#pragma unroll
+            for (int f = 0; f < F; ++f) pacc[cc][f] = fmaf(w, dv[f], pacc[cc][f]);
+        }
+    }
+    if (have) {
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc) {
+            float* dst = p.d_table + (d.offset + pidx[cc]) * F;
+            if constexpr (F == 8) {
+                atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[cc][0], pacc[cc][1], pacc[cc][2], pacc[cc][3]));
+                atomicAdd(reinterpret_cast<float4*>(dst) + 1, make_float4(pacc[cc][4], pacc[cc][5], pacc[cc][6], pacc[cc][7]));
+            } else if constexpr (F == 4) {
+                atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[cc][0], pacc[cc][1], pacc[cc][2], pacc[cc][3]));
+            } else {
+#pragma unroll
+                for (int f = 0; f < F; ++f) atomicAdd(dst + f, pacc[cc][f]);
+            }
+        }
+    }
+}
+
+template <int F>
+__global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int K0 = p.K0;
+    const int KX = K0 + 16;                                     // x0ext row width
+    uint8_t* w_s = smem;                                        // [256 x K0]   B of MMA1
+    uint8_t* wt_s = w_s + HID * K0 * 2;                         // [K0 x 256]   B of MMA2
+    uint8_t* a_s = wt_s + K0 * HID * 2;                         // [128 x K0]   encoding tile
+    // d_pre is split into fp16 hi + lo tiles (d_pre = hi + lo to ~2^-22) when both fit:
+    // the +eps and -eps taps of a sample carry large, nearly cancelling gradients,
+    // so a single fp16 rounding of d_pre would dominate the table-gradient error.
+    const bool split = K0 <= 64;
+    uint8_t* p_s = a_s + TILE_M * K0 * 2;                       // [128 x 256]  d_pre hi (fp16); reused as fp32 d_enc
+    uint8_t* p2_s = p_s + TILE_M * HID * 2;                     // [128 x 256]  d_pre lo (fp16), when split
+    float* w0x_s = reinterpret_cast<float*>(p2_s + (split ? TILE_M * HID * 2 : 0));
+    float* b0_s = w0x_s + HID * 3;
+    float* wh_s = b0_s + HID;
+    float* dwh_s = wh_s + HID;                                  // [256] d_whead accumulator
+    float* df_s = dwh_s + HID;                                  // [7][18] d f per evaluation
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(df_s + EVALS * SPT + 2);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    stage_rows_kmajor(w_s, (const __half*)p.w0e, 0, HID, K0, K0, tid, FIELD_THREADS, HID);
+    stage_rows_kmajor(wt_s, (const __half*)p.w0eT, 0, K0, HID, HID, tid, FIELD_THREADS, K0);
+    for (int i = tid; i < HID * 3; i += FIELD_THREADS) w0x_s[i] = p.w0x[i];
+    for (int i = tid; i < HID; i += FIELD_THREADS) {
+        b0_s[i] = p.b0[i];
+        wh_s[i] = p.whead[i];
+        dwh_s[i] = 0.0f;
+    }
+    for (int i = tid; i < TILE_M * K0 / 8; i += FIELD_THREADS)
+        reinterpret_cast<uint4*>(a_s)[i] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        umma::mbar_init(mbar, 1);
+        umma::fence_mbar_init();
+    }
+    if (warp == 0) {
+        umma::tmem_alloc(tslot, 512);
+        umma::tmem_relinquish();
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint32_t tmem2 = tmem + HID;                          // D2 columns [256, 256 + K0)
+    const uint32_t idesc1 = umma::idesc_f16(TILE_M, HID);
+    const uint32_t idesc2 = umma::idesc_f16(TILE_M, K0);
+    const uint32_t a_addr = umma::smem_u32(a_s), w_addr = umma::smem_u32(w_s);
+    const uint32_t p_addr = umma::smem_u32(p_s), wt_addr = umma::smem_u32(wt_s), p2_addr = umma::smem_u32(p2_s);
+    const int64_t ntiles = (p.Ns + SPT - 1) / SPT;
+    const int q = warp & 3, half = warp >> 2;
+    const int row = q * 32 + lane;
+    const int e_row = row / SPT, sl_row = row % SPT;
+    uint32_t phase = 0;
+    float dbh = 0.0f;
+    bool ok = true;
+
+    for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const int64_t s0 = t * SPT;
+        // (0) per-sample output gradients -> d f of each evaluation (modules.py:144-156)
+        if (tid < SPT) {
+            const int64_t s = s0 + tid;
+            float df[EVALS] = {0, 0, 0, 0, 0, 0, 0};
+            if (s < p.Ns) {
+                const int r = ray_of(p, s);
+                const bool out = p.outside && p.outside[r];
+                const float g0 = p.grad[3 * s], g1 = p.grad[3 * s + 1], g2 = p.grad[3 * s + 2];
+                float dg[3] = {p.d_grad[3 * s], p.d_grad[3 * s + 1], p.d_grad[3 * s + 2]};
+                // normals = g / max(|g|, 1e-12) feed the colour MLP (model.py:167)
+                const float* dn = p.d_xc + s * (int64_t)p.ld_dxc + p.normal_col;
+                const float n0 = dn[0], n1 = dn[1], n2 = dn[2];
+                const float len = sqrtf(g0 * g0 + g1 * g1 + g2 * g2);
+                if (len > 1e-12f) {
+                    const float inv = 1.0f / len;
+                    const float u0 = g0 * inv, u1 = g1 * inv, u2 = g2 * inv;
+                    const float dot = u0 * n0 + u1 * n1 + u2 * n2;
+                    dg[0] += (n0 - u0 * dot) * inv;
+                    dg[1] += (n1 - u1 * dot) * inv;
+                    dg[2] += (n2 - u2 * dot) * inv;
+                } else {
+                    dg[0] += n0 * 1e12f; dg[1] += n1 * 1e12f; dg[2] += n2 * 1e12f;
+                }
+                float hsum = 0.0f;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const float dh = p.d_hess[3 * s + d];
+                    const float a = dg[d] / p.two_eps, b = dh / p.eps2;
+                    df[1 + 2 * d] = a + b;
+                    df[2 + 2 * d] = -a + b;
+                    hsum += b;
+                }
+                // the centre feeds alpha and the Hessian only where it was not overwritten
+                df[0] = out ? 0.0f : (p.d_sdf[s] - 2.0f * hsum);
+            }
+#pragma unroll
+            for (int e = 0; e < EVALS; ++e) {
+                df_s[e * SPT + tid] = df[e];
+                dbh += df[e];
+            }
+        }
+        // (1) encoder features of the 126 rows
+        stage_encoding<F>(p, s0, a_s, nullptr);
+        umma::fence_proxy_async_smem();
+        __syncthreads();
+        // x0ext rows (encoding, x, y, z, 1) for the layer-0 weight gradient
+        for (int i = tid; i < SPT * EVALS; i += FIELD_THREADS) {
+            const int e = i / SPT, sl = i % SPT;
+            const int64_t s = s0 + sl;
+            if (s >= p.Ns) continue;
+            __half* dst = (__half*)p.x0ext + (s * EVALS + e) * (int64_t)KX;
+            for (int kc = 0; kc < K0; kc += 8)
+                *reinterpret_cast<uint4*>(dst + kc) = *reinterpret_cast<const uint4*>(a_s + umma::kmajor_offset(i, kc, K0));
+            float c[3], x[3];
+            sample_point(p, s, c);
+            eval_point(c, e, p.eps, x);
+            float tail[16] = {x[0], x[1], x[2], 1.0f, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+            store_half8(dst + K0, tail);
+            store_half8(dst + K0 + 8, tail + 8);
+        }
+        if (tid == 0) {
+            umma::fence_after_sync();
+            issue_tile_mma(tmem, a_addr, w_addr, K0, idesc1);
+            umma::mma_commit(mbar);
+        }
+        ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
+        phase ^= 1u;
+        if (!ok) {
+            flag_timeout(p.err, 1);
+            break;
+        }
+        umma::fence_after_sync();
+        // (2) d_pre = (d f * w_head + [centre] d_h0c) * softplus'(pre)
+        {
+            const int64_t s = s0 + sl_row;
+            const bool live = row < SPT * EVALS && s < p.Ns;
+            float x[3] = {0.f, 0.f, 0.f};
+            float df = 0.0f;
+            if (live) {
+                float c[3];
+                sample_point(p, s, c);
+                eval_point(c, e_row, p.eps, x);
+                df = df_s[row];
+            }
+            const bool centre = live && e_row == 0;
+#pragma unroll 1
+            for (int c0 = half * 128; c0 < half * 128 + 128; c0 += 32) {
+                float v[32];
+                umma::tmem_ld32(umma::taddr(tmem, q * 32, c0), v);
+                float dh0[32];
+                if (centre) {
+                    const float4* src = reinterpret_cast<const float4*>(p.d_h0c + s * HID + c0);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const float4 f = src[j];
+                        dh0[4 * j] = f.x; dh0[4 * j + 1] = f.y; dh0[4 * j + 2] = f.z; dh0[4 * j + 3] = f.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) dh0[j] = 0.0f;
+                }
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int n = c0 + j;
+                    const float z = v[j] + w0x_s[3 * n] * x[0] + w0x_s[3 * n + 1] * x[1] + w0x_s[3 * n + 2] * x[2] + b0_s[n];
+                    const float hval = softplus_beta(z, p.beta);
+                    const float dpre = live ? (df * wh_s[n] + dh0[j]) * softplus_grad(z, p.beta) : 0.0f;
+                    v[j] = dpre;
+                    // d w_head = sum_rows d f * h  (warp reduction, then shared accumulator)
+                    float contrib = live ? df * hval : 0.0f;
+                    contrib = warp_sum(contrib);
+                    if (lane == 0 && contrib != 0.0f) atomicAdd(&dwh_s[n], contrib);
+                }
+                // d_pre into the MMA2 A tile(s) (K-major over the 256 hidden units) and to global
+#pragma unroll
+                for (int j = 0; j < 32; j += 8) {
+                    store_half8(reinterpret_cast<__half*>(p_s + umma::kmajor_offset(row, c0 + j, HID)), v + j);
+                    if (split) {
+                        float lo[8];
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) lo[i] = v[j + i] - __half2float(__float2half_rn(v[j + i]));
+                        store_half8(reinterpret_cast<__half*>(p2_s + umma::kmajor_offset(row, c0 + j, HID)), lo);
+                    }
+                }
+                if (live) {
+                    __half* dst = (__half*)p.d_pre0 + (s * EVALS + e_row) * (int64_t)HID + c0;
+#pragma unroll
+                    for (int j = 0; j < 32; j += 8) store_half8(dst + j, v + j);
+                }
+            }
+        }
+        umma::fence_before_sync();
+        umma::fence_proxy_async_smem();
+        __syncthreads();
+        // (3) d_enc = d_pre * W0e  (MMA2: A = d_pre [128 x 256], B = W0e^T [K0 x 256])
+        if (tid == 0) {
+            umma::fence_after_sync();
+            issue_tile_mma(tmem2, p_addr, wt_addr, HID, idesc2);
+            if (split) issue_tile_mma(tmem2, p2_addr, wt_addr, HID, idesc2, true);
+            umma::mma_commit(mbar);
+        }
+        ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
+        phase ^= 1u;
+        if (!ok) {
+            flag_timeout(p.err, 1);
+            break;
+        }
+        umma::fence_after_sync();
+        float* denc_s = reinterpret_cast<float*>(p_s);          // [128 x K0] fp32 (P no longer read)
+        {
+            const int cols = K0 / 2;                            // each half of the warps stages half the columns
+            for (int c0 = half * cols; c0 < half * cols + cols; c0 += 16) {
+                float v[16];
+                umma::tmem_ld16(umma::taddr(tmem2, q * 32, c0), v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) denc_s[row * K0 + c0 + j] = v[j];
+            }
+        }
+        umma::fence_before_sync();
+        __syncthreads();
+        // (4) scatter into the table gradient, one thread per (sample, level)
+        for (int i = tid; i < SPT * p.active; i += FIELD_THREADS) {
+            const int sl = i / p.active, l = i % p.active;
+            const int64_t s = s0 + sl;
+            if (s >= p.Ns) continue;
+            float c[3];
+            sample_point(p, s, c);
+            scatter_sample_level<F>(p, c, l, denc_s, sl);
+        }
+        __syncthreads();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    for (int i = tid; i < HID; i += FIELD_THREADS)
+        if (dwh_s[i] != 0.0f) atomicAdd(&p.d_whead[i], dwh_s[i]);
+    dbh = warp_sum(dbh);
+    if (lane == 0 && dbh != 0.0f) atomicAdd(p.d_bhead, dbh);
+    if (warp == 0) umma::tmem_dealloc(tmem, 512);
+}
+
+static int num_sms() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+static size_t fwd_smem(int K0) {
+    return (size_t)HID * K0 * 2 + (size_t)TILE_M * K0 * 2 + (HID * 3 + 2 * HID + 2 * TILE_M + EVALS * SPT + 2) * 4 + 16;
+}
+static size_t bwd_smem(int K0) {
+    const size_t ptiles = K0 <= 64 ? 2 : 1;
+    return (size_t)HID * K0 * 2 * 2 + (size_t)TILE_M * K0 * 2 + ptiles * TILE_M * HID * 2 +
+           (HID * 3 + 3 * HID + EVALS * SPT + 2) * 4 + 16;
+}
+
+template <int F>
+static int launch_field(const FieldParams& p, bool backward, cudaStream_t s) {
+    const size_t smem = backward ? bwd_smem(p.K0) : fwd_smem(p.K0);
+    if (smem > 227 * 1024) {
+        set_error("field kernel needs %zu B of shared memory", smem);
+        return GBSDF_ERR_UNSUPPORTED;
+    }
+    const int64_t ntiles = (p.Ns + SPT - 1) / SPT;
+    int64_t grid = num_sms();
+    if (grid > ntiles) grid = ntiles;
+    if (backward) {
+        cudaFuncSetAttribute(k_field_bwd<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_field_bwd<F><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p);
+    } else {
+        cudaFuncSetAttribute(k_field_fwd<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_field_fwd<F><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p);
+    }
+    return launch_status(backward ? "field_bwd" : "field_fwd");
+}
+
+static int check_field(const FieldParams& p) {
+    GBSDF_CHECK_ARG(p.Ns >= 0, "Ns < 0");
+    GBSDF_CHECK_ARG(p.active >= 1 && p.active <= p.grid.n_levels, "active levels %d", p.active);
+    const int F = p.grid.n_features;
+    GBSDF_CHECK_ARG(F == 2 || F == 4 || F == 8, "n_features %d unsupported by the fused field", F);
+    GBSDF_CHECK_ARG(p.K0 % 16 == 0 && p.K0 >= p.active * F && p.K0 <= 128, "K0 %d", p.K0);
+    GBSDF_CHECK_ARG(p.S > 0 || p.sample_ray, "need S > 0 or sample_ray");
+    GBSDF_CHECK_ARG(p.center && p.ray_unit && p.dists && p.table && p.w0e && p.w0x && p.b0 && p.whead && p.bhead,
+                    "NULL pointer");
+    GBSDF_CHECK_ARG(aligned(p.table, 16) && aligned(p.w0e, 16), "table / w0e alignment");
+    return GBSDF_OK;
+}
+
+}  // namespace gbsdf
+
+using namespace gbsdf;
+
+extern "C" size_t gbsdf_field_args_size(void) { return sizeof(gbsdf_field_args); }
+
+extern "C" int gbsdf_field_fwd(const gbsdf_field_args* params, void* stream) {
+    clear_error();
+    GBSDF_CHECK_ARG(params != nullptr, "params NULL");
+    const FieldParams& p = *params;
+    if (int st = check_field(p)) return st;
+    if (p.Ns == 0) return GBSDF_OK;
+    GBSDF_CHECK_ARG(p.sdf && p.grad && p.hess && p.h0c, "NULL output");
+    GBSDF_CHECK_ARG(!p.xc || (p.ldxc % 16 == 0 && p.ldxc - HID >= 22 + p.app_dim && p.ldxc - HID <= 48),
+                    "xc leading dimension %d (needs 256 + 22 + app_dim <= ldxc <= 304, multiple of 16)", p.ldxc);
+    GBSDF_CHECK_ARG(!p.xc || p.app_dim == 0 || (p.app_table && p.app_idx), "appearance table / index missing");
+    switch (p.grid.n_features) {
+        case 2: return launch_field<2>(p, false, as_stream(stream));
+        case 4: return launch_field<4>(p, false, as_stream(stream));
+        default: return launch_field<8>(p, false, as_stream(stream));
+    }
+}
+
+extern "C" int gbsdf_field_bwd(const gbsdf_field_args* params, void* stream) {
+    clear_error();
+    GBSDF_CHECK_ARG(params != nullptr, "params NULL");
+    const FieldParams& p = *params;
+    if (int st = check_field(p)) return st;
+    if (p.Ns == 0) return GBSDF_OK;
+    GBSDF_CHECK_ARG(p.w0eT && p.grad && p.d_sdf && p.d_grad && p.d_hess && p.d_xc && p.d_h0c && p.d_table &&
+                        p.d_pre0 && p.x0ext && p.d_whead && p.d_bhead,
+                    "NULL pointer");
+    GBSDF_CHECK_ARG(aligned(p.d_table, 16), "d_table alignment");
+    switch (p.grid.n_features) {
+        case 2: return launch_field<2>(p, true, as_stream(stream));
+        case 4: return launch_field<4>(p, true, as_stream(stream));
+        default: return launch_field<8>(p, true, as_stream(stream));
+    }
+}

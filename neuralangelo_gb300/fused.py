@@ -1,0 +1,419 @@
+"""Fused mixed-precision training step of the field (FP16 tensor cores, FP32 masters).
+
+One call of ``FusedField.step(batch)`` runs the forward and backward of
+Model.render_rays_object + render_rays + Trainer._compute_loss
+(projects/neuralangelo/model.py:124-190, trainer.py:40-52; background off)
+through the libgbsdf kernels and leaves FP32 gradients in ``.grad`` of the
+FieldModel's master parameters, exactly where the plain drop-in's autograd
+puts them.
+
+Precision: the hash table and the MLP weights are used as FP16 copies of the
+FP32 masters; every contraction accumulates in FP32 (tcgen05 TMEM); the SDF
+head, positions, tap differences, transmittance (log space) and losses stay
+FP32; the loss sums are accumulated in FP64.  Gradients are computed with a
+static loss scale (2^15 by default) and unscaled into FP32; ``found_inf``
+reports an overflow so a caller can skip the step and lower the scale
+(dynamic loss scaling).
+
+Kernels per step (all on the current stream):
+  field_fwd, dense x (1 + colour layers), rgb_head_fwd, render_fused,
+  rgb_head_bwd, dense x (colour layers + 2), app_grad, field_bwd, and the
+  weight-gradient GEMMs (cuBLAS, fp16 in / fp32 out).
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+from .dense import EPI_DRELU, EPI_DSOFTPLUS, EPI_IDENTITY, EPI_RELU, EPI_SOFTPLUS
+
+c_i32, c_i64, c_f32, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_void_p
+
+
+class FieldArgs(ctypes.Structure):
+    _fields_ = [("Ns", c_i64), ("S", c_i32), ("pad0", c_i32), ("sample_ray", c_vp), ("center", c_vp),
+                ("ray_unit", c_vp), ("dists", c_vp), ("outside", c_vp), ("app_idx", c_vp),
+                ("grid", _lib.GridStruct), ("active", c_i32), ("K0", c_i32), ("table", c_vp), ("w0e", c_vp),
+                ("w0eT", c_vp), ("w0x", c_vp), ("b0", c_vp), ("whead", c_vp), ("bhead", c_vp),
+                ("beta", c_f32), ("eps", c_f32), ("two_eps", c_f32), ("eps2", c_f32), ("outside_val", c_f32),
+                ("pad1", c_i32), ("xc", c_vp), ("ldxc", c_i32), ("app_dim", c_i32), ("app_table", c_vp),
+                ("sdf", c_vp), ("grad", c_vp), ("hess", c_vp), ("h0c", c_vp), ("d_sdf", c_vp), ("d_grad", c_vp),
+                ("d_hess", c_vp), ("d_xc", c_vp), ("ld_dxc", c_i32), ("normal_col", c_i32), ("d_h0c", c_vp),
+                ("d_table", c_vp), ("d_pre0", c_vp), ("x0ext", c_vp), ("d_whead", c_vp), ("d_bhead", c_vp),
+                ("err", c_vp)]
+
+
+class RenderArgs(ctypes.Structure):
+    _fields_ = [("R", c_i64), ("S", c_i32), ("pad0", c_i32), ("ray_offsets", c_vp), ("ray_unit", c_vp),
+                ("dists", c_vp), ("far", c_vp), ("outside", c_vp), ("target", c_vp), ("s_var", c_vp),
+                ("sdf", c_vp), ("grad", c_vp), ("hess", c_vp), ("rgbs", c_vp), ("anneal", c_f32),
+                ("w_render", c_f32), ("w_eik", c_f32), ("w_curv", c_f32), ("l1_scale", c_f32),
+                ("mean_scale", c_f32), ("loss_scale", c_f32), ("pad1", c_i32), ("rgb", c_vp), ("weights", c_vp),
+                ("d_rgbs", c_vp), ("d_sdf", c_vp), ("d_grad", c_vp), ("d_hess", c_vp), ("d_s_var", c_vp),
+                ("loss_sums", c_vp), ("err", c_vp)]
+
+
+_lib.register("gbsdf_field_args_size", [])
+_lib.register("gbsdf_render_args_size", [])
+_lib.register("gbsdf_field_fwd", [c_vp, c_vp])
+_lib.register("gbsdf_field_bwd", [c_vp, c_vp])
+_lib.register("gbsdf_render_fused", [c_vp, c_vp])
+_lib.register("gbsdf_rgb_head_fwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp])
+_lib.register("gbsdf_rgb_head_bwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp])
+_lib.register("gbsdf_app_grad", [c_i64, c_i32, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_vp])
+_lib.register("gbsdf_gemm_wgrad", [c_i64, c_i32, c_i32, c_vp, c_i32, c_vp, c_i32, c_vp, c_i32, c_f32, c_f32, c_vp])
+
+
+def check_struct_sizes():
+    lib = _lib.load()
+    lib.gbsdf_field_args_size.restype = ctypes.c_size_t
+    lib.gbsdf_render_args_size.restype = ctypes.c_size_t
+    assert lib.gbsdf_field_args_size() == ctypes.sizeof(FieldArgs), "gbsdf_field_args layout mismatch"
+    assert lib.gbsdf_render_args_size() == ctypes.sizeof(RenderArgs), "gbsdf_render_args layout mismatch"
+
+
+def _p(t):
+    return None if t is None else t.data_ptr()
+
+
+def _round16(n):
+    return (n + 15) // 16 * 16
+
+
+def _dense(X, Wt, N, K, out, bias=None, epi=EPI_IDENTITY, beta=100.0, G=None, err=None):
+    """out[:, :N] = epi(X[:, :K] @ Wt[:N, :K].T + bias ; G) on the tcgen05 kernel."""
+    _lib.call("gbsdf_dense", X.shape[0], K, N, c_vp(X.data_ptr()), X.stride(0), c_vp(Wt.data_ptr()),
+              c_vp(_p(bias)), c_vp(_p(G)), G.stride(0) if G is not None else 0, c_vp(out.data_ptr()), out.stride(0),
+              1 if out.dtype == torch.float32 else 0, int(epi), float(beta), c_vp(_p(err)),
+              _lib.stream_ptr(X.device))
+
+
+def _wgrad(dZ, X, N, K, dW):
+    """dW[N, K] = dZ[:, :N]^T X[:, :K] (fp32 out)."""
+    _lib.call("gbsdf_gemm_wgrad", dZ.shape[0], N, K, c_vp(dZ.data_ptr()), dZ.stride(0), c_vp(X.data_ptr()),
+              X.stride(0), c_vp(dW.data_ptr()), dW.stride(0), 1.0, 0.0, _lib.stream_ptr(dZ.device))
+
+
+class FusedField:
+    """Fused FP16 forward+backward over a FieldModel's FP32 master parameters."""
+
+    def __init__(self, model, loss_scale=2.0 ** 15):
+        check_struct_sizes()
+        self.model = model
+        self.loss_scale = float(loss_scale)
+        sdf = model.neural_sdf
+        cfg = model.cfg
+        self.H = cfg.sdf.mlp.hidden_dim
+        if self.H != 256:
+            raise ValueError("the fused field is built for SDF hidden width 256")
+        if cfg.sdf.gradient.taps != 6 or cfg.sdf.gradient.mode != "numerical":
+            raise ValueError("the fused field implements the 6-tap numerical gradient")
+        if cfg.sdf.mlp.skip or cfg.sdf.mlp.num_layers != 1:
+            raise ValueError("the fused field implements the one-hidden-layer SDF MLP of the reference config")
+        rgb = cfg.rgb
+        if rgb.mode != "idr" or rgb.mlp.skip or rgb.encoding_view.levels != 3:
+            raise ValueError("the fused colour MLP implements mode 'idr' with SH degree 3 and no skips")
+        self.Hc = rgb.mlp.hidden_dim
+        if self.Hc not in (128, 256):
+            raise ValueError("colour hidden width must be 128 or 256")
+        self.n_rgb_hidden = rgb.mlp.num_layers
+        self.app_dim = cfg.appear_embed.dim if cfg.appear_embed.enabled else 0
+        self.tail = 22 + self.app_dim                  # x 3, SH 16, normal 3, app
+        self.Kc0 = 256 + _round16(self.tail)
+        self.F = sdf.tcnn_encoding.layout.n_features
+        self.L = sdf.tcnn_encoding.layout.n_levels
+        self.ws = None
+        self.err = None
+
+    # ------------------------------------------------------------------ parameters
+    def _pack(self):
+        """FP16 working copies of the FP32 masters (weight norm applied) for this step."""
+        m = self.model
+        sdf = m.neural_sdf
+        A = sdf.active_levels
+        F = self.F
+        self.A = A
+        self.K0 = max(16, _round16(A * F))
+        with torch.no_grad():
+            W0 = sdf.mlp.linears[0].weight                       # [256, 3 + L F]
+            w0e = torch.zeros(self.H, self.K0, device=W0.device, dtype=torch.float16)
+            w0e[:, :A * F] = W0[:, 3:3 + A * F]
+            pk = dict(
+                table=sdf.tcnn_encoding.params.detach().half(),
+                w0e=w0e, w0eT=w0e.t().contiguous(),
+                w0x=W0[:, :3].contiguous().float(), b0=sdf.mlp.linears[0].bias.detach().float(),
+                whead=sdf.mlp.linear_sdf.weight.detach()[0].contiguous().float(),
+                bhead=sdf.mlp.linear_sdf.bias.detach().float())
+            W1 = sdf.mlp.linears[1].weight
+            pk['w1'] = W1.half().contiguous()
+            pk['w1T'] = W1.t().half().contiguous()
+            pk['b1'] = sdf.mlp.linears[1].bias.detach().float()
+            lins = m.neural_rgb.mlp.linears
+            # colour layer 0 columns reordered to [feat 256 | x 3, SH 16, n 3, app | 0]
+            Wc0 = lins[0].weight
+            sh = 16
+            tail_src = torch.cat([Wc0[:, 0:3], Wc0[:, 3:3 + sh], Wc0[:, 3 + sh:6 + sh],
+                                  Wc0[:, 6 + sh + 256:6 + sh + 256 + self.app_dim]], dim=1)
+            wc0 = torch.zeros(self.Hc, self.Kc0, device=W0.device, dtype=torch.float16)
+            wc0[:, :256] = Wc0[:, 6 + sh:6 + sh + 256]
+            wc0[:, 256:256 + self.tail] = tail_src
+            pk['wc'] = [wc0.contiguous()]
+            pk['bc'] = [lins[0].bias.detach().float()]
+            for i in range(1, self.n_rgb_hidden):
+                pk['wc'].append(lins[i].weight.half().contiguous())
+                pk['bc'].append(lins[i].bias.detach().float())
+            # transposes for the input-gradient GEMMs
+            pk['wcT'] = [None] + [w.t().contiguous() for w in pk['wc'][1:]]
+            pk['wc0T_feat'] = wc0[:, :256].t().contiguous()           # [256, Hc]
+            t = torch.zeros(64, self.Hc, device=W0.device, dtype=torch.float16)
+            t[:self.Kc0 - 256] = wc0[:, 256:].t()
+            pk['wc0T_tail'] = t                                        # [64, Hc]
+            pk['wl'] = lins[-1].weight.detach().float().contiguous()  # [3, Hc]
+            pk['bl'] = lins[-1].bias.detach().float().contiguous()
+            pk['s_var'] = m.s_var.detach().reshape(1).float().contiguous()
+            pk['app'] = m.appear_embed.weight.detach().float().contiguous() if self.app_dim else None
+        self.pk = pk
+
+    # ------------------------------------------------------------------ workspace
+    def _workspace(self, R, S, Ns, device):
+        key = (R, S, Ns, self.K0)
+        if self.ws is not None and self.ws['key'] == key:
+            return self.ws
+        f16, f32 = torch.float16, torch.float32
+        e = lambda *s, dt=f32: torch.empty(*s, device=device, dtype=dt)  # noqa: E731
+        Hc = self.Hc
+        ws = dict(key=key)
+        ws.update(sdf=e(Ns), grad=e(Ns, 3), hess=e(Ns, 3), h0c=e(Ns, 256, dt=f16), xc=e(Ns, self.Kc0, dt=f16),
+                  ys=[e(Ns, Hc, dt=f16) for _ in range(self.n_rgb_hidden)], rgbs=e(Ns, 3), rgb=e(R, 3),
+                  weights=e(Ns), d_rgbs=e(Ns, 3), d_sdf=e(Ns), d_grad=e(Ns, 3), d_hess=e(Ns, 3),
+                  loss_sums=torch.zeros(4, device=device, dtype=torch.float64), d_s_var=torch.zeros(1, device=device),
+                  d_pre_last=e(Ns, 8, dt=f16), dzs=[e(Ns, Hc, dt=f16) for _ in range(2)], dzfeat=e(Ns, 256, dt=f16),
+                  dxc_tail=e(Ns, 64), d_h0c=e(Ns, 256), d_pre0=e(Ns * 7, 256, dt=f16),
+                  x0ext=e(Ns * 7, self.K0 + 16, dt=f16), d_whead=torch.zeros(256, device=device),
+                  d_bhead=torch.zeros(1, device=device), d_bl=torch.zeros(3, device=device),
+                  err=torch.zeros(1, device=device, dtype=torch.int32))
+        self.ws = ws
+        return ws
+
+    # ------------------------------------------------------------------ step
+    def step(self, batch, compute_loss=True):
+        """Forward + backward on a batch (same keys as FieldModel.render_step).
+
+        Ragged batches pass ``ray_offsets`` [R+1] (int64) and flat ``dists`` [Ns];
+        dense batches pass ``dists`` [R, S].  Returns a dict with the loss terms
+        (python floats when compute_loss) and writes FP32 ``.grad`` into the model."""
+        m = self.model
+        sdfm = m.neural_sdf
+        dev = batch['center'].device
+        self._pack()
+        pk = self.pk
+        dists = batch['dists']
+        R = batch['center'].shape[0]
+        ragged = 'ray_offsets' in batch
+        if ragged:
+            offs = batch['ray_offsets']
+            Ns = int(dists.numel())
+            S = 0
+            sample_ray = batch['sample_ray']
+        else:
+            S = dists.shape[1]
+            Ns = R * S
+            offs = None
+            sample_ray = None
+        ws = self._workspace(R, S, Ns, dev)
+        dists_f = dists.reshape(-1).contiguous().float()
+        center = batch['center'].contiguous().float()
+        ray_unit = batch['ray_unit'].contiguous().float()
+        far = batch['far'].reshape(-1).contiguous().float()
+        outside = batch['outside'].reshape(-1).to(torch.uint8).contiguous()
+        target = batch['target'].contiguous().float()
+        app_idx = batch['app_idx'].to(torch.int32).contiguous() if self.app_dim else None
+        stream = _lib.stream_ptr(dev)
+        eps = float(sdfm.normal_eps)
+        lay = sdfm.tcnn_encoding.layout
+        Hc = self.Hc
+        ws['err'].zero_()
+
+        fa = FieldArgs()
+        fa.Ns, fa.S = Ns, S
+        fa.sample_ray = _p(sample_ray)
+        fa.center, fa.ray_unit, fa.dists, fa.outside = _p(center), _p(ray_unit), _p(dists_f), _p(outside)
+        fa.app_idx = _p(app_idx)
+        fa.grid = lay.struct
+        fa.active, fa.K0 = self.A, self.K0
+        fa.table, fa.w0e, fa.w0eT = _p(pk['table']), _p(pk['w0e']), _p(pk['w0eT'])
+        fa.w0x, fa.b0, fa.whead, fa.bhead = _p(pk['w0x']), _p(pk['b0']), _p(pk['whead']), _p(pk['bhead'])
+        fa.beta = float(m.cfg.sdf.mlp.activ_params.beta)
+        fa.eps = eps
+        fa.two_eps = float(torch.tensor(2 * eps, dtype=torch.float32))
+        fa.eps2 = float(torch.tensor(eps ** 2, dtype=torch.float32))
+        fa.outside_val = float(m.outside_val)
+        fa.xc, fa.ldxc = _p(ws['xc']), self.Kc0
+        fa.app_dim, fa.app_table = self.app_dim, _p(pk['app'])
+        fa.sdf, fa.grad, fa.hess, fa.h0c = _p(ws['sdf']), _p(ws['grad']), _p(ws['hess']), _p(ws['h0c'])
+        fa.err = _p(ws['err'])
+        # ---------------- forward ----------------
+        _lib.call("gbsdf_field_fwd", ctypes.byref(fa), stream)
+        # SDF feature layer, written into the colour input's first 256 columns
+        _dense(ws['h0c'], pk['w1'], 256, 256, ws['xc'], bias=pk['b1'], epi=EPI_SOFTPLUS, beta=fa.beta,
+               err=ws['err'])
+        X, K = ws['xc'], self.Kc0
+        for i in range(self.n_rgb_hidden):
+            _dense(X, pk['wc'][i], Hc, K, ws['ys'][i], bias=pk['bc'][i], epi=EPI_RELU, err=ws['err'])
+            X, K = ws['ys'][i], Hc
+        ylast = ws['ys'][-1]
+        _lib.call("gbsdf_rgb_head_fwd", Ns, c_vp(ylast.data_ptr()), Hc, Hc, c_vp(pk['wl'].data_ptr()),
+                  c_vp(pk['bl'].data_ptr()), c_vp(ws['rgbs'].data_ptr()), stream)
+        # ---------------- render + losses, fwd + bwd ----------------
+        lw = m.cfg.loss_weight
+        n_mean = batch.get('mean_count', Ns)
+        ra = RenderArgs()
+        ra.R, ra.S = R, S
+        ra.ray_offsets = _p(offs)
+        ra.ray_unit, ra.dists, ra.far, ra.outside, ra.target = _p(ray_unit), _p(dists_f), _p(far), _p(outside), \
+            _p(target)
+        ra.s_var = _p(pk['s_var'])
+        ra.sdf, ra.grad, ra.hess, ra.rgbs = _p(ws['sdf']), _p(ws['grad']), _p(ws['hess']), _p(ws['rgbs'])
+        ra.anneal = min(m.progress / m.anneal_end, 1.0)
+        ra.w_render, ra.w_eik, ra.w_curv = float(lw.render), float(lw.eikonal), float(m.w_curv or 0.0)
+        ra.l1_scale = 3.0 / (3.0 * R)
+        ra.mean_scale = 1.0 / n_mean
+        ra.loss_scale = self.loss_scale
+        ra.rgb, ra.weights = _p(ws['rgb']), _p(ws['weights'])
+        ra.d_rgbs, ra.d_sdf, ra.d_grad, ra.d_hess = _p(ws['d_rgbs']), _p(ws['d_sdf']), _p(ws['d_grad']), \
+            _p(ws['d_hess'])
+        ws['d_s_var'].zero_()
+        ws['loss_sums'].zero_()
+        ra.d_s_var, ra.loss_sums = _p(ws['d_s_var']), _p(ws['loss_sums'])
+        ra.err = _p(ws['err'])
+        _lib.call("gbsdf_render_fused", ctypes.byref(ra), stream)
+        # ---------------- colour MLP backward ----------------
+        ws['d_bl'].zero_()
+        dz = ws['dzs'][0]
+        _lib.call("gbsdf_rgb_head_bwd", Ns, c_vp(ylast.data_ptr()), Hc, Hc, c_vp(pk['wl'].data_ptr()),
+                  c_vp(ws['rgbs'].data_ptr()), c_vp(ws['d_rgbs'].data_ptr()), c_vp(ws['d_pre_last'].data_ptr()),
+                  c_vp(dz.data_ptr()), c_vp(ws['d_bl'].data_ptr()), stream)
+        grads = {}
+        dev32 = dict(device=dev, dtype=torch.float32)
+        n = self.n_rgb_hidden
+        # last colour layer weight gradient
+        gl = torch.empty(3, Hc, **dev32)
+        _wgrad(ws['d_pre_last'], ylast, 3, Hc, gl)
+        grads['wl'], grads['bl'] = gl, ws['d_bl']
+        cur = 0
+        for i in range(n - 1, 0, -1):
+            dzi = ws['dzs'][cur]
+            gw = torch.empty(Hc, Hc, **dev32)
+            _wgrad(dzi, ws['ys'][i - 1], Hc, Hc, gw)
+            grads[f'wc{i}'], grads[f'bc{i}'] = gw, torch.sum(dzi, 0, dtype=torch.float32)
+            nxt = ws['dzs'][1 - cur]
+            _dense(dzi, pk['wcT'][i], Hc, Hc, nxt, epi=EPI_DRELU, G=ws['ys'][i - 1], err=ws['err'])
+            cur = 1 - cur
+        dz0 = ws['dzs'][cur]
+        gw0 = torch.empty(Hc, self.Kc0, **dev32)
+        _wgrad(dz0, ws['xc'], Hc, self.Kc0, gw0)
+        grads['wc0'], grads['bc0'] = gw0, torch.sum(dz0, 0, dtype=torch.float32)
+        # input gradient of colour layer 0: feature part through softplus', tail (x, SH, n, app) as is
+        _dense(dz0, pk['wc0T_feat'], 256, Hc, ws['dzfeat'], epi=EPI_DSOFTPLUS, beta=fa.beta, G=ws['xc'],
+               err=ws['err'])
+        _dense(dz0, pk['wc0T_tail'], 64, Hc, ws['dxc_tail'], epi=EPI_IDENTITY, err=ws['err'])
+        # SDF feature layer
+        gw1 = torch.empty(256, 256, **dev32)
+        _wgrad(ws['dzfeat'], ws['h0c'], 256, 256, gw1)
+        grads['w1'], grads['b1'] = gw1, torch.sum(ws['dzfeat'], 0, dtype=torch.float32)
+        _dense(ws['dzfeat'], pk['w1T'], 256, 256, ws['d_h0c'], epi=EPI_IDENTITY, err=ws['err'])
+        if self.app_dim:
+            g_app = torch.zeros_like(pk['app'])
+            _lib.call("gbsdf_app_grad", R, S, c_vp(_p(offs)), c_vp(app_idx.data_ptr()),
+                      c_vp(ws['dxc_tail'].data_ptr()), 64, 22, self.app_dim, c_vp(g_app.data_ptr()), stream)
+            grads['app'] = g_app
+        # ---------------- field backward ----------------
+        table = sdfm.tcnn_encoding.params
+        d_table = torch.zeros(table.shape, device=dev, dtype=torch.float32)
+        ws['d_whead'].zero_()
+        ws['d_bhead'].zero_()
+        fa.d_sdf, fa.d_grad, fa.d_hess = _p(ws['d_sdf']), _p(ws['d_grad']), _p(ws['d_hess'])
+        fa.d_xc, fa.ld_dxc, fa.normal_col = _p(ws['dxc_tail']), 64, 19
+        fa.d_h0c = _p(ws['d_h0c'])
+        fa.d_table, fa.d_pre0, fa.x0ext = _p(d_table), _p(ws['d_pre0']), _p(ws['x0ext'])
+        fa.d_whead, fa.d_bhead = _p(ws['d_whead']), _p(ws['d_bhead'])
+        _lib.call("gbsdf_field_bwd", ctypes.byref(fa), stream)
+        gw0x = torch.empty(256, self.K0 + 16, **dev32)
+        _wgrad(ws['d_pre0'], ws['x0ext'], 256, self.K0 + 16, gw0x)
+        grads['w0ext'] = gw0x
+        grads['table'] = d_table
+        self._scatter_grads(grads)
+        out = {}
+        if compute_loss:
+            sums = ws['loss_sums'].tolist()
+            l_render = 3.0 * sums[0] / (3.0 * R)
+            l_eik = sums[1] / n_mean
+            l_curv = sums[2] / n_mean
+            loss = lw.render * l_render + lw.eikonal * l_eik + (m.w_curv or 0.0) * l_curv
+            out = dict(loss=loss, l_render=l_render, l_eik=l_eik, l_curv=l_curv)
+        out['rgb'] = ws['rgb']
+        return out
+
+    def check_device_errors(self):
+        """Non-zero when a bounded device wait timed out or a ray was too long."""
+        return int(self.ws['err'].item()) if self.ws is not None else 0
+
+    # ------------------------------------------------------------------ gradients -> masters
+    def _scatter_grads(self, g):
+        """Unscale, map effective-weight gradients onto the weight-norm parameters
+        (W = g v / ||v||) with autograd, and accumulate into the masters' .grad."""
+        m = self.model
+        inv = 1.0 / self.loss_scale
+        sdf = m.neural_sdf
+        A, F = self.A, self.F
+        K0 = self.K0
+        l0, l1 = sdf.mlp.linears[0], sdf.mlp.linears[1]
+        lins = m.neural_rgb.mlp.linears
+        dW0 = torch.zeros_like(l0.weight_v)
+        dW0[:, 3:3 + A * F] = g['w0ext'][:, :A * F]
+        dW0[:, :3] = g['w0ext'][:, K0:K0 + 3]
+        db0 = g['w0ext'][:, K0 + 3]
+        # colour layer 0: undo the column reordering
+        sh = 16
+        Wc0_grad = torch.zeros(lins[0].weight_v.shape, device=dW0.device, dtype=torch.float32)
+        gc0 = g['wc0']
+        Wc0_grad[:, 6 + sh:6 + sh + 256] = gc0[:, :256]
+        Wc0_grad[:, 0:3] = gc0[:, 256:259]
+        Wc0_grad[:, 3:3 + sh] = gc0[:, 259:259 + sh]
+        Wc0_grad[:, 3 + sh:6 + sh] = gc0[:, 259 + sh:262 + sh]
+        if self.app_dim:
+            Wc0_grad[:, 6 + sh + 256:] = gc0[:, 262 + sh:262 + sh + self.app_dim]
+        eff = [(l0, dW0, db0), (l1, g['w1'], g['b1']), (lins[0], Wc0_grad, g['bc0'])]
+        for i in range(1, self.n_rgb_hidden):
+            eff.append((lins[i], g[f'wc{i}'], g[f'bc{i}']))
+        eff.append((lins[-1], g['wl'], g['bl']))
+        for lin, dW, db in eff:
+            with torch.enable_grad():
+                v = lin.weight_v.detach().requires_grad_(True)
+                gg = lin.weight_g.detach().requires_grad_(True)
+                W = v * (gg / v.norm(dim=1, keepdim=True))
+                dv, dg = torch.autograd.grad(W, (v, gg), grad_outputs=dW * inv)
+            _acc(lin.weight_v, dv)
+            _acc(lin.weight_g, dg)
+            _acc(lin.bias, db * inv)
+        _acc(sdf.mlp.linear_sdf.weight, (self.ws['d_whead'] * inv).reshape(1, -1))
+        _acc(sdf.mlp.linear_sdf.bias, self.ws['d_bhead'] * inv)
+        _acc(sdf.tcnn_encoding.params, g['table'].mul_(inv).to(sdf.tcnn_encoding.params.dtype))
+        _acc(m.s_var, (self.ws['d_s_var'] * inv).reshape(()))
+        if self.app_dim:
+            _acc(m.appear_embed.weight, g['app'] * inv)
+
+    def found_inf(self):
+        """True when any master gradient is non-finite (skip the step, halve the scale)."""
+        for prm in self.model.parameters():
+            if prm.grad is not None and not torch.isfinite(prm.grad).all():
+                return True
+        return False
+
+
+def _acc(param, grad):
+    grad = grad.to(param.dtype).reshape(param.shape)
+    if param.grad is None:
+        param.grad = grad
+    else:
+        param.grad.add_(grad)

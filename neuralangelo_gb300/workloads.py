@@ -1,0 +1,96 @@
+"""Seeded synthetic inputs with the benchmark shapes (no datasets are used).
+
+Rays come from cameras on a radius-3 sphere aimed at the origin with seeded
+jitter (all rays hit the unit sphere unless ``miss_frac`` > 0); sample
+distances are stratified in the unit-sphere interval [near, far]
+(projects/nerf/utils/nerf_util.py:20-38 with stratified=True); target colours
+are U[0,1].  Bounds follow Model.get_dist_bounds (projects/neuralangelo/model.py:207-213).
+"""
+import math
+
+import torch
+
+
+def sphere_bounds(center, ray_unit):
+    """intersect_with_sphere (nerf_util.py:199-205) + get_dist_bounds (model.py:207-213)."""
+    ctc = (center * center).sum(-1, keepdim=True)
+    ctv = (center * ray_unit).sum(-1, keepdim=True)
+    disc = ctv ** 2 - (ctc - 1.0)
+    near = (-ctv - disc.sqrt()).clamp(min=0)
+    far = -ctv + disc.sqrt()
+    outside = near.isnan()
+    near = torch.where(outside, torch.ones_like(near), near)
+    far = torch.where(outside, torch.full_like(far, 1.2), far)
+    return near, far, outside
+
+
+def make_rays(R, N, seed=0, miss_frac=0.0, n_images=0, device="cpu"):
+    g = torch.Generator().manual_seed(seed)
+    c = torch.randn(R, 3, generator=g)
+    c = 3.0 * c / c.norm(dim=-1, keepdim=True)
+    d = -c + 0.3 * torch.randn(R, 3, generator=g)
+    n_miss = int(round(miss_frac * R))
+    if n_miss:
+        d[:n_miss] = c[:n_miss]
+    d = d / d.norm(dim=-1, keepdim=True)
+    near, far, outside = sphere_bounds(c, d)
+    u = torch.rand(R, N, generator=g)
+    dists = (torch.arange(N, dtype=torch.float32)[None] + u) / N * (far - near) + near
+    target = torch.rand(R, 3, generator=g)
+    app_idx = torch.randint(0, max(n_images, 1), (R,), generator=g)
+    b = dict(center=c, ray_unit=d, dists=dists, far=far, outside=outside, target=target, app_idx=app_idx)
+    return {k: v.to(device) for k, v in b.items()}
+
+
+def init_field_params(model, seed=0, enc_perturb=1e-2):
+    """Reference initialisation (geometric init already applied by the modules) plus a
+    seeded N(0, enc_perturb) on SDF layer 0's encoding columns: geometric init zeroes
+    them (mlp.py:74-75), which would make every table gradient exactly zero."""
+    g = torch.Generator().manual_seed(seed)
+    with torch.no_grad():
+        lin0 = model.neural_sdf.mlp.linears[0]
+        v = lin0.weight_v
+        pert = torch.randn(v.shape[0], v.shape[1] - 3, generator=g) * enc_perturb
+        v[:, 3:] = pert.to(v)
+        lin0.weight_g.copy_(v.norm(dim=1, keepdim=True))
+        if model.appear_embed is not None:
+            model.appear_embed.weight.copy_(torch.randn(model.appear_embed.weight.shape, generator=g))
+    return model
+
+
+def full_field_iteration(active_levels=8, warm_up_end=5000, step=5000):
+    """The training iteration at which ``active_levels`` levels are annealed in (modules.py:97-100)."""
+    return warm_up_end + active_levels * step
+
+
+def flops_per_sample(cfg, active_levels):
+    """Algorithmic FLOPs of one sample's forward+backward (3x forward MACs x 2), counting
+    only active encoding columns: centre layer0 + feature layer + 6 taps x layer0 + colour MLP."""
+    H = cfg.sdf.mlp.hidden_dim
+    k0 = 3 + active_levels * cfg.sdf.encoding.hashgrid.dim
+    centre = k0 * H + H + H * H
+    taps = 6 * (k0 * H + H)
+    dims = [6 + 16 + H + (cfg.appear_embed.dim if cfg.appear_embed.enabled else 0)]
+    dims += [cfg.rgb.mlp.hidden_dim] * cfg.rgb.mlp.num_layers + [3]
+    rgb = sum(a * b for a, b in zip(dims[:-1], dims[1:]))
+    return 2 * 3 * (centre + taps + rgb)
+
+
+def encoder_bytes_per_sample(active_levels, F, table_bytes, evals=7):
+    """Algorithmic encoder bytes of one sample's forward+backward: every evaluation
+    reads 8 corners x F features per active level and read-modify-writes the same
+    FP32 gradient entries (4 B read + 4 B write)."""
+    return evals * active_levels * 8 * F * (table_bytes + 8)
+
+
+def pct(x):
+    return round(100.0 * x, 2)
+
+
+def median(v):
+    v = sorted(v)
+    n = len(v)
+    return v[n // 2] if n % 2 else 0.5 * (v[n // 2 - 1] + v[n // 2])
+
+
+_ = math

@@ -1,0 +1,117 @@
+"""Move parameters between the package's FieldModel and the oracle's dict layout."""
+import numpy as np
+import torch
+
+from neuralangelo_gb300.config import field_config, rgb_config, sdf_config, to_attr
+from neuralangelo_gb300.model import FieldModel
+
+
+def model_from_golden(g, device, table_dtype=torch.float32):
+    """FieldModel configured like a golden case, with the golden parameters loaded."""
+    c = g['cfg']
+    L, Fd = c['n_levels'], c['n_features']
+    min_logres = int(round(np.log2(c['base_resolution'])))
+    sdf = sdf_config(levels=L, dim=Fd, dict_size=c['log2_hashmap_size'], min_logres=min_logres,
+                     max_logres=None, per_level_scale=c['per_level_scale'], hidden=c['sdf_hidden'],
+                     taps=c['taps'])
+    rgb = rgb_config(layers=c['rgb_layers'], hidden=c['rgb_hidden'])
+    cfg = field_config("small")
+    cfg.sdf, cfg.rgb = sdf, rgb
+    cfg.appear_embed = to_attr(dict(enabled=c['app_dim'] > 0, dim=c['app_dim'], num_images=c['n_images']))
+    model = FieldModel(cfg, table_dtype=table_dtype).to(device)
+    load_oracle_params(model, g['params'])
+    sdfm = model.neural_sdf
+    sdfm.active_levels = c['active_levels']
+    sdfm.anneal_levels = g['anneal']
+    sdfm.set_normal_epsilon()
+    assert abs(sdfm.normal_eps - g['eps']) < 1e-15
+    model.progress = g['progress']
+    model.w_curv = g['w_curv']
+    cfg.loss_weight.eikonal = g['w_eik']
+    return model
+
+
+def load_oracle_params(model, p):
+    with torch.no_grad():
+        s = model.neural_sdf
+        s.tcnn_encoding.params.copy_(p['table'].to(s.tcnn_encoding.params.dtype))
+        for i in range(2):
+            lin = s.mlp.linears[i]
+            lin.weight_v.copy_(p[f'sdf.l{i}.v'])
+            lin.weight_g.copy_(p[f'sdf.l{i}.g'])
+            lin.bias.copy_(p[f'sdf.l{i}.b'])
+        s.mlp.linear_sdf.weight.copy_(p['sdf.head.w'])
+        s.mlp.linear_sdf.bias.copy_(p['sdf.head.b'])
+        for i, lin in enumerate(model.neural_rgb.mlp.linears):
+            lin.weight_v.copy_(p[f'rgb.l{i}.v'])
+            lin.weight_g.copy_(p[f'rgb.l{i}.g'])
+            lin.bias.copy_(p[f'rgb.l{i}.b'])
+        model.s_var.copy_(p['s_var'])
+        if model.appear_embed is not None:
+            model.appear_embed.weight.copy_(p['app'])
+
+
+def model_grads(model):
+    """Gradients of a FieldModel in the oracle's naming."""
+    s = model.neural_sdf
+    g = {'table': s.tcnn_encoding.params.grad, 'sdf.head.w': s.mlp.linear_sdf.weight.grad,
+         'sdf.head.b': s.mlp.linear_sdf.bias.grad, 's_var': model.s_var.grad}
+    for i in range(2):
+        lin = s.mlp.linears[i]
+        g[f'sdf.l{i}.v'], g[f'sdf.l{i}.g'], g[f'sdf.l{i}.b'] = lin.weight_v.grad, lin.weight_g.grad, lin.bias.grad
+    for i, lin in enumerate(model.neural_rgb.mlp.linears):
+        g[f'rgb.l{i}.v'], g[f'rgb.l{i}.g'], g[f'rgb.l{i}.b'] = lin.weight_v.grad, lin.weight_g.grad, lin.bias.grad
+    if model.appear_embed is not None:
+        g['app'] = model.appear_embed.weight.grad
+    return {k: (v.detach().double().cpu() if v is not None else None) for k, v in g.items()}
+
+
+def batch_to(batch, device, dtype=torch.float32):
+    out = {}
+    for k, v in batch.items():
+        if v.dtype in (torch.float64, torch.float32):
+            out[k] = v.to(device=device, dtype=dtype)
+        else:
+            out[k] = v.to(device)
+    return out
+
+
+def model_to_oracle(model, fp16_weights=False):
+    """FieldModel parameters -> the oracle's float64 dict.  With fp16_weights the
+    table and the MLP weight matrices are first rounded to fp16 the way the fused
+    step uses them (weight norm applied in fp32, then rounded; biases, SDF head,
+    s_var and the appearance table stay fp32)."""
+    s = model.neural_sdf
+    p = {}
+
+    def q(t):
+        return t.detach().half().double().cpu() if fp16_weights else t.detach().double().cpu()
+
+    p['table'] = q(s.tcnn_encoding.params)
+    def vg(lin, W):
+        if fp16_weights:
+            return W.double().cpu(), W.double().norm(dim=1, keepdim=True).cpu()
+        return lin.weight_v.detach().double().cpu(), lin.weight_g.detach().double().cpu()
+
+    for i in range(2):
+        lin = s.mlp.linears[i]
+        W = lin.weight.detach()
+        if fp16_weights and i == 0:
+            W = torch.cat([W[:, :3], W[:, 3:].half().float()], dim=1)    # position columns stay fp32
+        elif fp16_weights:
+            W = W.half().float()
+        p[f'sdf.l{i}.v'], p[f'sdf.l{i}.g'] = vg(lin, W)
+        p[f'sdf.l{i}.b'] = lin.bias.detach().double().cpu()
+    p['sdf.head.w'] = s.mlp.linear_sdf.weight.detach().double().cpu()
+    p['sdf.head.b'] = s.mlp.linear_sdf.bias.detach().double().cpu()
+    lins = model.neural_rgb.mlp.linears
+    for i, lin in enumerate(lins):
+        W = lin.weight.detach()
+        if fp16_weights and i != len(lins) - 1:
+            W = W.half().float()
+        p[f'rgb.l{i}.v'], p[f'rgb.l{i}.g'] = vg(lin, W)
+        p[f'rgb.l{i}.b'] = lin.bias.detach().double().cpu()
+    p['s_var'] = model.s_var.detach().double().cpu()
+    if model.appear_embed is not None:
+        p['app'] = model.appear_embed.weight.detach().double().cpu()
+    return p

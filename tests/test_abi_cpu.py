@@ -1,0 +1,62 @@
+"""CPU-side checks of the C ABI: the library loads, exports every symbol the
+header declares, validates arguments, and builds the same level table as the oracle."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from neuralangelo_gb300 import _lib
+from neuralangelo_gb300.build import build
+from oracle import hashgrid as hg
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build()
+    return _lib.load()
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "gbsdf.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*|size_t|int64_t)\s+(gbsdf_\w+)\s*\(", txt, re.M)))
+
+
+def test_exports_every_declared_symbol(lib):
+    syms = header_symbols()
+    assert len(syms) >= 10
+    for s in syms:
+        assert hasattr(lib, s), s
+
+
+def test_version_and_error(lib):
+    assert lib.gbsdf_version() >= 100
+    g = _lib.GridStruct()
+    st = lib.gbsdf_grid_init(ctypes.byref(g), 0, 8, 22, 32, ctypes.c_float(1.3))
+    assert st == 1
+    assert b"n_levels" in lib.gbsdf_last_error()
+
+
+@pytest.mark.parametrize("cfg", [(16, 8, 22, 32, float(np.exp((np.log(2048) - np.log(32)) / 15))),
+                                 (8, 4, 16, 16, 1.5), (8, 4, 10, 16, float(8 ** (1 / 7))),
+                                 (6, 2, 10, 8, float(8 ** (1 / 5)))])
+def test_grid_init_matches_oracle(lib, cfg):
+    from neuralangelo_gb300.encoding import GridLayout
+    lay = GridLayout(*cfg)
+    ref = hg.level_layout(*cfg)
+    np.testing.assert_array_equal(lay.scale, ref['scale'])
+    np.testing.assert_array_equal(lay.resolution, ref['resolution'])
+    np.testing.assert_array_equal(lay.size, ref['size'])
+    np.testing.assert_array_equal(lay.hashed, ref['hashed'])
+    np.testing.assert_array_equal(lay.offset, ref['offset'])
+
+
+def test_null_pointer_rejected_without_gpu(lib):
+    g = _lib.GridStruct()
+    assert lib.gbsdf_grid_init(ctypes.byref(g), 4, 2, 10, 8, ctypes.c_float(1.5)) == 0
+    st = lib.gbsdf_hashgrid_fwd(ctypes.byref(g), 4, None, 10, None, 0, None, 0, None)
+    assert st == 1 and b"NULL" in lib.gbsdf_last_error()
+    assert lib.gbsdf_hashgrid_fwd(ctypes.byref(g), 9, None, 10, None, 0, None, 0, None) == 1

@@ -1,0 +1,58 @@
+"""tcgen05 dense-layer kernel against a float32 torch reference of the same op."""
+import pytest
+import torch
+
+from neuralangelo_gb300 import dense as D
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+
+
+def ref(X, W, b, epi, beta, G):
+    z = X.float() @ W.float().t()
+    if epi in (D.EPI_IDENTITY, D.EPI_RELU, D.EPI_SOFTPLUS) and b is not None:
+        z = z + b
+    if epi == D.EPI_RELU:
+        z = torch.relu(z)
+    elif epi == D.EPI_SOFTPLUS:
+        z = torch.nn.functional.softplus(z, beta=beta)
+    elif epi == D.EPI_DRELU:
+        z = z * (G.float() > 0).float()
+    elif epi == D.EPI_DSOFTPLUS:
+        z = z * (1 - torch.exp(-beta * G.float()))
+    return z
+
+
+@pytest.mark.parametrize("M,K,N", [(128, 64, 256), (1000, 256, 256), (777, 304, 256), (300, 256, 128),
+                                   (129, 32, 64), (5000, 256, 256)])
+@pytest.mark.parametrize("epi", [D.EPI_IDENTITY, D.EPI_RELU, D.EPI_SOFTPLUS, D.EPI_DRELU, D.EPI_DSOFTPLUS])
+def test_dense_matches_torch(M, K, N, epi):
+    g = torch.Generator(DEV).manual_seed(M + K + N + epi)
+    X = (torch.randn(M, K, device=DEV, generator=g) * 0.5).half()
+    W = (torch.randn(N, K, device=DEV, generator=g) / K ** 0.5).half()
+    b = torch.randn(N, device=DEV, generator=g) * 0.1
+    G = None
+    if epi == D.EPI_DRELU:
+        G = torch.randn(M, N, device=DEV, generator=g).half()
+    elif epi == D.EPI_DSOFTPLUS:   # a softplus output is positive
+        G = (torch.rand(M, N, device=DEV, generator=g) * 0.05).half()
+    err = torch.zeros(1, dtype=torch.int32, device=DEV)
+    Y = D.dense(X, W, b, epi=epi, beta=100.0 if epi in (D.EPI_SOFTPLUS, D.EPI_DSOFTPLUS) else 1.0, G=G, err=err)
+    torch.cuda.synchronize()
+    assert int(err) == 0
+    beta = 100.0 if epi in (D.EPI_SOFTPLUS, D.EPI_DSOFTPLUS) else 1.0
+    R = ref(X, W, b, epi, beta, G)
+    e = (Y.float() - R).norm() / R.norm().clamp_min(1e-12)
+    assert e < 2e-3, float(e)
+
+
+def test_dense_strided_output_and_input():
+    M, K, N = 513, 256, 256
+    g = torch.Generator(DEV).manual_seed(7)
+    big = torch.randn(M, 320, device=DEV, generator=g).half()
+    W = (torch.randn(N, K, device=DEV, generator=g) / 16).half()
+    out = torch.zeros(M, 512, device=DEV, dtype=torch.float16)
+    D.dense(big, W, None, epi=D.EPI_RELU, out=out[:, 256:], K=K)
+    R = torch.relu(big[:, :K].float() @ W.float().t())
+    assert ((out[:, 256:].float() - R).norm() / R.norm()) < 2e-3
+    assert torch.all(out[:, :256] == 0)
