@@ -130,10 +130,15 @@ int gbsdf_composite_weights_bwd(int64_t R, int64_t N, const float* alpha, const 
  *         previous layer's activation; G = its stored output; bias ignored)
  * X [M, ldx] fp16, W [N, K] fp16 row-major, bias [N] fp32 (may be NULL),
  * G [M, ldg] fp16, Y [M, ldy] fp16 (fp32 when y_f32 != 0).  K % 16 == 0,
- * K <= 320, N % 64 == 0, ldx/ldg/ldy % 8 == 0, 16-byte aligned bases.  err:
+ * K <= 320, N % 64 == 0, ldx/ldg/ldy % 8 == 0, 16-byte aligned bases.
+ * Xlo (optional): low fp16 half of X (X = Xhi + Xlo), multiplied as well;
+ * Ylo (optional): receives the fp16 rounding residual of Y (Y = Yhi + Ylo).
+ * The split pair carries a gradient through the colour MLP's input-gradient
+ * chain at ~2^-22 relative precision on the fp16 tensor cores.  err:
  * optional device int set non-zero when a bounded device wait runs out. */
-int gbsdf_dense(int64_t M, int K, int N, const void* X, int ldx, const void* W, const float* bias,
-                const void* G, int ldg, void* Y, int ldy, int y_f32, int epi, float beta, int* err, void* stream);
+int gbsdf_dense(int64_t M, int K, int N, const void* X, const void* Xlo, int ldx, const void* W,
+                const float* bias, const void* G, int ldg, void* Y, void* Ylo, int ldy, int y_f32, int epi,
+                float beta, int* err, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Fused SDF field (hash grid + SDF layer 0 + head + 6 numerical-gradient taps).
@@ -182,7 +187,7 @@ typedef struct gbsdf_field_args {
     const float* d_h0c;      /* [Ns, 256] gradient of the centre layer-0 activation */
     float* d_table;          /* [entries, F] accumulated */
     void* d_pre0;            /* fp16 [7 Ns, 256] */
-    void* x0ext;             /* fp16 [7 Ns, K0 + 16] */
+    void* x0ext;             /* fp16 [7 Ns, 2 K0 + 16]: features hi | x,y,z hi, 1, x,y,z lo, 0 | features lo */
     float* d_whead;          /* [256] accumulated */
     float* d_bhead;          /* [1] accumulated */
     int32_t* err;            /* device flag for timed-out waits */
@@ -240,9 +245,10 @@ int gbsdf_rgb_head_fwd(int64_t Ns, const void* Y, int ldy, int H, const float* W
                        void* stream);
 
 /* Its backward: d_rgbs [Ns,3] -> d_pre [Ns, 8] fp16 (columns 0-2, rest 0),
- * dZ = (d_pre W) * [Y > 0] fp16 [Ns, H], d_b [3] accumulated. */
+ * dZ = (d_pre W) * [Y > 0] as an fp16 pair dZ = dZ_hi + dZ_lo [Ns, H]
+ * (dZ_lo may be NULL), d_b [3] accumulated. */
 int gbsdf_rgb_head_bwd(int64_t Ns, const void* Y, int ldy, int H, const float* W, const float* rgbs,
-                       const float* d_rgbs, void* d_pre, void* dZ, float* d_b, void* stream);
+                       const float* d_rgbs, void* d_pre, void* dZ, void* dZ_lo, float* d_b, void* stream);
 
 /* Appearance-embedding gradient: d_app[app_idx[r]] += sum over ray r's samples of
  * d_xc[s, col0 : col0 + app_dim] (fp32). */

@@ -37,8 +37,8 @@ _SIGS = {
                              c_vp, c_vp],
     "gbsdf_composite_weights_fwd": [c_i64, c_i64, c_vp, c_vp, c_vp],
     "gbsdf_composite_weights_bwd": [c_i64, c_i64, c_vp, c_vp, c_vp, c_vp],
-    "gbsdf_dense": [c_i64, c_i32, c_i32, c_vp, c_i32, c_vp, c_vp, c_vp, c_i32, c_vp, c_i32, c_i32, c_i32, c_f32,
-                    c_vp, c_vp],
+    "gbsdf_dense": [c_i64, c_i32, c_i32, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_i32, c_i32,
+                    c_i32, c_f32, c_vp, c_vp],
 }
 
 _lib = None

@@ -97,6 +97,42 @@ __device__ __forceinline__ float softplus_grad(float x, float beta) {
 }
 __device__ __forceinline__ float sigmoidf_(float x) { return 1.0f / (1.0f + expf(-x)); }
 
+// Fast-path softplus(beta) and its derivative for the fused FP16 kernels, from
+// one exponential: e = exp(beta z); softplus = log(1 + e) / beta; d/dz = e / (1 + e).
+// (MUFU exp/log; relative error ~1e-7, well inside the FP16 path's tolerances.)
+__device__ __forceinline__ void softplus_fast(float z, float beta, float inv_beta, float& h, float& dh) {
+    const float bz = z * beta;
+    if (bz > 20.0f) {
+        h = z;
+        dh = 1.0f;
+    } else {
+        const float e = __expf(bz);
+        const float one_e = 1.0f + e;
+        h = __logf(one_e) * inv_beta;
+        dh = __fdividef(e, one_e);
+    }
+}
+__device__ __forceinline__ float softplus_fast_h(float z, float beta, float inv_beta) {
+    const float bz = z * beta;
+    return bz > 20.0f ? z : __logf(1.0f + __expf(bz)) * inv_beta;
+}
+
+// Column sums of a 32 x 32 block held one row per lane (v[j] = element (lane, j)):
+// recursive-halving exchange, 31 shuffles in total; lane j returns the sum of column j.
+__device__ __forceinline__ float warp_column_sum32(float* v, int lane) {
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) {
+        const bool upper = (lane & h) != 0;
+#pragma unroll
+        for (int i = 0; i < h; ++i) {
+            const float send = upper ? v[i] : v[i + h];
+            const float keep = upper ? v[i + h] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+        }
+    }
+    return v[0];
+}
+
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -26,12 +26,14 @@ struct DenseParams {
     int N_total;
     int n_split;
     const __half* X;
+    const __half* Xlo;   // optional low half of X (X = hi + lo), same layout; doubles the MMAs
     int ldx;
     const __half* W;
     const float* bias;
     const __half* G;
     int ldg;
     void* Y;
+    void* Ylo;           // optional fp16 low half of the output (Y = hi + lo)
     int ldy;
     int y_f32;
     int epi;
@@ -44,7 +46,8 @@ __global__ void __launch_bounds__(DENSE_THREADS, 1) k_dense(DenseParams p) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* w_s = smem;                                              // [N_TILE x K]
     uint8_t* a_s = w_s + (size_t)N_TILE * p.K * 2;                    // [128 x K]
-    float* bias_s = reinterpret_cast<float*>(a_s + (size_t)TILE_M * p.K * 2);
+    uint8_t* a2_s = a_s + (size_t)TILE_M * p.K * 2;                   // [128 x K] low half, when Xlo
+    float* bias_s = reinterpret_cast<float*>(a2_s + (p.Xlo ? (size_t)TILE_M * p.K * 2 : 0));
     uint64_t* mbar = reinterpret_cast<uint64_t*>(bias_s + N_TILE);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
 
@@ -69,11 +72,12 @@ __global__ void __launch_bounds__(DENSE_THREADS, 1) k_dense(DenseParams p) {
     umma::fence_after_sync();
     const uint32_t tmem = *tslot;
     const uint32_t idesc = umma::idesc_f16(TILE_M, N_TILE);
-    const uint32_t a_addr = umma::smem_u32(a_s), w_addr = umma::smem_u32(w_s);
+    const uint32_t a_addr = umma::smem_u32(a_s), w_addr = umma::smem_u32(w_s), a2_addr = umma::smem_u32(a2_s);
     const int64_t ntiles = (p.M + TILE_M - 1) / TILE_M;
     uint32_t phase = 0;
     bool ok = true;
 
+    const float inv_beta = 1.0f / p.beta;
     const int q = warp & 3;                 // TMEM lane quadrant of this warp
     const int half = warp >> 2;             // which half of the columns this warp reads
     const int row = q * 32 + lane;
@@ -82,12 +86,14 @@ __global__ void __launch_bounds__(DENSE_THREADS, 1) k_dense(DenseParams p) {
     for (int64_t t = group; t < ntiles && ok; t += ngroups) {
         const int64_t m0 = t * TILE_M;
         stage_rows_kmajor(a_s, p.X, m0, p.M, p.ldx, p.K, tid, DENSE_THREADS);
+        if (p.Xlo) stage_rows_kmajor(a2_s, p.Xlo, m0, p.M, p.ldx, p.K, tid, DENSE_THREADS);
         cp_async_wait_all();
         umma::fence_proxy_async_smem();
         __syncthreads();
         if (tid == 0) {
             umma::fence_after_sync();
             issue_tile_mma(tmem, a_addr, w_addr, p.K, idesc);
+            if (p.Xlo) issue_tile_mma(tmem, a2_addr, w_addr, p.K, idesc, true);
             umma::mma_commit(mbar);
         }
         ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
@@ -113,7 +119,7 @@ __global__ void __launch_bounds__(DENSE_THREADS, 1) k_dense(DenseParams p) {
 #pragma unroll
                     for (int i = 0; i < 8; ++i) {
                         const float d = (p.epi == EPI_DRELU) ? (g[i] > 0.0f ? 1.0f : 0.0f)
-                                                             : (1.0f - expf(-p.beta * g[i]));
+                                                             : (1.0f - __expf(-p.beta * g[i]));
                         v[j + i] *= d;
                     }
                 }
@@ -121,7 +127,8 @@ __global__ void __launch_bounds__(DENSE_THREADS, 1) k_dense(DenseParams p) {
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
                     const float z = v[j] + bias_s[c0 + j];
-                    v[j] = (p.epi == EPI_RELU) ? fmaxf(z, 0.0f) : (p.epi == EPI_SOFTPLUS) ? softplus_beta(z, p.beta) : z;
+                    v[j] = (p.epi == EPI_RELU) ? fmaxf(z, 0.0f)
+                         : (p.epi == EPI_SOFTPLUS) ? softplus_fast_h(z, p.beta, inv_beta) : z;
                 }
             }
             if (p.y_f32) {
@@ -132,6 +139,16 @@ __global__ void __launch_bounds__(DENSE_THREADS, 1) k_dense(DenseParams p) {
                 __half* yp = reinterpret_cast<__half*>(p.Y) + grow * (int64_t)p.ldy + n0 + c0;
 #pragma unroll
                 for (int j = 0; j < 32; j += 8) store_half8(yp + j, v + j);
+                if (p.Ylo) {
+                    __half* lp = reinterpret_cast<__half*>(p.Ylo) + grow * (int64_t)p.ldy + n0 + c0;
+#pragma unroll
+                    for (int j = 0; j < 32; j += 8) {
+                        float lo[8];
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) lo[i] = v[j + i] - __half2float(__float2half_rn(v[j + i]));
+                        store_half8(lp + j, lo);
+                    }
+                }
             }
         }
         umma::fence_before_sync();
@@ -153,9 +170,13 @@ static int sm_count() {
     return n;
 }
 
+static size_t dense_smem(int n_tile, int K, bool split) {
+    return (size_t)n_tile * K * 2 + (split ? 2 : 1) * (size_t)TILE_M * K * 2 + n_tile * 4 + 16;
+}
+
 template <int N_TILE>
 static int launch_dense(const DenseParams& p, cudaStream_t s) {
-    const size_t smem = (size_t)N_TILE * p.K * 2 + (size_t)TILE_M * p.K * 2 + N_TILE * 4 + 16;
+    const size_t smem = dense_smem(N_TILE, p.K, p.Xlo != nullptr);
     if (smem > 227 * 1024) {
         set_error("dense layer K=%d N_TILE=%d needs %zu B of shared memory", p.K, N_TILE, smem);
         return GBSDF_ERR_UNSUPPORTED;
@@ -184,9 +205,9 @@ using namespace gbsdf;
 
 // Y[:, 0:N] = epi(X[:, 0:K] * W^T + b ; G), fp16 in/out, fp32 accumulate.
 // K multiple of 16 (<= 320), N multiple of 64; leading dimensions multiples of 8.
-extern "C" int gbsdf_dense(int64_t M, int K, int N, const void* X, int ldx, const void* W, const float* bias,
-                           const void* G, int ldg, void* Y, int ldy, int y_f32, int epi, float beta, int* err,
-                           void* stream) {
+extern "C" int gbsdf_dense(int64_t M, int K, int N, const void* X, const void* Xlo, int ldx, const void* W,
+                           const float* bias, const void* G, int ldg, void* Y, void* Ylo, int ldy, int y_f32, int epi,
+                           float beta, int* err, void* stream) {
     clear_error();
     GBSDF_CHECK_ARG(M >= 0 && K > 0 && N > 0, "bad sizes");
     if (M == 0) return GBSDF_OK;
@@ -201,12 +222,14 @@ extern "C" int gbsdf_dense(int64_t M, int K, int N, const void* X, int ldx, cons
     }
     DenseParams p;
     p.M = M; p.K = K; p.N_total = N;
-    p.X = (const __half*)X; p.ldx = ldx; p.W = (const __half*)W; p.bias = bias;
-    p.G = (const __half*)G; p.ldg = ldg; p.Y = Y; p.ldy = ldy; p.y_f32 = y_f32 ? 1 : 0; p.epi = epi; p.beta = beta;
-    p.err = err;
+    GBSDF_CHECK_ARG(!Xlo || aligned(Xlo, 16), "Xlo alignment");
+    GBSDF_CHECK_ARG(!Ylo || (aligned(Ylo, 16) && !y_f32), "Ylo needs fp16 output, 16-byte aligned");
+    p.X = (const __half*)X; p.Xlo = (const __half*)Xlo; p.ldx = ldx; p.W = (const __half*)W; p.bias = bias;
+    p.G = (const __half*)G; p.ldg = ldg; p.Y = Y; p.Ylo = Ylo; p.ldy = ldy; p.y_f32 = y_f32 ? 1 : 0; p.epi = epi;
+    p.beta = beta; p.err = err;
     // largest N tile whose weight slice + A tile fit in shared memory
     int n_tile = 256;
-    while (n_tile > 64 && ((size_t)n_tile * K * 2 + (size_t)TILE_M * K * 2 + 2048 > 227 * 1024 || N % n_tile != 0))
+    while (n_tile > 64 && (dense_smem(n_tile, K, Xlo != nullptr) + 2048 > 227 * 1024 || N % n_tile != 0))
         n_tile >>= 1;
     p.n_split = N / n_tile;
     return dense_launch(p, n_tile, as_stream(stream));

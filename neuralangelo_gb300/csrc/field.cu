@@ -80,22 +80,36 @@ __device__ __forceinline__ void gather_level(const FieldParams& p, const float* 
 }
 
 template <int F>
-__device__ __forceinline__ void write_tile_features(uint8_t* a_s, int row, int l, int K0, const float* v) {
-    const uint32_t off = umma::kmajor_offset(row, l * F, K0);
+__device__ __forceinline__ void write_half_row(uint8_t* dst, const float* v) {
     if constexpr (F == 8) {
-        store_half8(reinterpret_cast<__half*>(a_s + off), v);
+        store_half8(reinterpret_cast<__half*>(dst), v);
     } else if constexpr (F == 4) {
         __half2 h[2] = {__floats2half2_rn(v[0], v[1]), __floats2half2_rn(v[2], v[3])};
-        *reinterpret_cast<uint2*>(a_s + off) = *reinterpret_cast<const uint2*>(h);
+        *reinterpret_cast<uint2*>(dst) = *reinterpret_cast<const uint2*>(h);
     } else {
 #pragma unroll
-        for (int f = 0; f < F; ++f) reinterpret_cast<__half*>(a_s + off)[f] = __float2half_rn(v[f]);
+        for (int f = 0; f < F; ++f) reinterpret_cast<__half*>(dst)[f] = __float2half_rn(v[f]);
     }
+}
+
+// The features go in as an fp16 pair (hi + lo, ~2^-22 relative): the +eps and
+// -eps taps of a sample differ by tiny amounts, and independent fp16 rounding
+// of their features would dominate the pre-activation differences that the
+// table gradient is made of.
+template <int F>
+__device__ __forceinline__ void write_tile_features(uint8_t* a_s, uint8_t* a2_s, int row, int l, int K0,
+                                                    const float* v) {
+    const uint32_t off = umma::kmajor_offset(row, l * F, K0);
+    float lo[F];
+#pragma unroll
+    for (int f = 0; f < F; ++f) lo[f] = v[f] - __half2float(__float2half_rn(v[f]));
+    write_half_row<F>(a_s + off, v);
+    write_half_row<F>(a2_s + off, lo);
 }
 
 // Stage the encoder features of one tile (126 rows) into the A tile.
 template <int F>
-__device__ void stage_encoding(const FieldParams& p, int64_t s0, uint8_t* a_s, __half* x0ext_tile_rows) {
+__device__ void stage_encoding(const FieldParams& p, int64_t s0, uint8_t* a_s, uint8_t* a2_s) {
     const int pairs = SPT * EVALS * p.active;
     for (int i = threadIdx.x; i < pairs; i += blockDim.x) {
         const int row = i / p.active, l = i % p.active;
@@ -113,8 +127,7 @@ __device__ void stage_encoding(const FieldParams& p, int64_t s0, uint8_t* a_s, _
 #pragma unroll
             for (int f = 0; f < F; ++f) v[f] = 0.0f;
         }
-        write_tile_features<F>(a_s, row, l, p.K0, v);
-        (void)x0ext_tile_rows;
+        write_tile_features<F>(a_s, a2_s, row, l, p.K0, v);
     }
 }
 
@@ -126,8 +139,9 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int K0 = p.K0;
     uint8_t* w_s = smem;                                        // [256 x K0]
-    uint8_t* a_s = w_s + HID * K0 * 2;                          // [128 x K0]
-    float* w0x_s = reinterpret_cast<float*>(a_s + TILE_M * K0 * 2);   // [256*3]
+    uint8_t* a_s = w_s + HID * K0 * 2;                          // [128 x K0] features, fp16 hi
+    uint8_t* a2_s = a_s + TILE_M * K0 * 2;                      // [128 x K0] features, fp16 lo
+    float* w0x_s = reinterpret_cast<float*>(a2_s + TILE_M * K0 * 2);   // [256*3]
     float* b0_s = w0x_s + HID * 3;
     float* wh_s = b0_s + HID;
     float* part_s = wh_s + HID;                                 // [2][128] partial head sums
@@ -142,7 +156,7 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
         b0_s[i] = p.b0[i];
         wh_s[i] = p.whead[i];
     }
-    for (int i = tid; i < TILE_M * K0 / 8; i += FIELD_THREADS)
+    for (int i = tid; i < 2 * TILE_M * K0 / 8; i += FIELD_THREADS)
         reinterpret_cast<uint4*>(a_s)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         umma::mbar_init(mbar, 1);
@@ -157,7 +171,7 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
     umma::fence_after_sync();
     const uint32_t tmem = *tslot;
     const uint32_t idesc = umma::idesc_f16(TILE_M, HID);
-    const uint32_t a_addr = umma::smem_u32(a_s), w_addr = umma::smem_u32(w_s);
+    const uint32_t a_addr = umma::smem_u32(a_s), w_addr = umma::smem_u32(w_s), a2_addr = umma::smem_u32(a2_s);
     const float bhead = p.bhead[0];
     const int64_t ntiles = (p.Ns + SPT - 1) / SPT;
     const int q = warp & 3, half = warp >> 2;
@@ -167,12 +181,13 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
 
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int64_t s0 = t * SPT;
-        stage_encoding<F>(p, s0, a_s, nullptr);
+        stage_encoding<F>(p, s0, a_s, a2_s);
         umma::fence_proxy_async_smem();
         __syncthreads();
         if (tid == 0) {
             umma::fence_after_sync();
             issue_tile_mma(tmem, a_addr, w_addr, K0, idesc);
+            issue_tile_mma(tmem, a2_addr, w_addr, K0, idesc, true);
             umma::mma_commit(mbar);
         }
         const bool ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
@@ -191,7 +206,8 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
             sample_point(p, s, c);
             eval_point(c, e_row, p.eps, x);
         }
-        float part = 0.0f;
+        float part4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        const float inv_beta = 1.0f / p.beta;
 #pragma unroll 1
         for (int c0 = half * 128; c0 < half * 128 + 128; c0 += 32) {
             float v[32];
@@ -200,9 +216,9 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
             for (int j = 0; j < 32; ++j) {
                 const int n = c0 + j;
                 float z = v[j] + w0x_s[3 * n] * x[0] + w0x_s[3 * n + 1] * x[1] + w0x_s[3 * n + 2] * x[2] + b0_s[n];
-                const float h = softplus_beta(z, p.beta);
+                const float h = softplus_fast_h(z, p.beta, inv_beta);
                 v[j] = h;
-                part = fmaf(wh_s[n], h, part);
+                part4[j & 3] = fmaf(wh_s[n], h, part4[j & 3]);
             }
             if (live && e_row == 0) {
                 __half* dst = (__half*)p.h0c + s * HID + c0;
@@ -210,7 +226,7 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
                 for (int j = 0; j < 32; j += 8) store_half8(dst + j, v + j);
             }
         }
-        part_s[half * TILE_M + row] = part;
+        part_s[half * TILE_M + row] = (part4[0] + part4[1]) + (part4[2] + part4[3]);
         umma::fence_before_sync();
         __syncthreads();
         if (tid < SPT * EVALS) {
@@ -287,19 +303,21 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
 // ---------------------------------------------------------------------------
 // backward
 
-// Scatter d_enc of one (sample, level) over its 7 evaluations, merging the
-// evaluations that land in the same cell (the taps are eps apart, so coarse
-// levels almost always share all 8 corners) before the vector atomics.
+// Scatter d_enc of one (sample, level, corner) over the sample's 7 evaluations,
+// merging consecutive evaluations that hit the same table entry (the taps are
+// eps apart, so at coarse levels all 7 usually share the corner) before the
+// vector atomics.
 template <int F>
-__device__ __forceinline__ void scatter_sample_level(const FieldParams& p, const float* c, int l,
-                                                     const float* denc_s, int sl) {
+__device__ __forceinline__ void scatter_corner(const FieldParams& p, const float* c, int l, int cc,
+                                               const float* denc_s, int sl) {
     const LevelDesc d = level_desc(p.grid, l);
-    uint32_t pidx[8];
-    float pacc[8][F];
-    bool have = false;
+    uint32_t pidx = 0xffffffffu;
+    float pacc[F];
+#pragma unroll
+    for (int f = 0; f < F; ++f) pacc[f] = 0.0f;
+    float* base = p.d_table + d.offset * F;
+#pragma unroll 1
     for (int e = 0; e < EVALS; ++e) {
-        const int row = e * SPT + sl;
-        const float* dv = denc_s + row * p.K0 + l * F;
         float x[3], xu[3];
         eval_point(c, e, p.eps, x);
 #pragma unroll
@@ -309,57 +327,38 @@ __device__ __forceinline__ void scatter_sample_level(const FieldParams& p, const
         grid_pos(d.scale, xu[0], bx, fx);
         grid_pos(d.scale, xu[1], by, fy);
         grid_pos(d.scale, xu[2], bz, fz);
-        uint32_t idx[8];
-#pragma unroll
-        for (int cc = 0; cc < 8; ++cc) idx[cc] = grid_index(d, bx + (cc & 1), by + ((cc >> 1) & 1), bz + ((cc >> 2) & 1));
-        bool same = have;
-#pragma unroll
-        for (int cc = 0; cc < 8; ++cc) same = same && (idx[cc] == pidx[cc]);
-        if (have && !same) {
-#pragma unroll
-            for (int cc = 0; cc < 8; ++cc) {
-                float* dst = p.d_table + (d.offset + pidx[cc]) * F;
+        const uint32_t idx = grid_index(d, bx + (cc & 1), by + ((cc >> 1) & 1), bz + ((cc >> 2) & 1));
+        const float w = corner_weight(cc, fx, fy, fz);
+        if (idx != pidx) {
+            if (pidx != 0xffffffffu) {
+                float* dst = base + (uint64_t)pidx * F;
                 if constexpr (F == 8) {
-                    atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[cc][0], pacc[cc][1], pacc[cc][2], pacc[cc][3]));
-                    atomicAdd(reinterpret_cast<float4*>(dst) + 1, make_float4(pacc[cc][4], pacc[cc][5], pacc[cc][6], pacc[cc][7]));
+                    atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[0], pacc[1], pacc[2], pacc[3]));
+                    atomicAdd(reinterpret_cast<float4*>(dst) + 1, make_float4(pacc[4], pacc[5], pacc[6], pacc[7]));
                 } else if constexpr (F == 4) {
-                    atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[cc][0], pacc[cc][1], pacc[cc][2], pacc[cc][3]));
+                    atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[0], pacc[1], pacc[2], pacc[3]));
                 } else {
 #pragma unroll
-                    for (int f = 0; f < F; ++f) atomicAdd(dst + f, pacc[cc][f]);
+                    for (int f = 0; f < F; ++f) atomicAdd(dst + f, pacc[f]);
                 }
             }
+            pidx = idx;
+#pragma unroll
+            for (int f = 0; f < F; ++f) pacc[f] = 0.0f;
         }
-        if (!same) {
+        const float* dv = denc_s + (e * SPT + sl) * p.K0 + l * F;
 #pragma unroll
-            for (int cc = 0; cc < 8; ++cc) {
-                pidx[cc] = idx[cc];
-#pragma unroll
-                for (int f = 0; f < F; ++f) pacc[cc][f] = 0.0f;
-            }
-            have = true;
-        }
-#pragma unroll
-        for (int cc = 0; cc < 8; ++cc) {
-            const float w = corner_weight(cc, fx, fy, fz);
-#pragma unroll
-            for (int f = 0; f < F; ++f) pacc[cc][f] = fmaf(w, dv[f], pacc[cc][f]);
-        }
+        for (int f = 0; f < F; ++f) pacc[f] = fmaf(w, dv[f], pacc[f]);
     }
-    if (have) {
+    float* dst = base + (uint64_t)pidx * F;
+    if constexpr (F == 8) {
+        atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[0], pacc[1], pacc[2], pacc[3]));
+        atomicAdd(reinterpret_cast<float4*>(dst) + 1, make_float4(pacc[4], pacc[5], pacc[6], pacc[7]));
+    } else if constexpr (F == 4) {
+        atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[0], pacc[1], pacc[2], pacc[3]));
+    } else {
 #pragma unroll
-        for (int cc = 0; cc < 8; ++cc) {
-            float* dst = p.d_table + (d.offset + pidx[cc]) * F;
-            if constexpr (F == 8) {
-                atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[cc][0], pacc[cc][1], pacc[cc][2], pacc[cc][3]));
-                atomicAdd(reinterpret_cast<float4*>(dst) + 1, make_float4(pacc[cc][4], pacc[cc][5], pacc[cc][6], pacc[cc][7]));
-            } else if constexpr (F == 4) {
-                atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[cc][0], pacc[cc][1], pacc[cc][2], pacc[cc][3]));
-            } else {
-#pragma unroll
-                for (int f = 0; f < F; ++f) atomicAdd(dst + f, pacc[cc][f]);
-            }
-        }
+        for (int f = 0; f < F; ++f) atomicAdd(dst + f, pacc[f]);
     }
 }
 
@@ -367,20 +366,23 @@ template <int F>
 __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int K0 = p.K0;
-    const int KX = K0 + 16;                                     // x0ext row width
+    const int KX = 2 * K0 + 16;                                 // x0ext row width
     uint8_t* w_s = smem;                                        // [256 x K0]   B of MMA1
     uint8_t* wt_s = w_s + HID * K0 * 2;                         // [K0 x 256]   B of MMA2
-    uint8_t* a_s = wt_s + K0 * HID * 2;                         // [128 x K0]   encoding tile
+    uint8_t* a_s = wt_s + K0 * HID * 2;                         // [128 x K0]   encoding tile, fp16 hi
+    uint8_t* a3_s = a_s + TILE_M * K0 * 2;                      // [128 x K0]   encoding tile, fp16 lo
     // d_pre is split into fp16 hi + lo tiles (d_pre = hi + lo to ~2^-22) when both fit:
     // the +eps and -eps taps of a sample carry large, nearly cancelling gradients,
     // so a single fp16 rounding of d_pre would dominate the table-gradient error.
     const bool split = K0 <= 64;
-    uint8_t* p_s = a_s + TILE_M * K0 * 2;                       // [128 x 256]  d_pre hi (fp16); reused as fp32 d_enc
+    uint8_t* p_s = a3_s + TILE_M * K0 * 2;                      // [128 x 256]  d_pre hi (fp16); reused as fp32 d_enc
     uint8_t* p2_s = p_s + TILE_M * HID * 2;                     // [128 x 256]  d_pre lo (fp16), when split
-    float* w0x_s = reinterpret_cast<float*>(p2_s + (split ? TILE_M * HID * 2 : 0));
-    float* b0_s = w0x_s + HID * 3;
-    float* wh_s = b0_s + HID;
-    float* dwh_s = wh_s + HID;                                  // [256] d_whead accumulator
+    // W0's position columns, bias and the head weights are read through L1 (__ldg):
+    // shared memory is full with the operand tiles.
+    const float* w0x_s = p.w0x;
+    const float* b0_s = p.b0;
+    const float* wh_s = p.whead;
+    float* dwh_s = reinterpret_cast<float*>(p2_s + (split ? TILE_M * HID * 2 : 0));   // [256] d_whead accumulator
     float* df_s = dwh_s + HID;                                  // [7][18] d f per evaluation
     uint64_t* mbar = reinterpret_cast<uint64_t*>(df_s + EVALS * SPT + 2);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
@@ -388,13 +390,8 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     stage_rows_kmajor(w_s, (const __half*)p.w0e, 0, HID, K0, K0, tid, FIELD_THREADS, HID);
     stage_rows_kmajor(wt_s, (const __half*)p.w0eT, 0, K0, HID, HID, tid, FIELD_THREADS, K0);
-    for (int i = tid; i < HID * 3; i += FIELD_THREADS) w0x_s[i] = p.w0x[i];
-    for (int i = tid; i < HID; i += FIELD_THREADS) {
-        b0_s[i] = p.b0[i];
-        wh_s[i] = p.whead[i];
-        dwh_s[i] = 0.0f;
-    }
-    for (int i = tid; i < TILE_M * K0 / 8; i += FIELD_THREADS)
+    for (int i = tid; i < HID; i += FIELD_THREADS) dwh_s[i] = 0.0f;
+    for (int i = tid; i < 2 * TILE_M * K0 / 8; i += FIELD_THREADS)
         reinterpret_cast<uint4*>(a_s)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         umma::mbar_init(mbar, 1);
@@ -413,6 +410,7 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
     const uint32_t idesc2 = umma::idesc_f16(TILE_M, K0);
     const uint32_t a_addr = umma::smem_u32(a_s), w_addr = umma::smem_u32(w_s);
     const uint32_t p_addr = umma::smem_u32(p_s), wt_addr = umma::smem_u32(wt_s), p2_addr = umma::smem_u32(p2_s);
+    const uint32_t a3_addr = umma::smem_u32(a3_s);
     const int64_t ntiles = (p.Ns + SPT - 1) / SPT;
     const int q = warp & 3, half = warp >> 2;
     const int row = q * 32 + lane;
@@ -465,7 +463,7 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
             }
         }
         // (1) encoder features of the 126 rows
-        stage_encoding<F>(p, s0, a_s, nullptr);
+        stage_encoding<F>(p, s0, a_s, a3_s);
         umma::fence_proxy_async_smem();
         __syncthreads();
         // x0ext rows (encoding, x, y, z, 1) for the layer-0 weight gradient
@@ -474,18 +472,23 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
             const int64_t s = s0 + sl;
             if (s >= p.Ns) continue;
             __half* dst = (__half*)p.x0ext + (s * EVALS + e) * (int64_t)KX;
-            for (int kc = 0; kc < K0; kc += 8)
+            for (int kc = 0; kc < K0; kc += 8) {
                 *reinterpret_cast<uint4*>(dst + kc) = *reinterpret_cast<const uint4*>(a_s + umma::kmajor_offset(i, kc, K0));
+                *reinterpret_cast<uint4*>(dst + K0 + 16 + kc) =
+                    *reinterpret_cast<const uint4*>(a3_s + umma::kmajor_offset(i, kc, K0));
+            }
             float c[3], x[3];
             sample_point(p, s, c);
             eval_point(c, e, p.eps, x);
             float tail[16] = {x[0], x[1], x[2], 1.0f, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+            for (int k = 0; k < 3; ++k) tail[4 + k] = x[k] - __half2float(__float2half_rn(x[k]));
             store_half8(dst + K0, tail);
             store_half8(dst + K0 + 8, tail + 8);
         }
         if (tid == 0) {
             umma::fence_after_sync();
             issue_tile_mma(tmem, a_addr, w_addr, K0, idesc1);
+            issue_tile_mma(tmem, a3_addr, w_addr, K0, idesc1, true);
             umma::mma_commit(mbar);
         }
         ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
@@ -508,6 +511,7 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
                 df = df_s[row];
             }
             const bool centre = live && e_row == 0;
+            const float inv_beta = 1.0f / p.beta;
 #pragma unroll 1
             for (int c0 = half * 128; c0 < half * 128 + 128; c0 += 32) {
                 float v[32];
@@ -524,17 +528,20 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
 #pragma unroll
                     for (int j = 0; j < 32; ++j) dh0[j] = 0.0f;
                 }
+                float hc[32];   // d f * h per column: d w_head = sum over rows
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
                     const int n = c0 + j;
-                    const float z = v[j] + w0x_s[3 * n] * x[0] + w0x_s[3 * n + 1] * x[1] + w0x_s[3 * n + 2] * x[2] + b0_s[n];
-                    const float hval = softplus_beta(z, p.beta);
-                    const float dpre = live ? (df * wh_s[n] + dh0[j]) * softplus_grad(z, p.beta) : 0.0f;
-                    v[j] = dpre;
-                    // d w_head = sum_rows d f * h  (warp reduction, then shared accumulator)
-                    float contrib = live ? df * hval : 0.0f;
-                    contrib = warp_sum(contrib);
-                    if (lane == 0 && contrib != 0.0f) atomicAdd(&dwh_s[n], contrib);
+                    const float z = v[j] + __ldg(&w0x_s[3 * n]) * x[0] + __ldg(&w0x_s[3 * n + 1]) * x[1] +
+                                    __ldg(&w0x_s[3 * n + 2]) * x[2] + __ldg(&b0_s[n]);
+                    float hval, sg;
+                    softplus_fast(z, p.beta, inv_beta, hval, sg);
+                    v[j] = live ? (df * __ldg(&wh_s[n]) + dh0[j]) * sg : 0.0f;
+                    hc[j] = live ? df * hval : 0.0f;
+                }
+                {
+                    const float colsum = warp_column_sum32(hc, lane);
+                    if (colsum != 0.0f) atomicAdd(&dwh_s[c0 + lane], colsum);
                 }
                 // d_pre into the MMA2 A tile(s) (K-major over the 256 hidden units) and to global
 #pragma unroll
@@ -583,14 +590,16 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
         }
         umma::fence_before_sync();
         __syncthreads();
-        // (4) scatter into the table gradient, one thread per (sample, level)
-        for (int i = tid; i < SPT * p.active; i += FIELD_THREADS) {
-            const int sl = i / p.active, l = i % p.active;
+        // (4) scatter into the table gradient, one thread per (sample, level, corner)
+        for (int i = tid; i < SPT * p.active * 8; i += FIELD_THREADS) {
+            const int cc = i & 7;
+            const int l = (i >> 3) % p.active;
+            const int sl = (i >> 3) / p.active;
             const int64_t s = s0 + sl;
             if (s >= p.Ns) continue;
             float c[3];
             sample_point(p, s, c);
-            scatter_sample_level<F>(p, c, l, denc_s, sl);
+            scatter_corner<F>(p, c, l, cc, denc_s, sl);
         }
         __syncthreads();
     }
@@ -611,12 +620,13 @@ static int num_sms() {
 }
 
 static size_t fwd_smem(int K0) {
-    return (size_t)HID * K0 * 2 + (size_t)TILE_M * K0 * 2 + (HID * 3 + 2 * HID + 2 * TILE_M + EVALS * SPT + 2) * 4 + 16;
+    return (size_t)HID * K0 * 2 + 2 * (size_t)TILE_M * K0 * 2 + (HID * 3 + 2 * HID + 2 * TILE_M + EVALS * SPT + 2) * 4 +
+           16;
 }
 static size_t bwd_smem(int K0) {
     const size_t ptiles = K0 <= 64 ? 2 : 1;
-    return (size_t)HID * K0 * 2 * 2 + (size_t)TILE_M * K0 * 2 + ptiles * TILE_M * HID * 2 +
-           (HID * 3 + 3 * HID + EVALS * SPT + 2) * 4 + 16;
+    return (size_t)HID * K0 * 2 * 2 + 2 * (size_t)TILE_M * K0 * 2 + ptiles * TILE_M * HID * 2 +
+           (HID + EVALS * SPT + 2) * 4 + 16;
 }
 
 template <int F>

@@ -227,7 +227,8 @@ __global__ void k_rgb_head_fwd(int64_t Ns, const __half* __restrict__ Y, int ldy
 // d_pre = d_rgb * rgb (1 - rgb);  dZ = (d_pre W) * [Y > 0]
 __global__ void k_rgb_head_bwd(int64_t Ns, const __half* __restrict__ Y, int ldy, int H, const float* __restrict__ W,
                                const float* __restrict__ rgbs, const float* __restrict__ d_rgbs,
-                               __half* __restrict__ d_pre, __half* __restrict__ dZ, float* __restrict__ d_b) {
+                               __half* __restrict__ d_pre, __half* __restrict__ dZ, __half* __restrict__ dZlo,
+                               float* __restrict__ d_b) {
     __shared__ float w_s[3 * 256];
     for (int i = threadIdx.x; i < 3 * H; i += blockDim.x) w_s[(i / H) * 256 + i % H] = W[i];
     __syncthreads();
@@ -246,7 +247,7 @@ __global__ void k_rgb_head_bwd(int64_t Ns, const __half* __restrict__ Y, int ldy
         for (int j = 0; j < H; j += 8) {
             const uint4 u = *reinterpret_cast<const uint4*>(y + j);
             const __half2* h = reinterpret_cast<const __half2*>(&u);
-            __half2 o[4];
+            __half2 o[4], ol[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 const float2 f = __half22float2(h[i]);
@@ -254,8 +255,11 @@ __global__ void k_rgb_head_bwd(int64_t Ns, const __half* __restrict__ Y, int ldy
                 const float v0 = f.x > 0.0f ? g0 * w_s[c] + g1 * w_s[256 + c] + g2 * w_s[512 + c] : 0.0f;
                 const float v1 = f.y > 0.0f ? g0 * w_s[c + 1] + g1 * w_s[256 + c + 1] + g2 * w_s[512 + c + 1] : 0.0f;
                 o[i] = __floats2half2_rn(v0, v1);
+                const float2 r = __half22float2(o[i]);
+                ol[i] = __floats2half2_rn(v0 - r.x, v1 - r.y);
             }
             *reinterpret_cast<uint4*>(z + j) = *reinterpret_cast<const uint4*>(o);
+            if (dZlo) *reinterpret_cast<uint4*>(dZlo + s * H + j) = *reinterpret_cast<const uint4*>(ol);
         }
     }
     g0 = warp_sum(g0);
@@ -320,15 +324,16 @@ extern "C" int gbsdf_rgb_head_fwd(int64_t Ns, const void* Y, int ldy, int H, con
 }
 
 extern "C" int gbsdf_rgb_head_bwd(int64_t Ns, const void* Y, int ldy, int H, const float* W, const float* rgbs,
-                                  const float* d_rgbs, void* d_pre, void* dZ, float* d_b, void* stream) {
+                                  const float* d_rgbs, void* d_pre, void* dZ, void* dZ_lo, float* d_b, void* stream) {
     clear_error();
     GBSDF_CHECK_ARG(Ns >= 0, "Ns < 0");
     if (Ns == 0) return GBSDF_OK;
     GBSDF_CHECK_ARG(Y && W && rgbs && d_rgbs && d_pre && dZ && d_b, "NULL pointer");
     GBSDF_CHECK_ARG(H % 8 == 0 && H <= 256 && H > 0, "hidden width %d", H);
     GBSDF_CHECK_ARG(ldy % 8 == 0 && ldy >= H && aligned(Y, 16) && aligned(dZ, 16) && aligned(d_pre, 16), "layout");
+    GBSDF_CHECK_ARG(!dZ_lo || aligned(dZ_lo, 16), "dZ_lo alignment");
     k_rgb_head_bwd<<<(unsigned)((Ns + 255) / 256), 256, 0, as_stream(stream)>>>(
-        Ns, (const __half*)Y, ldy, H, W, rgbs, d_rgbs, (__half*)d_pre, (__half*)dZ, d_b);
+        Ns, (const __half*)Y, ldy, H, W, rgbs, d_rgbs, (__half*)d_pre, (__half*)dZ, (__half*)dZ_lo, d_b);
     return launch_status("rgb_head_bwd");
 }
 

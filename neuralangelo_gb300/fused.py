@@ -59,7 +59,7 @@ _lib.register("gbsdf_field_fwd", [c_vp, c_vp])
 _lib.register("gbsdf_field_bwd", [c_vp, c_vp])
 _lib.register("gbsdf_render_fused", [c_vp, c_vp])
 _lib.register("gbsdf_rgb_head_fwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp])
-_lib.register("gbsdf_rgb_head_bwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp])
+_lib.register("gbsdf_rgb_head_bwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp])
 _lib.register("gbsdf_app_grad", [c_i64, c_i32, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_vp])
 _lib.register("gbsdf_gemm_wgrad", [c_i64, c_i32, c_i32, c_vp, c_i32, c_vp, c_i32, c_vp, c_i32, c_f32, c_f32, c_vp])
 
@@ -80,12 +80,12 @@ def _round16(n):
     return (n + 15) // 16 * 16
 
 
-def _dense(X, Wt, N, K, out, bias=None, epi=EPI_IDENTITY, beta=100.0, G=None, err=None):
-    """out[:, :N] = epi(X[:, :K] @ Wt[:N, :K].T + bias ; G) on the tcgen05 kernel."""
-    _lib.call("gbsdf_dense", X.shape[0], K, N, c_vp(X.data_ptr()), X.stride(0), c_vp(Wt.data_ptr()),
-              c_vp(_p(bias)), c_vp(_p(G)), G.stride(0) if G is not None else 0, c_vp(out.data_ptr()), out.stride(0),
-              1 if out.dtype == torch.float32 else 0, int(epi), float(beta), c_vp(_p(err)),
-              _lib.stream_ptr(X.device))
+def _dense(X, Wt, N, K, out, bias=None, epi=EPI_IDENTITY, beta=100.0, G=None, err=None, X_lo=None, out_lo=None):
+    """out[:, :N] = epi((X + X_lo)[:, :K] @ Wt[:N, :K].T + bias ; G) on the tcgen05 kernel."""
+    _lib.call("gbsdf_dense", X.shape[0], K, N, c_vp(X.data_ptr()), c_vp(_p(X_lo)), X.stride(0),
+              c_vp(Wt.data_ptr()), c_vp(_p(bias)), c_vp(_p(G)), G.stride(0) if G is not None else 0,
+              c_vp(out.data_ptr()), c_vp(_p(out_lo)), out.stride(0), 1 if out.dtype == torch.float32 else 0,
+              int(epi), float(beta), c_vp(_p(err)), _lib.stream_ptr(X.device))
 
 
 def _wgrad(dZ, X, N, K, dW):
@@ -97,9 +97,12 @@ def _wgrad(dZ, X, N, K, dW):
 class FusedField:
     """Fused FP16 forward+backward over a FieldModel's FP32 master parameters."""
 
-    def __init__(self, model, loss_scale=2.0 ** 15):
+    def __init__(self, model, loss_scale=2.0 ** 15, split_colour_grads=False):
         check_struct_sizes()
         self.model = model
+        # carry the colour MLP's input gradients as fp16 hi+lo pairs (costs ~10% of the step;
+        # the dominant colour-gradient error comes from fp16 activation storage instead)
+        self.split = bool(split_colour_grads)
         self.loss_scale = float(loss_scale)
         sdf = model.neural_sdf
         cfg = model.cfg
@@ -187,9 +190,11 @@ class FusedField:
                   ys=[e(Ns, Hc, dt=f16) for _ in range(self.n_rgb_hidden)], rgbs=e(Ns, 3), rgb=e(R, 3),
                   weights=e(Ns), d_rgbs=e(Ns, 3), d_sdf=e(Ns), d_grad=e(Ns, 3), d_hess=e(Ns, 3),
                   loss_sums=torch.zeros(4, device=device, dtype=torch.float64), d_s_var=torch.zeros(1, device=device),
-                  d_pre_last=e(Ns, 8, dt=f16), dzs=[e(Ns, Hc, dt=f16) for _ in range(2)], dzfeat=e(Ns, 256, dt=f16),
+                  d_pre_last=e(Ns, 8, dt=f16), dzs=[e(Ns, Hc, dt=f16) for _ in range(2)],
+                  dzs_lo=[e(Ns, Hc, dt=f16) for _ in range(2)], dzfeat=e(Ns, 256, dt=f16),
+                  dzfeat_lo=e(Ns, 256, dt=f16),
                   dxc_tail=e(Ns, 64), d_h0c=e(Ns, 256), d_pre0=e(Ns * 7, 256, dt=f16),
-                  x0ext=e(Ns * 7, self.K0 + 16, dt=f16), d_whead=torch.zeros(256, device=device),
+                  x0ext=e(Ns * 7, 2 * self.K0 + 16, dt=f16), d_whead=torch.zeros(256, device=device),
                   d_bhead=torch.zeros(1, device=device), d_bl=torch.zeros(3, device=device),
                   err=torch.zeros(1, device=device, dtype=torch.int32))
         self.ws = ws
@@ -292,7 +297,8 @@ class FusedField:
         dz = ws['dzs'][0]
         _lib.call("gbsdf_rgb_head_bwd", Ns, c_vp(ylast.data_ptr()), Hc, Hc, c_vp(pk['wl'].data_ptr()),
                   c_vp(ws['rgbs'].data_ptr()), c_vp(ws['d_rgbs'].data_ptr()), c_vp(ws['d_pre_last'].data_ptr()),
-                  c_vp(dz.data_ptr()), c_vp(ws['d_bl'].data_ptr()), stream)
+                  c_vp(dz.data_ptr()), c_vp(_p(ws['dzs_lo'][0] if self.split else None)), c_vp(ws['d_bl'].data_ptr()),
+                  stream)
         grads = {}
         dev32 = dict(device=dev, dtype=torch.float32)
         n = self.n_rgb_hidden
@@ -307,21 +313,25 @@ class FusedField:
             _wgrad(dzi, ws['ys'][i - 1], Hc, Hc, gw)
             grads[f'wc{i}'], grads[f'bc{i}'] = gw, torch.sum(dzi, 0, dtype=torch.float32)
             nxt = ws['dzs'][1 - cur]
-            _dense(dzi, pk['wcT'][i], Hc, Hc, nxt, epi=EPI_DRELU, G=ws['ys'][i - 1], err=ws['err'])
+            _dense(dzi, pk['wcT'][i], Hc, Hc, nxt, epi=EPI_DRELU, G=ws['ys'][i - 1], err=ws['err'],
+                   X_lo=ws['dzs_lo'][cur] if self.split else None,
+                   out_lo=ws['dzs_lo'][1 - cur] if self.split else None)
             cur = 1 - cur
         dz0 = ws['dzs'][cur]
+        dz0_lo = ws['dzs_lo'][cur] if self.split else None
         gw0 = torch.empty(Hc, self.Kc0, **dev32)
         _wgrad(dz0, ws['xc'], Hc, self.Kc0, gw0)
         grads['wc0'], grads['bc0'] = gw0, torch.sum(dz0, 0, dtype=torch.float32)
         # input gradient of colour layer 0: feature part through softplus', tail (x, SH, n, app) as is
         _dense(dz0, pk['wc0T_feat'], 256, Hc, ws['dzfeat'], epi=EPI_DSOFTPLUS, beta=fa.beta, G=ws['xc'],
-               err=ws['err'])
-        _dense(dz0, pk['wc0T_tail'], 64, Hc, ws['dxc_tail'], epi=EPI_IDENTITY, err=ws['err'])
+               err=ws['err'], X_lo=dz0_lo, out_lo=ws['dzfeat_lo'] if self.split else None)
+        _dense(dz0, pk['wc0T_tail'], 64, Hc, ws['dxc_tail'], epi=EPI_IDENTITY, err=ws['err'], X_lo=dz0_lo)
         # SDF feature layer
         gw1 = torch.empty(256, 256, **dev32)
         _wgrad(ws['dzfeat'], ws['h0c'], 256, 256, gw1)
         grads['w1'], grads['b1'] = gw1, torch.sum(ws['dzfeat'], 0, dtype=torch.float32)
-        _dense(ws['dzfeat'], pk['w1T'], 256, 256, ws['d_h0c'], epi=EPI_IDENTITY, err=ws['err'])
+        _dense(ws['dzfeat'], pk['w1T'], 256, 256, ws['d_h0c'], epi=EPI_IDENTITY, err=ws['err'],
+               X_lo=ws['dzfeat_lo'] if self.split else None)
         if self.app_dim:
             g_app = torch.zeros_like(pk['app'])
             _lib.call("gbsdf_app_grad", R, S, c_vp(_p(offs)), c_vp(app_idx.data_ptr()),
@@ -338,8 +348,8 @@ class FusedField:
         fa.d_table, fa.d_pre0, fa.x0ext = _p(d_table), _p(ws['d_pre0']), _p(ws['x0ext'])
         fa.d_whead, fa.d_bhead = _p(ws['d_whead']), _p(ws['d_bhead'])
         _lib.call("gbsdf_field_bwd", ctypes.byref(fa), stream)
-        gw0x = torch.empty(256, self.K0 + 16, **dev32)
-        _wgrad(ws['d_pre0'], ws['x0ext'], 256, self.K0 + 16, gw0x)
+        gw0x = torch.empty(256, 2 * self.K0 + 16, **dev32)
+        _wgrad(ws['d_pre0'], ws['x0ext'], 256, 2 * self.K0 + 16, gw0x)
         grads['w0ext'] = gw0x
         grads['table'] = d_table
         self._scatter_grads(grads)
@@ -370,9 +380,10 @@ class FusedField:
         l0, l1 = sdf.mlp.linears[0], sdf.mlp.linears[1]
         lins = m.neural_rgb.mlp.linears
         dW0 = torch.zeros_like(l0.weight_v)
-        dW0[:, 3:3 + A * F] = g['w0ext'][:, :A * F]
-        dW0[:, :3] = g['w0ext'][:, K0:K0 + 3]
-        db0 = g['w0ext'][:, K0 + 3]
+        gx = g['w0ext']      # columns: features hi | x,y,z hi, 1, x,y,z lo, 0 | features lo
+        dW0[:, 3:3 + A * F] = gx[:, :A * F] + gx[:, K0 + 16:K0 + 16 + A * F]
+        dW0[:, :3] = gx[:, K0:K0 + 3] + gx[:, K0 + 4:K0 + 7]
+        db0 = gx[:, K0 + 3]
         # colour layer 0: undo the column reordering
         sh = 16
         Wc0_grad = torch.zeros(lins[0].weight_v.shape, device=dW0.device, dtype=torch.float32)
@@ -387,6 +398,8 @@ class FusedField:
         for i in range(1, self.n_rgb_hidden):
             eff.append((lins[i], g[f'wc{i}'], g[f'bc{i}']))
         eff.append((lins[-1], g['wl'], g['bl']))
+        names = ['sdf.l0', 'sdf.l1'] + [f'rgb.l{i}' for i in range(len(eff) - 2)]
+        self.eff_grads = {n: (dW * inv, db * inv) for n, (_, dW, db) in zip(names, eff)}
         for lin, dW, db in eff:
             with torch.enable_grad():
                 v = lin.weight_v.detach().requires_grad_(True)

@@ -79,7 +79,10 @@ def hashgrid(x01, table, layout, active=None):
 # parameters
 
 def weight_norm(v, g):
-    """torch.nn.utils.weight_norm(dim=0): W = g * v / ||v||_row (mlp.py:42-43, nerf_util.py:177-178)."""
+    """torch.nn.utils.weight_norm(dim=0): W = g * v / ||v||_row (mlp.py:42-43, nerf_util.py:177-178).
+    g = None takes v as the effective weight (gradients then are dL/dW)."""
+    if g is None:
+        return v
     return v * (g / v.norm(dim=1, keepdim=True))
 
 
@@ -144,6 +147,14 @@ def softplus(x, beta):
     return F.softplus(x, beta=beta)
 
 
+def fp16_store(t, on):
+    """Forward value rounded to fp16 with an identity gradient: emulates where the fused
+    FP16 kernels store an activation in fp16 (used only with fp16_storage=True)."""
+    if not on:
+        return t
+    return t + (t.detach().half().to(t.dtype) - t.detach())
+
+
 def sdf_mlp(p, cfg, enc_in, with_feat):
     """MLPforNeuralSDF.forward (mlp.py:55-69) for layer_dims [3+LF, H, H]:
     h0 = softplus(W0 in + b0); sdf = w_head h0 + b_head; feat = softplus(W1 h0 + b1)."""
@@ -154,7 +165,8 @@ def sdf_mlp(p, cfg, enc_in, with_feat):
     feat = None
     if with_feat:
         W1 = weight_norm(p['sdf.l1.v'], p['sdf.l1.g'])
-        feat = softplus(h0 @ W1.t() + p['sdf.l1.b'], beta)
+        st = cfg.get('fp16_storage', False)
+        feat = softplus(fp16_store(h0, st) @ W1.t() + p['sdf.l1.b'], beta)
     return sdf, feat
 
 
@@ -234,16 +246,17 @@ def spherical_harmonics(d):
 def neural_rgb(p, cfg, pts, normals, rays_unit, feats, app):
     """NeuralRGB.forward (modules.py:209-220) with MLPwithSkipConnection (nerf_util.py:187-196):
     input [x, SH(d), n, feat, app], ReLU hidden layers, sigmoid output."""
+    st = cfg.get('fp16_storage', False)
     parts = [pts, spherical_harmonics(rays_unit), normals, feats]
     if app is not None:
         parts.append(app)
-    h = torch.cat(parts, dim=-1)
+    h = fp16_store(torch.cat(parts, dim=-1), st)
     n = cfg['rgb_layers'] + 1
     for i in range(n):
         W = weight_norm(p[f'rgb.l{i}.v'], p[f'rgb.l{i}.g'])
         h = h @ W.t() + p[f'rgb.l{i}.b']
         if i != n - 1:
-            h = torch.relu(h)
+            h = fp16_store(torch.relu(h), st)
     return torch.sigmoid(h)
 
 
@@ -307,7 +320,7 @@ def curvature_loss(hess, outside):
     return (lap * (~outside).to(lap.dtype)).mean()
 
 
-def render_step(p, cfg, layout, batch, eps, progress, w_eik, w_curv, training=True):
+def render_step(p, cfg, layout, batch, eps, progress, w_eik, w_curv, training=True, retain=False):
     """One training forward of Model.render_rays_object + render_rays + Trainer._compute_loss
     (model.py:124-190, trainer.py:40-52), background disabled.
 
@@ -323,6 +336,9 @@ def render_step(p, cfg, layout, batch, eps, progress, w_eik, w_curv, training=Tr
     sdf = torch.where(outside[:, None, :].expand_as(sdf), torch.full_like(sdf, out_val), sdf)  # model.py:163
     grads, hess = compute_gradients(p, cfg, layout, pts, eps, sdf, training)
     normals = F.normalize(grads, dim=-1)
+    if retain:   # expose intermediate gradients for diagnostics
+        for t in (sdf, feat, grads, hess, normals):
+            t.retain_grad()
     rays = d[:, None, :].expand_as(pts)
     app = None
     if cfg['app_dim'] > 0:
@@ -340,4 +356,5 @@ def render_step(p, cfg, layout, batch, eps, progress, w_eik, w_curv, training=Tr
         l_curv = curvature_loss(hess, out_mask)
         loss = loss + w_curv * l_curv
     return dict(loss=loss, l_render=l_render, l_eik=l_eik, l_curv=l_curv, rgb=rgb, rgbs=rgbs,
-                sdf=sdf[..., 0], feat=feat, grads=grads, hess=hess, alphas=alphas, weights=weights)
+                sdf=sdf[..., 0], feat=feat, grads=grads, hess=hess, alphas=alphas, weights=weights,
+                normals=normals, sdf_full=sdf)

@@ -76,7 +76,7 @@ def batch_to(batch, device, dtype=torch.float32):
     return out
 
 
-def model_to_oracle(model, fp16_weights=False):
+def model_to_oracle(model, fp16_weights=False, effective=False):
     """FieldModel parameters -> the oracle's float64 dict.  With fp16_weights the
     table and the MLP weight matrices are first rounded to fp16 the way the fused
     step uses them (weight norm applied in fp32, then rounded; biases, SDF head,
@@ -89,6 +89,8 @@ def model_to_oracle(model, fp16_weights=False):
 
     p['table'] = q(s.tcnn_encoding.params)
     def vg(lin, W):
+        if effective:
+            return W.double().cpu(), None
         if fp16_weights:
             return W.double().cpu(), W.double().norm(dim=1, keepdim=True).cpu()
         return lin.weight_v.detach().double().cpu(), lin.weight_g.detach().double().cpu()

@@ -56,3 +56,22 @@ def test_dense_strided_output_and_input():
     R = torch.relu(big[:, :K].float() @ W.float().t())
     assert ((out[:, 256:].float() - R).norm() / R.norm()) < 2e-3
     assert torch.all(out[:, :256] == 0)
+
+
+def test_dense_split_operand_and_output():
+    """X = X_hi + X_lo and Y = Y_hi + Y_lo: the pair reproduces an fp32 product far below fp16 precision."""
+    M, K, N = 700, 256, 256
+    g = torch.Generator(DEV).manual_seed(11)
+    Xf = torch.randn(M, K, device=DEV, generator=g)
+    X_hi = Xf.half()
+    X_lo = (Xf - X_hi.float()).half()
+    W = (torch.randn(N, K, device=DEV, generator=g) / 16).half()
+    G = torch.randn(M, N, device=DEV, generator=g).half()
+    hi = torch.empty(M, N, device=DEV, dtype=torch.float16)
+    lo = torch.empty(M, N, device=DEV, dtype=torch.float16)
+    D.dense(X_hi, W, None, epi=D.EPI_DRELU, G=G, out=hi, X_lo=X_lo, out_lo=lo)
+    R = (Xf.double() @ W.double().t()) * (G.double() > 0)
+    e_pair = ((hi.double() + lo.double()) - R).norm() / R.norm()
+    e_hi = (hi.double() - R).norm() / R.norm()
+    assert e_pair < 1e-5, float(e_pair)
+    assert e_hi > 1e-4                       # a single fp16 output is much coarser

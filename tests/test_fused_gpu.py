@@ -42,7 +42,7 @@ def build(log2T=14, n_images=10, seed=0, table_range=0.05, rgb_layers=4, rgb_hid
     return model
 
 
-def oracle_run(model, batch, fp16):
+def oracle_run(model, batch, fp16, effective=False, retain=False, fp16_storage=False):
     c = model.cfg
     hg = c.sdf.encoding.hashgrid
     ocfg = of.make_config(n_levels=c.sdf.encoding.levels, n_features=hg.dim, log2_hashmap_size=hg.dict_size,
@@ -51,14 +51,17 @@ def oracle_run(model, batch, fp16):
                           rgb_hidden=c.rgb.mlp.hidden_dim, rgb_layers=c.rgb.mlp.num_layers,
                           app_dim=c.appear_embed.dim if c.appear_embed.enabled else 0,
                           n_images=c.appear_embed.num_images if c.appear_embed.enabled else 0)
+    ocfg['fp16_storage'] = fp16_storage
     from oracle import hashgrid as hgo
     layout = hgo.level_layout(ocfg['n_levels'], ocfg['n_features'], ocfg['log2_hashmap_size'],
                               ocfg['base_resolution'], ocfg['per_level_scale'])
-    p = {k: v.clone().requires_grad_(True) for k, v in params_io.model_to_oracle(model, fp16).items()}
+    p = {k: (v.clone().requires_grad_(True) if v is not None else None)
+         for k, v in params_io.model_to_oracle(model, fp16, effective).items()}
     b = {k: (v.double().cpu() if v.is_floating_point() else v.cpu()) for k, v in batch.items()}
-    out = of.render_step(p, ocfg, layout, b, model.neural_sdf.normal_eps, model.progress, 0.1, model.w_curv)
+    out = of.render_step(p, ocfg, layout, b, model.neural_sdf.normal_eps, model.progress, 0.1, model.w_curv,
+                         retain=retain)
     out['loss'].backward()
-    return out, {k: v.grad for k, v in p.items()}
+    return out, {k: (v.grad if v is not None else None) for k, v in p.items()}
 
 
 def fused_grads(model):
@@ -86,23 +89,44 @@ def test_fused_matches_oracle(small):
     e_tab = rel(mine['table'], g_q['table'])
     e_rgb = rel(rgb_mine, out_q['rgb'].detach())
     e_loss = abs(res['loss'] - float(out_q['loss'])) / abs(float(out_q['loss']))
-    # every parameter against the oracle on the FP32 masters
-    out_m, g_m = oracle_run(model, batch, fp16=False)
+    # every weight gradient in effective-weight space against the oracle on the same fp16 weights
+    out_e, g_e = oracle_run(model, batch, fp16=True, effective=True, retain=True)
     worst = {}
-    for k, v in g_m.items():
-        if v is None or mine.get(k) is None or float(np.linalg.norm(v)) == 0.0:
-            continue
-        worst[k] = rel(mine[k], v)
-    allp = rel(np.concatenate([mine[k].reshape(-1) for k in worst]),
-               np.concatenate([g_m[k].reshape(-1) for k in worst]))
+    for name, (dW, db) in ff.eff_grads.items():
+        worst[name + '.W'] = rel(dW.double().cpu(), g_e[name + '.v'])
+        worst[name + '.b'] = rel(db.double().cpu(), g_e[name + '.b'])
+    for k in ('sdf.head.w', 'sdf.head.b', 's_var', 'app'):
+        if k in g_e and g_e[k] is not None:
+            worst[k] = rel(mine[k], g_e[k])
+    allp = rel(np.concatenate([ff.eff_grads[n][0].double().cpu().reshape(-1) for n in ff.eff_grads] +
+                              [mine['table'].reshape(-1)]),
+               np.concatenate([g_e[n + '.v'].reshape(-1) for n in ff.eff_grads] + [g_e['table'].reshape(-1)]))
+    # intermediate gradients (loss-scaled buffers of the fused step) against the oracle's
+    sc = ff.loss_scale
+    ins = inside[:, None].expand(R, S)
+    diag = dict(
+        d_normal=rel(ff.ws['dxc_tail'][:, 19:22].reshape(R, S, 3).cpu() / sc, out_e['normals'].grad),
+        d_hess=rel((ff.ws['d_hess'].reshape(R, S, 3).cpu() / sc)[ins], out_e['hess'].grad[ins]),
+    )
+    # the same oracle with the fused path's fp16 activation storage emulated: isolates the
+    # arithmetic of the fused backward from the precision of fp16 activation storage
+    out_s, g_s = oracle_run(model, batch, fp16=True, effective=True, fp16_storage=True)
+    storage = {}
+    for name, (dW, db) in ff.eff_grads.items():
+        storage[name + '.W'] = rel(dW.double().cpu(), g_s[name + '.v'])
     print(f"\nsdf {e_sdf:.2e} table {e_tab:.2e} rgb {e_rgb:.2e} loss {e_loss:.2e} all-params {allp:.2e}")
-    print({k: f"{v:.1e}" for k, v in worst.items()})
-    assert e_sdf < 1e-4
-    assert e_rgb < 2e-3
-    assert e_loss < 2e-3
-    assert e_tab < 1e-3
-    for k, e in worst.items():
-        assert e < 1e-2, (k, e)
+    print("vs fp16-weight oracle", {k: f"{v:.1e}" for k, v in worst.items()})
+    print("vs fp16-storage oracle", {k: f"{v:.1e}" for k, v in storage.items()})
+    print({k: f"{v:.1e}" for k, v in diag.items()})
+    assert e_sdf < 1e-4                      # SDF gate
+    assert e_tab < 1e-3                      # table-gradient gate
+    assert e_rgb < 1e-4
+    assert e_loss < 1e-5
+    assert allp < 5e-3
+    for k, e in worst.items():               # bounded by fp16 activation storage (see below)
+        assert e < 2e-2, (k, e)
+    for k, e in storage.items():             # the backward arithmetic itself
+        assert e < 5e-3, (k, e)
 
 
 def test_fused_matches_plain_full_table():
