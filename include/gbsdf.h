@@ -255,6 +255,35 @@ int gbsdf_rgb_head_bwd(int64_t Ns, const void* Y, int ldy, int H, const float* W
 int gbsdf_app_grad(int64_t R, int32_t S, const int64_t* ray_offsets, const int32_t* app_idx, const void* d_xc,
                    int ld_dxc, int col0, int app_dim, float* d_app, void* stream);
 
+/* SDF at points (pts [M,3]) or on a lattice block (pts NULL: point m = (i, j, k)
+ * x-major with coordinates ax[i], ay[j], az[k], nx*ny*nz == M), times sign.
+ * Replaces NeuralSDF.sdf (modules.py:73-74) as called by extract_mesh
+ * (mesh.py:33-35, sign -1 per scripts/extract_mesh.py:85) and by the sampler's
+ * no-grad evaluations (model.py:238, 245).  Only the weight fields of args are
+ * read (grid, active, K0, table, w0e, w0x, b0, whead, bhead, beta, err). */
+int gbsdf_sdf_points(const gbsdf_field_args* args, int64_t M, const float* pts, const float* ax, const float* ay,
+                     const float* az, int nx, int ny, int nz, float sign, float* out, void* stream);
+
+/* Canonical marching-cubes case table (host-only): tri [256][16][3] edge ids
+ * (-1 padded), count [256] triangles per configuration. */
+int gbsdf_mc_table(int32_t* tri, int32_t* count);
+
+/* Workspace bytes for gbsdf_mc_block on an nx x ny x nz block. */
+size_t gbsdf_mc_workspace_size(int nx, int ny, int nz);
+
+/* Marching cubes at iso of one block (vol [nx,ny,nz] float32 device, x-major),
+ * vertices in world space V = index position * intv + origin (origin: 3 doubles,
+ * HOST pointer), then the unit-sphere filter (mesh.py:119-148).
+ * Replaces mcubes.marching_cubes + filter_points_outside_bounding_sphere.
+ * V [V_cap, 3] double and F [F_cap, 3] int64 (device) must hold the worst case
+ * (3 nx ny nz vertices, 5 (nx-1)(ny-1)(nz-1) faces); counts [2] (device) gets
+ * the kept vertex and face counts.  workspace: gbsdf_mc_workspace_size bytes,
+ * 256-byte aligned.  The first call on a device uploads the case table to
+ * constant memory (make it before any stream capture). */
+int gbsdf_mc_block(const float* vol, int nx, int ny, int nz, double iso, const double* origin, double intv,
+                   void* workspace, size_t ws_bytes, double* V, int64_t V_cap, int64_t* F, int64_t F_cap,
+                   int64_t* counts, void* stream);
+
 /* Weight gradient dW [N, K] = alpha * dZ[M, N]^T X[M, K] + beta * dW (fp16 in,
  * fp32 out; cuBLAS).  dW of every MLP layer of the fused step. */
 int gbsdf_gemm_wgrad(int64_t M, int N, int K, const void* dZ, int ldz, const void* X, int ldx, float* dW,

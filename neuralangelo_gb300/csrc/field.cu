@@ -612,6 +612,132 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
     if (warp == 0) umma::tmem_dealloc(tmem, 512);
 }
 
+// ---------------------------------------------------------------------------
+// SDF-only evaluation at arbitrary points or on a lattice block (forward only):
+// NeuralSDF.sdf (modules.py:73-74) for mesh extraction (mesh.py:33-35, with the
+// sign flip of scripts/extract_mesh.py:85) and for the sampler's no-grad
+// evaluations (model.py:238, 245).  Tile = 128 points, one evaluation each.
+
+struct SdfPointsArgs {
+    int64_t M;
+    const float* pts;          // [M, 3] or NULL for lattice mode
+    const float* ax;           // lattice axes: x [nx], y [ny], z [nz]
+    const float* ay;
+    const float* az;
+    int nx, ny, nz;
+    float sign;                // +1, or -1 for the mesh's negated field
+    float* out;                // [M]
+};
+
+template <int F>
+__global__ void __launch_bounds__(FIELD_THREADS, 1) k_sdf_points(FieldParams p, SdfPointsArgs q) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int K0 = p.K0;
+    uint8_t* w_s = smem;
+    uint8_t* a_s = w_s + HID * K0 * 2;
+    uint8_t* a2_s = a_s + TILE_M * K0 * 2;
+    float* w0x_s = reinterpret_cast<float*>(a2_s + TILE_M * K0 * 2);
+    float* b0_s = w0x_s + HID * 3;
+    float* wh_s = b0_s + HID;
+    float* part_s = wh_s + HID;                                 // [2][128]
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(part_s + 2 * TILE_M);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    stage_rows_kmajor(w_s, (const __half*)p.w0e, 0, HID, K0, K0, tid, FIELD_THREADS, HID);
+    for (int i = tid; i < HID * 3; i += FIELD_THREADS) w0x_s[i] = p.w0x[i];
+    for (int i = tid; i < HID; i += FIELD_THREADS) {
+        b0_s[i] = p.b0[i];
+        wh_s[i] = p.whead[i];
+    }
+    for (int i = tid; i < 2 * TILE_M * K0 / 8; i += FIELD_THREADS)
+        reinterpret_cast<uint4*>(a_s)[i] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        umma::mbar_init(mbar, 1);
+        umma::fence_mbar_init();
+    }
+    if (warp == 0) {
+        umma::tmem_alloc(tslot, HID);
+        umma::tmem_relinquish();
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint32_t idesc = umma::idesc_f16(TILE_M, HID);
+    const uint32_t a_addr = umma::smem_u32(a_s), a2_addr = umma::smem_u32(a2_s), w_addr = umma::smem_u32(w_s);
+    const float bhead = p.bhead[0];
+    const float inv_beta = 1.0f / p.beta;
+    const int64_t ntiles = (q.M + TILE_M - 1) / TILE_M;
+    const int qd = warp & 3, half = warp >> 2;
+    const int row = qd * 32 + lane;
+    uint32_t phase = 0;
+    auto point = [&](int64_t m, float* x) {
+        if (q.pts) {
+            x[0] = q.pts[3 * m]; x[1] = q.pts[3 * m + 1]; x[2] = q.pts[3 * m + 2];
+        } else {
+            const int k = (int)(m % q.nz), j = (int)((m / q.nz) % q.ny), i = (int)(m / ((int64_t)q.ny * q.nz));
+            x[0] = q.ax[i]; x[1] = q.ay[j]; x[2] = q.az[k];
+        }
+    };
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int64_t m0 = t * TILE_M;
+        for (int i = tid; i < TILE_M * p.active; i += FIELD_THREADS) {
+            const int r = i / p.active, l = i % p.active;
+            const int64_t m = m0 + r;
+            float v[F];
+            if (m < q.M) {
+                float x[3], xu[3];
+                point(m, x);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) xu[k] = to_unit(x[k]);
+                gather_level<F>(p, xu, l, v);
+            } else {
+#pragma unroll
+                for (int f = 0; f < F; ++f) v[f] = 0.0f;
+            }
+            write_tile_features<F>(a_s, a2_s, r, l, K0, v);
+        }
+        umma::fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            umma::fence_after_sync();
+            issue_tile_mma(tmem, a_addr, w_addr, K0, idesc);
+            issue_tile_mma(tmem, a2_addr, w_addr, K0, idesc, true);
+            umma::mma_commit(mbar);
+        }
+        const bool ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
+        phase ^= 1u;
+        if (!ok) {
+            flag_timeout(p.err, 1);
+            break;
+        }
+        umma::fence_after_sync();
+        const int64_t m = m0 + row;
+        float x[3] = {0.f, 0.f, 0.f};
+        if (m < q.M) point(m, x);
+        float part4[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
+        for (int c0 = half * 128; c0 < half * 128 + 128; c0 += 32) {
+            float v[32];
+            umma::tmem_ld32(umma::taddr(tmem, qd * 32, c0), v);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const int n = c0 + j;
+                const float z = v[j] + w0x_s[3 * n] * x[0] + w0x_s[3 * n + 1] * x[1] + w0x_s[3 * n + 2] * x[2] + b0_s[n];
+                part4[j & 3] = fmaf(wh_s[n], softplus_fast_h(z, p.beta, inv_beta), part4[j & 3]);
+            }
+        }
+        part_s[half * TILE_M + row] = (part4[0] + part4[1]) + (part4[2] + part4[3]);
+        umma::fence_before_sync();
+        __syncthreads();
+        if (tid < TILE_M && m0 + tid < q.M) q.out[m0 + tid] = q.sign * (part_s[tid] + part_s[TILE_M + tid] + bhead);
+        __syncthreads();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, HID);
+}
+
 static int num_sms() {
     int dev = 0, n = 0;
     cudaGetDevice(&dev);
@@ -649,16 +775,21 @@ static int launch_field(const FieldParams& p, bool backward, cudaStream_t s) {
     return launch_status(backward ? "field_bwd" : "field_fwd");
 }
 
-static int check_field(const FieldParams& p) {
-    GBSDF_CHECK_ARG(p.Ns >= 0, "Ns < 0");
+static int check_field_weights(const FieldParams& p) {
     GBSDF_CHECK_ARG(p.active >= 1 && p.active <= p.grid.n_levels, "active levels %d", p.active);
     const int F = p.grid.n_features;
     GBSDF_CHECK_ARG(F == 2 || F == 4 || F == 8, "n_features %d unsupported by the fused field", F);
     GBSDF_CHECK_ARG(p.K0 % 16 == 0 && p.K0 >= p.active * F && p.K0 <= 128, "K0 %d", p.K0);
-    GBSDF_CHECK_ARG(p.S > 0 || p.sample_ray, "need S > 0 or sample_ray");
-    GBSDF_CHECK_ARG(p.center && p.ray_unit && p.dists && p.table && p.w0e && p.w0x && p.b0 && p.whead && p.bhead,
-                    "NULL pointer");
+    GBSDF_CHECK_ARG(p.table && p.w0e && p.w0x && p.b0 && p.whead && p.bhead, "NULL weight pointer");
     GBSDF_CHECK_ARG(aligned(p.table, 16) && aligned(p.w0e, 16), "table / w0e alignment");
+    return GBSDF_OK;
+}
+
+static int check_field(const FieldParams& p) {
+    GBSDF_CHECK_ARG(p.Ns >= 0, "Ns < 0");
+    if (int st = check_field_weights(p)) return st;
+    GBSDF_CHECK_ARG(p.S > 0 || p.sample_ray, "need S > 0 or sample_ray");
+    GBSDF_CHECK_ARG(p.center && p.ray_unit && p.dists, "NULL ray pointer");
     return GBSDF_OK;
 }
 
@@ -700,4 +831,42 @@ extern "C" int gbsdf_field_bwd(const gbsdf_field_args* params, void* stream) {
         case 4: return launch_field<4>(p, true, as_stream(stream));
         default: return launch_field<8>(p, true, as_stream(stream));
     }
+}
+
+extern "C" int gbsdf_sdf_points(const gbsdf_field_args* params, int64_t M, const float* pts, const float* ax,
+                                const float* ay, const float* az, int nx, int ny, int nz, float sign, float* out,
+                                void* stream) {
+    clear_error();
+    GBSDF_CHECK_ARG(params != nullptr && out != nullptr, "NULL pointer");
+    const FieldParams& p = *params;
+    if (int st = check_field_weights(p)) return st;
+    GBSDF_CHECK_ARG(M >= 0, "M < 0");
+    if (M == 0) return GBSDF_OK;
+    SdfPointsArgs q;
+    q.M = M; q.pts = pts; q.ax = ax; q.ay = ay; q.az = az; q.nx = nx; q.ny = ny; q.nz = nz; q.sign = sign; q.out = out;
+    if (!pts) {
+        GBSDF_CHECK_ARG(ax && ay && az && nx > 0 && ny > 0 && nz > 0 && (int64_t)nx * ny * nz == M,
+                        "lattice mode needs axes with nx*ny*nz == M");
+    }
+    const size_t smem = (size_t)HID * p.K0 * 2 + 2 * (size_t)TILE_M * p.K0 * 2 + (HID * 5 + 2 * TILE_M) * 4 + 16;
+    GBSDF_CHECK_ARG(smem <= 227 * 1024, "K0 too large");
+    const int64_t ntiles = (M + TILE_M - 1) / TILE_M;
+    int64_t grid = num_sms();
+    if (grid > ntiles) grid = ntiles;
+    cudaStream_t s = as_stream(stream);
+    switch (p.grid.n_features) {
+        case 2:
+            cudaFuncSetAttribute(k_sdf_points<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_sdf_points<2><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p, q);
+            break;
+        case 4:
+            cudaFuncSetAttribute(k_sdf_points<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_sdf_points<4><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p, q);
+            break;
+        default:
+            cudaFuncSetAttribute(k_sdf_points<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_sdf_points<8><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p, q);
+            break;
+    }
+    return launch_status("sdf_points");
 }

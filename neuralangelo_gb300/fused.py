@@ -61,6 +61,7 @@ _lib.register("gbsdf_render_fused", [c_vp, c_vp])
 _lib.register("gbsdf_rgb_head_fwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp])
 _lib.register("gbsdf_rgb_head_bwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp])
 _lib.register("gbsdf_app_grad", [c_i64, c_i32, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_vp])
+_lib.register("gbsdf_sdf_points", [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_f32, c_vp, c_vp])
 _lib.register("gbsdf_gemm_wgrad", [c_i64, c_i32, c_i32, c_vp, c_i32, c_vp, c_i32, c_vp, c_i32, c_f32, c_f32, c_vp])
 
 
@@ -92,6 +93,38 @@ def _wgrad(dZ, X, N, K, dW):
     """dW[N, K] = dZ[:, :N]^T X[:, :K] (fp32 out)."""
     _lib.call("gbsdf_gemm_wgrad", dZ.shape[0], N, K, c_vp(dZ.data_ptr()), dZ.stride(0), c_vp(X.data_ptr()),
               X.stride(0), c_vp(dW.data_ptr()), dW.stride(0), 1.0, 0.0, _lib.stream_ptr(dZ.device))
+
+
+def pack_sdf(sdf):
+    """FP16 working copies of a NeuralSDF's hash table and layer-0 weights (weight norm
+    applied) plus the FP32 position columns, bias and head; returns (pk, active, K0)."""
+    A = sdf.active_levels
+    F = sdf.tcnn_encoding.layout.n_features
+    K0 = max(16, _round16(A * F))
+    H = sdf.cfg_sdf.mlp.hidden_dim
+    with torch.no_grad():
+        W0 = sdf.mlp.linears[0].weight                           # [256, 3 + L F]
+        w0e = torch.zeros(H, K0, device=W0.device, dtype=torch.float16)
+        w0e[:, :A * F] = W0[:, 3:3 + A * F]
+        pk = dict(
+            table=sdf.tcnn_encoding.params.detach().half(),
+            w0e=w0e, w0eT=w0e.t().contiguous(),
+            w0x=W0[:, :3].contiguous().float(), b0=sdf.mlp.linears[0].bias.detach().float(),
+            whead=sdf.mlp.linear_sdf.weight.detach()[0].contiguous().float(),
+            bhead=sdf.mlp.linear_sdf.bias.detach().float())
+    return pk, A, K0
+
+
+def sdf_weight_args(sdf, pk, A, K0, err=None):
+    """A FieldArgs carrying only the SDF weights (for gbsdf_sdf_points)."""
+    fa = FieldArgs()
+    fa.grid = sdf.tcnn_encoding.layout.struct
+    fa.active, fa.K0 = A, K0
+    fa.table, fa.w0e, fa.w0eT = _p(pk['table']), _p(pk['w0e']), _p(pk['w0eT'])
+    fa.w0x, fa.b0, fa.whead, fa.bhead = _p(pk['w0x']), _p(pk['b0']), _p(pk['whead']), _p(pk['bhead'])
+    fa.beta = float(sdf.cfg_sdf.mlp.activ_params.beta)
+    fa.err = _p(err)
+    return fa
 
 
 class FusedField:
@@ -133,20 +166,9 @@ class FusedField:
         """FP16 working copies of the FP32 masters (weight norm applied) for this step."""
         m = self.model
         sdf = m.neural_sdf
-        A = sdf.active_levels
-        F = self.F
-        self.A = A
-        self.K0 = max(16, _round16(A * F))
+        pk, self.A, self.K0 = pack_sdf(sdf)
         with torch.no_grad():
-            W0 = sdf.mlp.linears[0].weight                       # [256, 3 + L F]
-            w0e = torch.zeros(self.H, self.K0, device=W0.device, dtype=torch.float16)
-            w0e[:, :A * F] = W0[:, 3:3 + A * F]
-            pk = dict(
-                table=sdf.tcnn_encoding.params.detach().half(),
-                w0e=w0e, w0eT=w0e.t().contiguous(),
-                w0x=W0[:, :3].contiguous().float(), b0=sdf.mlp.linears[0].bias.detach().float(),
-                whead=sdf.mlp.linear_sdf.weight.detach()[0].contiguous().float(),
-                bhead=sdf.mlp.linear_sdf.bias.detach().float())
+            W0 = sdf.mlp.linears[0].weight
             W1 = sdf.mlp.linears[1].weight
             pk['w1'] = W1.half().contiguous()
             pk['w1T'] = W1.t().half().contiguous()

@@ -94,3 +94,45 @@ def median(v):
 
 
 _ = math
+
+
+def shapes_union(seed=0, n_spheres=3, n_boxes=2):
+    """Seeded union of spheres and axis-aligned boxes (radii / half-sizes 0.1-0.4) inside
+    [-1, 1]^3 as an analytic signed distance (negative inside).  Returns a callable
+    on [..., 3] tensors."""
+    g = torch.Generator().manual_seed(seed)
+    sph = [((torch.rand(3, generator=g) * 2 - 1) * 0.5, 0.1 + 0.3 * float(torch.rand(1, generator=g)))
+           for _ in range(n_spheres)]
+    box = [((torch.rand(3, generator=g) * 2 - 1) * 0.5, 0.1 + 0.3 * torch.rand(3, generator=g))
+           for _ in range(n_boxes)]
+
+    def sdf(x):
+        d = None
+        for c, r in sph:
+            v = (x - c.to(x)).norm(dim=-1) - r
+            d = v if d is None else torch.minimum(d, v)
+        for c, h in box:
+            q = (x - c.to(x)).abs() - h.to(x)
+            v = q.clamp(min=0).norm(dim=-1) + q.max(dim=-1).values.clamp(max=0)
+            d = torch.minimum(d, v)
+        return d
+    return sdf
+
+
+def fit_sdf(neural_sdf, target, steps=300, batch=65536, lr=1e-3, seed=0):
+    """Fit a NeuralSDF (plain FP32 path) to an analytic SDF with Adam on L1, points
+    uniform in [-1, 1]^3 plus a jittered copy of them."""
+    dev = neural_sdf.tcnn_encoding.params.device
+    g = torch.Generator(device=dev).manual_seed(seed)
+    opt = torch.optim.Adam(neural_sdf.parameters(), lr=lr)
+    loss = torch.zeros(())
+    for _ in range(steps):
+        x = torch.rand(batch, 3, device=dev, generator=g) * 2 - 1
+        pts = torch.cat([x, x + 0.02 * torch.randn(batch, 3, device=dev, generator=g)])
+        with torch.no_grad():
+            tgt = target(pts)
+        loss = (neural_sdf.sdf(pts)[:, 0] - tgt).abs().mean()
+        opt.zero_grad(set_to_none=True)
+        loss.backward()
+        opt.step()
+    return float(loss)
