@@ -284,6 +284,19 @@ int gbsdf_mc_block(const float* vol, int nx, int ny, int nz, double iso, const d
                    void* workspace, size_t ws_bytes, double* V, int64_t V_cap, int64_t* F, int64_t F_cap,
                    int64_t* counts, void* stream);
 
+/* Marching cubes of one block without any device allocation (no counterpart in
+ * the reference).  For callers that cannot allocate device memory -- a host
+ * application that owns the device budget and forbids allocations after
+ * start-up, or a latency-critical loop where cudaMalloc/cudaFree could
+ * synchronise the device.  Same inputs, outputs and results as gbsdf_mc_block,
+ * but the scratch lives in a fixed 12.5 MiB file-scope device array of this
+ * library, so blocks are limited to 33 x 33 x 33 points (larger ones are
+ * rejected with GBSDF_ERR_ARG).  The first call on a device looks up the
+ * array's device address (make it before any stream capture).  All calls share
+ * the array: calls that overlap on the GPU race and must be serialised. */
+int gbsdf_mc_block_noalloc(const float* vol, int nx, int ny, int nz, double iso, const double* origin, double intv,
+                           double* V, int64_t V_cap, int64_t* F, int64_t F_cap, int64_t* counts, void* stream);
+
 /* Weight gradient dW [N, K] = alpha * dZ[M, N]^T X[M, K] + beta * dW (fp16 in,
  * fp32 out; cuBLAS).  dW of every MLP layer of the fused step. */
 int gbsdf_gemm_wgrad(int64_t M, int N, int K, const void* dZ, int ldz, const void* X, int ldx, float* dW,

@@ -426,3 +426,72 @@ extern "C" int gbsdf_mc_block(const float* vol, int nx, int ny, int nz, double i
     mc_layout(nx, ny, nz, mc_vcap(nx, ny, nz), mc_fcap(nx, ny, nz), (uint8_t*)workspace, &w);
     return mc_run(vol, nx, ny, nz, iso, origin, intv, w, V, F, counts, as_stream(stream));
 }
+
+// ---------------------------------------------------------------------------
+// Marching cubes without any device allocation.
+//
+// Some callers cannot allocate device memory: a host application that owns the
+// whole device budget and forbids allocations after start-up (a renderer or an
+// engine plugin with a fixed pool), or a caller in a latency-critical loop where
+// cudaMalloc / cudaFree could synchronise the device.  For them this variant
+// keeps its scratch in a file-scope __device__ array of fixed size, enough for
+// blocks of up to 33 x 33 x 33 lattice points (32^3 cubes).  The array exists on
+// every device that loads this library, for the life of the process
+// (12.5 MiB).  Host code may not take the array's name as a device address, so
+// the device address is looked up with cudaGetSymbolAddress once per device, on
+// the first call made with that device current; make that first call before any
+// stream capture.  Every call reuses the same array: two calls whose kernels
+// overlap on the GPU (different streams, or several host threads) race, so
+// serialise them.  Every scratch element is written before it is read in a
+// call, so nothing carries over from the previous call.
+
+constexpr int kNoAllocMaxPoints = 33;
+constexpr size_t kNoAllocScratchBytes = 13119488;   // gbsdf_mc_workspace_size(33, 33, 33)
+
+static __device__ __align__(256) uint8_t g_mc_scratch[kNoAllocScratchBytes];
+
+static int noalloc_scratch(void** out) {
+    static void* addr[64] = {nullptr};
+    static std::mutex mu;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        set_error("no current CUDA device");
+        return GBSDF_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_mc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            set_error("cudaGetSymbolAddress of the marching-cubes scratch failed: %s", cudaGetErrorString(e));
+            return GBSDF_ERR_CUDA;
+        }
+        addr[dev] = p;
+    }
+    *out = addr[dev];
+    return GBSDF_OK;
+}
+
+extern "C" int gbsdf_mc_block_noalloc(const float* vol, int nx, int ny, int nz, double iso, const double* origin,
+                                      double intv, double* V, int64_t V_cap, int64_t* F, int64_t F_cap,
+                                      int64_t* counts, void* stream) {
+    clear_error();
+    GBSDF_CHECK_ARG(vol && origin && V && F && counts, "NULL pointer");
+    GBSDF_CHECK_ARG(nx >= 2 && ny >= 2 && nz >= 2, "block must have at least 2 points per axis");
+    GBSDF_CHECK_ARG(nx <= kNoAllocMaxPoints && ny <= kNoAllocMaxPoints && nz <= kNoAllocMaxPoints,
+                    "block %d x %d x %d exceeds the allocation-free limit of %d points per axis "
+                    "(use gbsdf_mc_block with a caller workspace for larger blocks)",
+                    nx, ny, nz, kNoAllocMaxPoints);
+    GBSDF_CHECK_ARG(V_cap >= mc_vcap(nx, ny, nz) && F_cap >= mc_fcap(nx, ny, nz),
+                    "output capacity below the worst case (3 nx ny nz vertices, 5 (nx-1)(ny-1)(nz-1) faces)");
+    if (gbsdf_mc_workspace_size(nx, ny, nz) > kNoAllocScratchBytes) {
+        set_error("internal: scratch layout larger than the static array");
+        return GBSDF_ERR_UNSUPPORTED;
+    }
+    if (int st = upload_table_once()) return st;
+    void* scratch = nullptr;
+    if (int st = noalloc_scratch(&scratch)) return st;
+    McWorkspace w;
+    mc_layout(nx, ny, nz, mc_vcap(nx, ny, nz), mc_fcap(nx, ny, nz), (uint8_t*)scratch, &w);
+    return mc_run(vol, nx, ny, nz, iso, origin, intv, w, V, F, counts, as_stream(stream));
+}

@@ -20,6 +20,24 @@ c_i32, c_i64, c_vp, c_dbl, c_sz = ctypes.c_int32, ctypes.c_int64, ctypes.c_void_
 _lib.register("gbsdf_mc_block", [c_vp, c_i32, c_i32, c_i32, c_dbl, c_vp, c_dbl, c_vp, c_sz, c_vp, c_i64, c_vp, c_i64,
                                  c_vp, c_vp])
 _lib.register("gbsdf_mc_table", [c_vp, c_vp])
+_lib.register("gbsdf_mc_block_noalloc", [c_vp, c_i32, c_i32, c_i32, c_dbl, c_vp, c_dbl, c_vp, c_i64, c_vp, c_i64,
+                                         c_vp, c_vp])
+
+NOALLOC_MAX_POINTS = 33
+
+
+def marching_cubes_noalloc(vol, origin, intv, V, F, counts, iso=0.0):
+    """gbsdf_mc_block_noalloc: marching cubes of one block (<= 33 points per axis) using
+    the library's fixed device scratch, for callers that must not allocate device
+    memory.  V [>= 3 nx ny nz, 3] float64, F [>= 5 (nx-1)(ny-1)(nz-1), 3] int64 and
+    counts [2] int64 are caller-owned device buffers; returns the filled views."""
+    nx, ny, nz = vol.shape
+    org = (ctypes.c_double * 3)(*[float(o) for o in origin])
+    _lib.call("gbsdf_mc_block_noalloc", c_vp(vol.data_ptr()), nx, ny, nz, float(iso), org, float(intv),
+              c_vp(V.data_ptr()), V.shape[0], c_vp(F.data_ptr()), F.shape[0], c_vp(counts.data_ptr()),
+              _lib.stream_ptr(vol.device))
+    nv, nf = counts.tolist()
+    return V[:nv], F[:nf]
 
 
 def _ws_size(nx, ny, nz):
