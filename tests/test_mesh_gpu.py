@@ -90,7 +90,7 @@ def test_extract_mesh_blocks_match_oracle_on_same_values():
     Vr, Fr = om.extract_mesh_blocks(vol_fn, bounds, intv, block)
     assert mesh.faces.shape[0] > 100
     assert np.array_equal(mesh.faces, Fr)                         # connectivity: bit-exact
-    assert np.allclose(mesh.vertices, Vr, rtol=1e-6, atol=1e-9)   # vertices: within 1e-6 relative
+    assert np.allclose(mesh.vertices, Vr, rtol=0, atol=1e-12)
     # geometric init: the zero level set is close to the sphere of radius 0.5
     r = np.linalg.norm(mesh.vertices, axis=1)
     assert abs(np.median(r) - 0.5) < 0.05
@@ -101,10 +101,10 @@ def test_extract_mesh_with_callable_like_reference():
     bounds, intv = [(-1, 1)] * 3, 2.0 / 32
     mesh = gm.extract_mesh(lambda x: -target(x)[..., None], bounds, intv, block_res=8, device=DEV)
 
-    def vol_fn(xs, ys, zs):
-        X, Y, Z = np.meshgrid(xs, ys, zs, indexing='ij')
-        return -target(torch.from_numpy(np.stack([X, Y, Z], -1))).numpy().astype(np.float32)
+    def vol_fn(xs, ys, zs):   # the same CUDA evaluation the GPU path makes, so both see identical values
+        X, Y, Z = torch.meshgrid(*[torch.from_numpy(a).to(DEV) for a in (xs, ys, zs)], indexing='ij')
+        return -target(torch.stack([X, Y, Z], -1)).cpu().numpy()
 
     Vr, Fr = om.extract_mesh_blocks(vol_fn, bounds, intv, 8)
     assert np.array_equal(mesh.faces, Fr)
-    assert np.allclose(mesh.vertices, Vr, rtol=1e-6, atol=1e-9)
+    assert np.allclose(mesh.vertices, Vr, rtol=0, atol=1e-12)
