@@ -186,8 +186,10 @@ typedef struct gbsdf_field_args {
     int32_t normal_col;
     const float* d_h0c;      /* [Ns, 256] gradient of the centre layer-0 activation */
     float* d_table;          /* [entries, F] accumulated */
-    void* d_pre0;            /* fp16 [7 Ns, 256] */
-    void* x0ext;             /* fp16 [7 Ns, 2 K0 + 16]: features hi | x,y,z hi, 1, x,y,z lo, 0 | features lo */
+    void* d_pre0;            /* fp16 [126 T, 256], T = ceil(Ns / 18) tiles, tile-major rows (backward) */
+    void* x0ext;             /* fp16 [126 T, 2 K0 + 16] tile-major rows: features hi | x,y,z hi, 1,
+                                x,y,z lo, 0 | features lo; written by the forward, read by the backward */
+    float* d_enc;            /* [126 T, K0] gradient of the encoder features (backward workspace) */
     float* d_whead;          /* [256] accumulated */
     float* d_bhead;          /* [1] accumulated */
     int32_t* err;            /* device flag for timed-out waits */

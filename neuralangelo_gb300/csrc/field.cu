@@ -107,6 +107,19 @@ __device__ __forceinline__ void write_tile_features(uint8_t* a_s, uint8_t* a2_s,
     write_half_row<F>(a2_s + off, lo);
 }
 
+template <int F>
+__device__ __forceinline__ void scatter_add(float* dst, const float* v) {
+    if constexpr (F == 8) {
+        atomicAdd(reinterpret_cast<float4*>(dst), make_float4(v[0], v[1], v[2], v[3]));
+        atomicAdd(reinterpret_cast<float4*>(dst) + 1, make_float4(v[4], v[5], v[6], v[7]));
+    } else if constexpr (F == 4) {
+        atomicAdd(reinterpret_cast<float4*>(dst), make_float4(v[0], v[1], v[2], v[3]));
+    } else {
+#pragma unroll
+        for (int f = 0; f < F; ++f) atomicAdd(dst + f, v[f]);
+    }
+}
+
 // Stage the encoder features of one tile (126 rows) into the A tile.
 template <int F>
 __device__ void stage_encoding(const FieldParams& p, int64_t s0, uint8_t* a_s, uint8_t* a2_s) {
@@ -129,6 +142,120 @@ __device__ void stage_encoding(const FieldParams& p, int64_t s0, uint8_t* a_s, u
         }
         write_tile_features<F>(a_s, a2_s, row, l, p.K0, v);
     }
+}
+
+// ---------------------------------------------------------------------------
+// hash-grid gather and table-gradient scatter as their own kernels: one thread
+// per (row, level) / (sample, level, corner) keeps thousands of independent
+// loads and atomics in flight, which the tensor-core kernels (one CTA of eight
+// warps per SM) cannot.
+
+// x0ext row t*126 + r (r = e*18 + sl) of every tile: the features of level l in
+// columns [l F, l F + F) as fp16 hi and, at K0 + 16 + l F, the fp16 residual lo;
+// the level-0 thread also writes the tail (x, y, z hi, 1, x, y, z lo) and zeroes
+// the padding columns.  Rows of samples past the end are zeros.
+template <int F>
+__global__ void __launch_bounds__(256) k_field_gather(FieldParams p, int64_t ntiles) {
+    const int A = p.active, K0 = p.K0, KX = 2 * K0 + 16;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t rows = ntiles * (SPT * EVALS);
+    if (i >= rows * A) return;
+    const int64_t grow = i / A;
+    const int l = (int)(i % A);
+    const int64_t t = grow / (SPT * EVALS);
+    const int r = (int)(grow % (SPT * EVALS));
+    const int e = r / SPT, sl = r % SPT;
+    const int64_t s = t * SPT + sl;
+    __half* dst = (__half*)p.x0ext + grow * KX;
+    float v[F], lo[F];
+    float x[3] = {0.f, 0.f, 0.f};
+    const bool live = s < p.Ns;
+    if (live) {
+        float c[3], xu[3];
+        sample_point(p, s, c);
+        eval_point(c, e, p.eps, x);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) xu[k] = to_unit(x[k]);
+        gather_level<F>(p, xu, l, v);
+    } else {
+#pragma unroll
+        for (int f = 0; f < F; ++f) v[f] = 0.0f;
+    }
+#pragma unroll
+    for (int f = 0; f < F; ++f) lo[f] = v[f] - __half2float(__float2half_rn(v[f]));
+    write_half_row<F>(reinterpret_cast<uint8_t*>(dst + l * F), v);
+    write_half_row<F>(reinterpret_cast<uint8_t*>(dst + K0 + 16 + l * F), lo);
+    if (l == 0) {
+        float tail[16] = {0.f};
+        if (live) {
+            tail[0] = x[0]; tail[1] = x[1]; tail[2] = x[2]; tail[3] = 1.0f;
+            for (int k = 0; k < 3; ++k) tail[4 + k] = x[k] - __half2float(__float2half_rn(x[k]));
+        }
+        store_half8(dst + K0, tail);
+        store_half8(dst + K0 + 8, tail + 8);
+        for (int c0 = A * F; c0 < K0; ++c0) {
+            dst[c0] = __float2half_rn(0.0f);
+            dst[K0 + 16 + c0] = __float2half_rn(0.0f);
+        }
+    }
+}
+
+// Table gradient of one (sample, level, corner) over the sample's 7 evaluations,
+// merging consecutive evaluations that hit the same entry (the taps are eps
+// apart: at coarse levels all 7 usually share the corner) before the atomics.
+template <int F>
+__global__ void __launch_bounds__(256) k_field_scatter(FieldParams p) {
+    const int A = p.active, K0 = p.K0;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= p.Ns * A * 8) return;
+    const int cc = (int)(i & 7);
+    const int l = (int)((i >> 3) % A);
+    const int64_t s = (i >> 3) / A;
+    const int64_t t = s / SPT;
+    const int sl = (int)(s % SPT);
+    float c[3];
+    sample_point(p, s, c);
+    const LevelDesc d = level_desc(p.grid, l);
+    float* base = p.d_table + d.offset * F;
+    uint32_t pidx = 0xffffffffu;
+    float pacc[F];
+#pragma unroll
+    for (int f = 0; f < F; ++f) pacc[f] = 0.0f;
+#pragma unroll 1
+    for (int e = 0; e < EVALS; ++e) {
+        float x[3], xu[3];
+        eval_point(c, e, p.eps, x);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) xu[k] = to_unit(x[k]);
+        uint32_t bx, by, bz;
+        float fx, fy, fz;
+        grid_pos(d.scale, xu[0], bx, fx);
+        grid_pos(d.scale, xu[1], by, fy);
+        grid_pos(d.scale, xu[2], bz, fz);
+        const uint32_t idx = grid_index(d, bx + (cc & 1), by + ((cc >> 1) & 1), bz + ((cc >> 2) & 1));
+        const float w = corner_weight(cc, fx, fy, fz);
+        if (idx != pidx) {
+            if (pidx != 0xffffffffu) scatter_add<F>(base + (uint64_t)pidx * F, pacc);
+            pidx = idx;
+#pragma unroll
+            for (int f = 0; f < F; ++f) pacc[f] = 0.0f;
+        }
+        const float* dv = p.d_enc + (t * (SPT * EVALS) + e * SPT + sl) * (int64_t)K0 + l * F;
+        float g[F];
+        if constexpr (F % 4 == 0) {
+#pragma unroll
+            for (int f = 0; f < F; f += 4) {
+                const float4 q4 = __ldg(reinterpret_cast<const float4*>(dv + f));
+                g[f] = q4.x; g[f + 1] = q4.y; g[f + 2] = q4.z; g[f + 3] = q4.w;
+            }
+        } else {
+#pragma unroll
+            for (int f = 0; f < F; ++f) g[f] = __ldg(dv + f);
+        }
+#pragma unroll
+        for (int f = 0; f < F; ++f) pacc[f] = fmaf(w, g[f], pacc[f]);
+    }
+    scatter_add<F>(base + (uint64_t)pidx * F, pacc);
 }
 
 // ---------------------------------------------------------------------------
@@ -181,7 +308,13 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
 
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int64_t s0 = t * SPT;
-        stage_encoding<F>(p, s0, a_s, a2_s);
+        {   // features of the tile, gathered by k_field_gather into x0ext (hi | tail | lo)
+            const int64_t xrows = ntiles * (int64_t)(SPT * EVALS);
+            const __half* xb = (const __half*)p.x0ext;
+            stage_rows_kmajor(a_s, xb, t * (SPT * EVALS), xrows, 2 * K0 + 16, K0, tid, FIELD_THREADS);
+            stage_rows_kmajor(a2_s, xb + K0 + 16, t * (SPT * EVALS), xrows, 2 * K0 + 16, K0, tid, FIELD_THREADS);
+            cp_async_wait_all();
+        }
         umma::fence_proxy_async_smem();
         __syncthreads();
         if (tid == 0) {
@@ -303,65 +436,6 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
 // ---------------------------------------------------------------------------
 // backward
 
-// Scatter d_enc of one (sample, level, corner) over the sample's 7 evaluations,
-// merging consecutive evaluations that hit the same table entry (the taps are
-// eps apart, so at coarse levels all 7 usually share the corner) before the
-// vector atomics.
-template <int F>
-__device__ __forceinline__ void scatter_corner(const FieldParams& p, const float* c, int l, int cc,
-                                               const float* denc_s, int sl) {
-    const LevelDesc d = level_desc(p.grid, l);
-    uint32_t pidx = 0xffffffffu;
-    float pacc[F];
-#pragma unroll
-    for (int f = 0; f < F; ++f) pacc[f] = 0.0f;
-    float* base = p.d_table + d.offset * F;
-#pragma unroll 1
-    for (int e = 0; e < EVALS; ++e) {
-        float x[3], xu[3];
-        eval_point(c, e, p.eps, x);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) xu[k] = to_unit(x[k]);
-        uint32_t bx, by, bz;
-        float fx, fy, fz;
-        grid_pos(d.scale, xu[0], bx, fx);
-        grid_pos(d.scale, xu[1], by, fy);
-        grid_pos(d.scale, xu[2], bz, fz);
-        const uint32_t idx = grid_index(d, bx + (cc & 1), by + ((cc >> 1) & 1), bz + ((cc >> 2) & 1));
-        const float w = corner_weight(cc, fx, fy, fz);
-        if (idx != pidx) {
-            if (pidx != 0xffffffffu) {
-                float* dst = base + (uint64_t)pidx * F;
-                if constexpr (F == 8) {
-                    atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[0], pacc[1], pacc[2], pacc[3]));
-                    atomicAdd(reinterpret_cast<float4*>(dst) + 1, make_float4(pacc[4], pacc[5], pacc[6], pacc[7]));
-                } else if constexpr (F == 4) {
-                    atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[0], pacc[1], pacc[2], pacc[3]));
-                } else {
-#pragma unroll
-                    for (int f = 0; f < F; ++f) atomicAdd(dst + f, pacc[f]);
-                }
-            }
-            pidx = idx;
-#pragma unroll
-            for (int f = 0; f < F; ++f) pacc[f] = 0.0f;
-        }
-        const float* dv = denc_s + (e * SPT + sl) * p.K0 + l * F;
-#pragma unroll
-        for (int f = 0; f < F; ++f) pacc[f] = fmaf(w, dv[f], pacc[f]);
-    }
-    float* dst = base + (uint64_t)pidx * F;
-    if constexpr (F == 8) {
-        atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[0], pacc[1], pacc[2], pacc[3]));
-        atomicAdd(reinterpret_cast<float4*>(dst) + 1, make_float4(pacc[4], pacc[5], pacc[6], pacc[7]));
-    } else if constexpr (F == 4) {
-        atomicAdd(reinterpret_cast<float4*>(dst), make_float4(pacc[0], pacc[1], pacc[2], pacc[3]));
-    } else {
-#pragma unroll
-        for (int f = 0; f < F; ++f) atomicAdd(dst + f, pacc[f]);
-    }
-}
-
 template <int F>
 __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -462,29 +536,18 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
                 dbh += df[e];
             }
         }
-        // (1) encoder features of the 126 rows
-        stage_encoding<F>(p, s0, a_s, a3_s);
+        // (1) encoder features of the tile, streamed back from the forward's x0ext rows
+        //     (rows 126-127 of the tile read the next tile's first rows or zeros; their
+        //     MMA results are never used)
+        {
+            const int64_t xrows = ntiles * (int64_t)(SPT * EVALS);
+            const __half* xb = (const __half*)p.x0ext;
+            stage_rows_kmajor(a_s, xb, t * (SPT * EVALS), xrows, KX, K0, tid, FIELD_THREADS);
+            stage_rows_kmajor(a3_s, xb + K0 + 16, t * (SPT * EVALS), xrows, KX, K0, tid, FIELD_THREADS);
+            cp_async_wait_all();
+        }
         umma::fence_proxy_async_smem();
         __syncthreads();
-        // x0ext rows (encoding, x, y, z, 1) for the layer-0 weight gradient
-        for (int i = tid; i < SPT * EVALS; i += FIELD_THREADS) {
-            const int e = i / SPT, sl = i % SPT;
-            const int64_t s = s0 + sl;
-            if (s >= p.Ns) continue;
-            __half* dst = (__half*)p.x0ext + (s * EVALS + e) * (int64_t)KX;
-            for (int kc = 0; kc < K0; kc += 8) {
-                *reinterpret_cast<uint4*>(dst + kc) = *reinterpret_cast<const uint4*>(a_s + umma::kmajor_offset(i, kc, K0));
-                *reinterpret_cast<uint4*>(dst + K0 + 16 + kc) =
-                    *reinterpret_cast<const uint4*>(a3_s + umma::kmajor_offset(i, kc, K0));
-            }
-            float c[3], x[3];
-            sample_point(p, s, c);
-            eval_point(c, e, p.eps, x);
-            float tail[16] = {x[0], x[1], x[2], 1.0f, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-            for (int k = 0; k < 3; ++k) tail[4 + k] = x[k] - __half2float(__float2half_rn(x[k]));
-            store_half8(dst + K0, tail);
-            store_half8(dst + K0 + 8, tail + 8);
-        }
         if (tid == 0) {
             umma::fence_after_sync();
             issue_tile_mma(tmem, a_addr, w_addr, K0, idesc1);
@@ -554,8 +617,8 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
                         store_half8(reinterpret_cast<__half*>(p2_s + umma::kmajor_offset(row, c0 + j, HID)), lo);
                     }
                 }
-                if (live) {
-                    __half* dst = (__half*)p.d_pre0 + (s * EVALS + e_row) * (int64_t)HID + c0;
+                if (row < SPT * EVALS) {   // dead samples store zeros (their x0ext rows are zero too)
+                    __half* dst = (__half*)p.d_pre0 + (t * (SPT * EVALS) + row) * (int64_t)HID + c0;
 #pragma unroll
                     for (int j = 0; j < 32; j += 8) store_half8(dst + j, v + j);
                 }
@@ -578,29 +641,19 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
             break;
         }
         umma::fence_after_sync();
-        float* denc_s = reinterpret_cast<float*>(p_s);          // [128 x K0] fp32 (P no longer read)
-        {
-            const int cols = K0 / 2;                            // each half of the warps stages half the columns
+        {   // (4) d_enc rows to global for k_field_scatter
+            const int cols = K0 / 2;                            // each half of the warps stores half the columns
             for (int c0 = half * cols; c0 < half * cols + cols; c0 += 16) {
                 float v[16];
                 umma::tmem_ld16(umma::taddr(tmem2, q * 32, c0), v);
+                if (row < SPT * EVALS) {
+                    float* dst = p.d_enc + (t * (SPT * EVALS) + row) * (int64_t)K0 + c0;
 #pragma unroll
-                for (int j = 0; j < 16; ++j) denc_s[row * K0 + c0 + j] = v[j];
+                    for (int j = 0; j < 16; j += 4) *reinterpret_cast<float4*>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                }
             }
         }
         umma::fence_before_sync();
-        __syncthreads();
-        // (4) scatter into the table gradient, one thread per (sample, level, corner)
-        for (int i = tid; i < SPT * p.active * 8; i += FIELD_THREADS) {
-            const int cc = i & 7;
-            const int l = (i >> 3) % p.active;
-            const int sl = (i >> 3) / p.active;
-            const int64_t s = s0 + sl;
-            if (s >= p.Ns) continue;
-            float c[3];
-            sample_point(p, s, c);
-            scatter_corner<F>(p, c, l, cc, denc_s, sl);
-        }
         __syncthreads();
     }
     umma::fence_before_sync();
@@ -768,7 +821,11 @@ static int launch_field(const FieldParams& p, bool backward, cudaStream_t s) {
     if (backward) {
         cudaFuncSetAttribute(k_field_bwd<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_field_bwd<F><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p);
+        const int64_t items = p.Ns * p.active * 8;
+        k_field_scatter<F><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p);
     } else {
+        const int64_t items = ntiles * (SPT * EVALS) * p.active;
+        k_field_gather<F><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p, ntiles);
         cudaFuncSetAttribute(k_field_fwd<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_field_fwd<F><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p);
     }
@@ -805,7 +862,7 @@ extern "C" int gbsdf_field_fwd(const gbsdf_field_args* params, void* stream) {
     const FieldParams& p = *params;
     if (int st = check_field(p)) return st;
     if (p.Ns == 0) return GBSDF_OK;
-    GBSDF_CHECK_ARG(p.sdf && p.grad && p.hess && p.h0c, "NULL output");
+    GBSDF_CHECK_ARG(p.sdf && p.grad && p.hess && p.h0c && p.x0ext, "NULL output");
     GBSDF_CHECK_ARG(!p.xc || (p.ldxc % 16 == 0 && p.ldxc - HID >= 22 + p.app_dim && p.ldxc - HID <= 48),
                     "xc leading dimension %d (needs 256 + 22 + app_dim <= ldxc <= 304, multiple of 16)", p.ldxc);
     GBSDF_CHECK_ARG(!p.xc || p.app_dim == 0 || (p.app_table && p.app_idx), "appearance table / index missing");
@@ -823,9 +880,9 @@ extern "C" int gbsdf_field_bwd(const gbsdf_field_args* params, void* stream) {
     if (int st = check_field(p)) return st;
     if (p.Ns == 0) return GBSDF_OK;
     GBSDF_CHECK_ARG(p.w0eT && p.grad && p.d_sdf && p.d_grad && p.d_hess && p.d_xc && p.d_h0c && p.d_table &&
-                        p.d_pre0 && p.x0ext && p.d_whead && p.d_bhead,
+                        p.d_pre0 && p.x0ext && p.d_enc && p.d_whead && p.d_bhead,
                     "NULL pointer");
-    GBSDF_CHECK_ARG(aligned(p.d_table, 16), "d_table alignment");
+    GBSDF_CHECK_ARG(aligned(p.d_table, 16) && aligned(p.d_enc, 16), "d_table / d_enc alignment");
     switch (p.grid.n_features) {
         case 2: return launch_field<2>(p, true, as_stream(stream));
         case 4: return launch_field<4>(p, true, as_stream(stream));

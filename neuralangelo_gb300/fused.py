@@ -39,7 +39,8 @@ class FieldArgs(ctypes.Structure):
                 ("pad1", c_i32), ("xc", c_vp), ("ldxc", c_i32), ("app_dim", c_i32), ("app_table", c_vp),
                 ("sdf", c_vp), ("grad", c_vp), ("hess", c_vp), ("h0c", c_vp), ("d_sdf", c_vp), ("d_grad", c_vp),
                 ("d_hess", c_vp), ("d_xc", c_vp), ("ld_dxc", c_i32), ("normal_col", c_i32), ("d_h0c", c_vp),
-                ("d_table", c_vp), ("d_pre0", c_vp), ("x0ext", c_vp), ("d_whead", c_vp), ("d_bhead", c_vp),
+                ("d_table", c_vp), ("d_pre0", c_vp), ("x0ext", c_vp), ("d_enc", c_vp), ("d_whead", c_vp),
+                ("d_bhead", c_vp),
                 ("err", c_vp)]
 
 
@@ -204,6 +205,7 @@ class FusedField:
         key = (R, S, Ns, self.K0)
         if self.ws is not None and self.ws['key'] == key:
             return self.ws
+        rows0 = (Ns + 17) // 18 * 126      # layer-0 rows: 18 samples x 7 evaluations per tile
         f16, f32 = torch.float16, torch.float32
         e = lambda *s, dt=f32: torch.empty(*s, device=device, dtype=dt)  # noqa: E731
         Hc = self.Hc
@@ -215,8 +217,9 @@ class FusedField:
                   d_pre_last=e(Ns, 8, dt=f16), dzs=[e(Ns, Hc, dt=f16) for _ in range(2)],
                   dzs_lo=[e(Ns, Hc, dt=f16) for _ in range(2)], dzfeat=e(Ns, 256, dt=f16),
                   dzfeat_lo=e(Ns, 256, dt=f16),
-                  dxc_tail=e(Ns, 64), d_h0c=e(Ns, 256), d_pre0=e(Ns * 7, 256, dt=f16),
-                  x0ext=e(Ns * 7, 2 * self.K0 + 16, dt=f16), d_whead=torch.zeros(256, device=device),
+                  dxc_tail=e(Ns, 64), d_h0c=e(Ns, 256), d_pre0=e(rows0, 256, dt=f16),
+                  x0ext=e(rows0, 2 * self.K0 + 16, dt=f16), d_enc=e(rows0, self.K0),
+                  d_whead=torch.zeros(256, device=device),
                   d_bhead=torch.zeros(1, device=device), d_bl=torch.zeros(3, device=device),
                   err=torch.zeros(1, device=device, dtype=torch.int32))
         self.ws = ws
@@ -278,6 +281,7 @@ class FusedField:
         fa.xc, fa.ldxc = _p(ws['xc']), self.Kc0
         fa.app_dim, fa.app_table = self.app_dim, _p(pk['app'])
         fa.sdf, fa.grad, fa.hess, fa.h0c = _p(ws['sdf']), _p(ws['grad']), _p(ws['hess']), _p(ws['h0c'])
+        fa.x0ext = _p(ws['x0ext'])
         fa.err = _p(ws['err'])
         # ---------------- forward ----------------
         _lib.call("gbsdf_field_fwd", ctypes.byref(fa), stream)
@@ -367,7 +371,7 @@ class FusedField:
         fa.d_sdf, fa.d_grad, fa.d_hess = _p(ws['d_sdf']), _p(ws['d_grad']), _p(ws['d_hess'])
         fa.d_xc, fa.ld_dxc, fa.normal_col = _p(ws['dxc_tail']), 64, 19
         fa.d_h0c = _p(ws['d_h0c'])
-        fa.d_table, fa.d_pre0, fa.x0ext = _p(d_table), _p(ws['d_pre0']), _p(ws['x0ext'])
+        fa.d_table, fa.d_pre0, fa.d_enc = _p(d_table), _p(ws['d_pre0']), _p(ws['d_enc'])
         fa.d_whead, fa.d_bhead = _p(ws['d_whead']), _p(ws['d_bhead'])
         _lib.call("gbsdf_field_bwd", ctypes.byref(fa), stream)
         gw0x = torch.empty(256, 2 * self.K0 + 16, **dev32)
