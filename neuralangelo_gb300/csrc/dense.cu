@@ -83,19 +83,31 @@ __global__ void __launch_bounds__(DENSE_THREADS, 1) k_dense(DenseParams p) {
     const int row = q * 32 + lane;
     constexpr int COLS_PER_WARP = N_TILE / 2;
 
-    for (int64_t t = group; t < ntiles && ok; t += ngroups) {
-        const int64_t m0 = t * TILE_M;
-        stage_rows_kmajor(a_s, p.X, m0, p.M, p.ldx, p.K, tid, DENSE_THREADS);
-        if (p.Xlo) stage_rows_kmajor(a2_s, p.Xlo, m0, p.M, p.ldx, p.K, tid, DENSE_THREADS);
-        cp_async_wait_all();
-        umma::fence_proxy_async_smem();
-        __syncthreads();
+    // Software pipeline: the A tile of tile t+1 is loaded (cp.async) while the
+    // epilogue of tile t reads TMEM; A's shared memory is free as soon as tile t's
+    // MMAs have completed.
+    auto stage = [&](int64_t t) {
+        stage_rows_kmajor(a_s, p.X, t * TILE_M, p.M, p.ldx, p.K, tid, DENSE_THREADS);
+        if (p.Xlo) stage_rows_kmajor(a2_s, p.Xlo, t * TILE_M, p.M, p.ldx, p.K, tid, DENSE_THREADS);
+    };
+    auto issue = [&]() {
         if (tid == 0) {
             umma::fence_after_sync();
             issue_tile_mma(tmem, a_addr, w_addr, p.K, idesc);
             if (p.Xlo) issue_tile_mma(tmem, a2_addr, w_addr, p.K, idesc, true);
             umma::mma_commit(mbar);
         }
+    };
+    int64_t t = group;
+    if (t < ntiles) {
+        stage(t);
+        cp_async_wait_all();
+        umma::fence_proxy_async_smem();
+    }
+    __syncthreads();
+    if (t < ntiles) issue();
+    for (; t < ntiles; t += ngroups) {
+        const int64_t m0 = t * TILE_M;
         ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
         phase ^= 1u;
         if (!ok) {
@@ -103,6 +115,8 @@ __global__ void __launch_bounds__(DENSE_THREADS, 1) k_dense(DenseParams p) {
             break;
         }
         umma::fence_after_sync();
+        const int64_t tn = t + ngroups;
+        if (tn < ntiles) stage(tn);                 // overlaps the epilogue below
         const int64_t grow = m0 + row;
         const bool live = grow < p.M;
 #pragma unroll 1
@@ -152,7 +166,12 @@ __global__ void __launch_bounds__(DENSE_THREADS, 1) k_dense(DenseParams p) {
             }
         }
         umma::fence_before_sync();
+        if (tn < ntiles) {
+            cp_async_wait_all();
+            umma::fence_proxy_async_smem();
+        }
         __syncthreads();
+        if (tn < ntiles) issue();
     }
     umma::fence_before_sync();
     __syncthreads();

@@ -26,15 +26,19 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+// Walk (row group, K chunk) in nested loops so no integer division is needed.
 __device__ __forceinline__ void stage_rows_kmajor(uint8_t* tile, const __half* src, int64_t row0, int64_t rows,
                                                   int ld, int K, int tid, int nthreads, int nrows = TILE_M) {
     const int KC = K >> 3;
+    const int per_group = 8 * KC;                 // chunks of one 8-row group
+    // each thread starts at chunk tid and strides by nthreads; decompose once, then advance
+    int c = tid;
+    int rg = 0, rem = c;
+    while (rem >= per_group) { rem -= per_group; ++rg; }
     const int total = nrows * KC;
-    for (int c = tid; c < total; c += nthreads) {
-        const int r_lo = c & 7;
-        const int rest = c >> 3;
-        const int kc = rest % KC;
-        const int rg = rest / KC;
+    for (; c < total; c += nthreads) {
+        const int r_lo = rem & 7;
+        const int kc = rem >> 3;
         const int r = rg * 8 + r_lo;
         uint8_t* dst = tile + (size_t)c * 16;
         const int64_t gr = row0 + r;
@@ -43,6 +47,8 @@ __device__ __forceinline__ void stage_rows_kmajor(uint8_t* tile, const __half* s
         } else {
             *reinterpret_cast<uint4*>(dst) = make_uint4(0, 0, 0, 0);
         }
+        rem += nthreads;
+        while (rem >= per_group) { rem -= per_group; ++rg; }
     }
 }
 

@@ -306,23 +306,32 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
     const int e_row = row / SPT, sl_row = row % SPT;
     uint32_t phase = 0;
 
-    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int64_t s0 = t * SPT;
-        {   // features of the tile, gathered by k_field_gather into x0ext (hi | tail | lo)
-            const int64_t xrows = ntiles * (int64_t)(SPT * EVALS);
-            const __half* xb = (const __half*)p.x0ext;
-            stage_rows_kmajor(a_s, xb, t * (SPT * EVALS), xrows, 2 * K0 + 16, K0, tid, FIELD_THREADS);
-            stage_rows_kmajor(a2_s, xb + K0 + 16, t * (SPT * EVALS), xrows, 2 * K0 + 16, K0, tid, FIELD_THREADS);
-            cp_async_wait_all();
-        }
-        umma::fence_proxy_async_smem();
-        __syncthreads();
+    // features of a tile, gathered by k_field_gather into x0ext (hi | tail | lo); the
+    // next tile's load overlaps this tile's epilogue (A is free once its MMAs completed)
+    const int64_t xrows = ntiles * (int64_t)(SPT * EVALS);
+    auto stage = [&](int64_t tt) {
+        const __half* xb = (const __half*)p.x0ext;
+        stage_rows_kmajor(a_s, xb, tt * (SPT * EVALS), xrows, 2 * K0 + 16, K0, tid, FIELD_THREADS);
+        stage_rows_kmajor(a2_s, xb + K0 + 16, tt * (SPT * EVALS), xrows, 2 * K0 + 16, K0, tid, FIELD_THREADS);
+    };
+    auto issue = [&]() {
         if (tid == 0) {
             umma::fence_after_sync();
             issue_tile_mma(tmem, a_addr, w_addr, K0, idesc);
             issue_tile_mma(tmem, a2_addr, w_addr, K0, idesc, true);
             umma::mma_commit(mbar);
         }
+    };
+    int64_t t = blockIdx.x;
+    if (t < ntiles) {
+        stage(t);
+        cp_async_wait_all();
+        umma::fence_proxy_async_smem();
+    }
+    __syncthreads();
+    if (t < ntiles) issue();
+    for (; t < ntiles; t += gridDim.x) {
+        const int64_t s0 = t * SPT;
         const bool ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
         phase ^= 1u;
         if (!ok) {
@@ -330,6 +339,8 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
             break;
         }
         umma::fence_after_sync();
+        const int64_t tn = t + gridDim.x;
+        if (tn < ntiles) stage(tn);
         // epilogue: pre = acc + W0x x + b0 ; h = softplus ; partial head dot
         const int64_t s = s0 + sl_row;
         const bool live = row < SPT * EVALS && s < p.Ns;
@@ -426,7 +437,12 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
                 }
             }
         }
+        if (tn < ntiles) {
+            cp_async_wait_all();
+            umma::fence_proxy_async_smem();
+        }
         __syncthreads();
+        if (tn < ntiles) issue();
     }
     umma::fence_before_sync();
     __syncthreads();
@@ -493,9 +509,9 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
     float dbh = 0.0f;
     bool ok = true;
 
-    for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        const int64_t s0 = t * SPT;
-        // (0) per-sample output gradients -> d f of each evaluation (modules.py:144-156)
+    // per-sample output gradients -> d f of each evaluation (modules.py:144-156)
+    auto prologue = [&](int64_t tt) {
+        const int64_t s0 = tt * SPT;
         if (tid < SPT) {
             const int64_t s = s0 + tid;
             float df[EVALS] = {0, 0, 0, 0, 0, 0, 0};
@@ -536,30 +552,43 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
                 dbh += df[e];
             }
         }
-        // (1) encoder features of the tile, streamed back from the forward's x0ext rows
-        //     (rows 126-127 of the tile read the next tile's first rows or zeros; their
-        //     MMA results are never used)
-        {
-            const int64_t xrows = ntiles * (int64_t)(SPT * EVALS);
-            const __half* xb = (const __half*)p.x0ext;
-            stage_rows_kmajor(a_s, xb, t * (SPT * EVALS), xrows, KX, K0, tid, FIELD_THREADS);
-            stage_rows_kmajor(a3_s, xb + K0 + 16, t * (SPT * EVALS), xrows, KX, K0, tid, FIELD_THREADS);
-            cp_async_wait_all();
-        }
-        umma::fence_proxy_async_smem();
-        __syncthreads();
+    };
+    // encoder features of a tile, streamed back from the forward's x0ext rows (rows
+    // 126-127 of a tile read the next tile's first rows or zeros; their MMA results
+    // are never used); the next tile's load overlaps this tile's epilogue
+    const int64_t xrows = ntiles * (int64_t)(SPT * EVALS);
+    auto stage = [&](int64_t tt) {
+        const __half* xb = (const __half*)p.x0ext;
+        stage_rows_kmajor(a_s, xb, tt * (SPT * EVALS), xrows, KX, K0, tid, FIELD_THREADS);
+        stage_rows_kmajor(a3_s, xb + K0 + 16, tt * (SPT * EVALS), xrows, KX, K0, tid, FIELD_THREADS);
+    };
+    auto issue1 = [&]() {
         if (tid == 0) {
             umma::fence_after_sync();
             issue_tile_mma(tmem, a_addr, w_addr, K0, idesc1);
             issue_tile_mma(tmem, a3_addr, w_addr, K0, idesc1, true);
             umma::mma_commit(mbar);
         }
+    };
+    int64_t t = blockIdx.x;
+    if (t < ntiles) {
+        prologue(t);
+        stage(t);
+        cp_async_wait_all();
+        umma::fence_proxy_async_smem();
+    }
+    __syncthreads();
+    if (t < ntiles) issue1();
+    for (; t < ntiles && ok; t += gridDim.x) {
+        const int64_t s0 = t * SPT;
         ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
         phase ^= 1u;
         if (!ok) {
             flag_timeout(p.err, 1);
             break;
         }
+        const int64_t tn = t + gridDim.x;
+        if (tn < ntiles) stage(tn);                  // A is free: MMA1 of tile t completed
         umma::fence_after_sync();
         // (2) d_pre = (d f * w_head + [centre] d_h0c) * softplus'(pre)
         {
@@ -654,7 +683,14 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
             }
         }
         umma::fence_before_sync();
+        __syncthreads();                              // df_s of tile t fully read
+        if (tn < ntiles) {
+            prologue(tn);
+            cp_async_wait_all();
+            umma::fence_proxy_async_smem();
+        }
         __syncthreads();
+        if (tn < ntiles) issue1();
     }
     umma::fence_before_sync();
     __syncthreads();
