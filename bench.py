@@ -39,7 +39,77 @@ def parse():
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP32 denominator (profiling runs)")
     p.add_argument("--rays", type=int, default=R_RAYS)
     p.add_argument("--samples", type=int, default=N_SAMPLES)
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the ragged-batching, sampler and mesh measurements")
     return p.parse_args()
+
+
+# --------------------------------------------------------------------------- extra workloads
+
+def bench_ragged(model, device, steps, warmup, rays=65536, seed=0):
+    """Ragged batching: 65536 rays, 30% culled to zero samples, the rest 16..256 samples
+    (6.2M samples), the fused step captured in one CUDA graph; against the same rays in
+    the reference's dense layout padded to 128 samples (8.4M samples, misses computed)."""
+    import torch
+    from neuralangelo_gb300.fused import CapturedStep, FusedField
+    from neuralangelo_gb300.workloads import make_ragged_rays, padded
+    rag = make_ragged_rays(rays, seed=seed, n_images=100, device=device)
+    useful = int(rag['dists'].numel())
+    out = dict(rays=rays, useful_samples=useful)
+    for name, b in (("padded_128", padded(rag, 128, seed=seed)), ("ragged", rag)):
+        ff = FusedField(model)
+        ns = int(b['dists'].numel())
+        if name == "ragged":   # eager launches, for the graph's benefit
+            ms_e = time_steps(lambda: ff.step(b, compute_loss=False), steps, warmup, lambda: None)
+            out["ragged_eager_ms_per_step"] = round(ms_e, 3)
+        cap = CapturedStep(ff, b)
+        ms = time_steps(cap.replay, steps, warmup, lambda: None)
+        out[name] = dict(samples=ns, ms_per_step=round(ms, 3), samples_per_s=round(ns / (ms * 1e-3), 1),
+                         useful_samples_per_s=round(useful / (ms * 1e-3), 1))
+        assert ff.check_device_errors() == 0
+        del cap
+        ff.release()
+        torch.cuda.empty_cache()
+    out["speedup_vs_padded"] = round(out["padded_128"]["ms_per_step"] / out["ragged"]["ms_per_step"], 3)
+    return out
+
+
+def bench_sampler(model, device, steps=5, warmup=2, rays=R_RAYS, seed=0):
+    """The no-grad hierarchical pre-pass (64 coarse + 4 x 16 importance samples per ray,
+    SDF of the fused field kernel), timed separately from the training step."""
+    import torch
+    from neuralangelo_gb300.sampler import HierarchicalSampler, field_sdf_fn
+    from neuralangelo_gb300.workloads import make_rays, sphere_bounds
+    b = make_rays(rays, 1, seed=seed, device=device)
+    near, far, _ = sphere_bounds(b['center'], b['ray_unit'])
+    u = torch.rand(rays, 64, device=device, generator=torch.Generator(device=device).manual_seed(seed))
+    smp = HierarchicalSampler(64, 16, 4)
+    fn = field_sdf_fn(model.neural_sdf)
+    ms = time_steps(lambda: smp(fn, b['center'], b['ray_unit'], near, far, u=u), steps, warmup, lambda: None)
+    evals = rays * (64 + 3 * 16)
+    return dict(rays=rays, samples_per_ray=smp.n_samples, ms_per_call=round(ms, 3),
+                rays_per_s=round(rays / (ms * 1e-3), 1), sdf_evals_per_s=round(evals / (ms * 1e-3), 1))
+
+
+def bench_mesh(model, device, res=512, block_res=128):
+    """Mesh extraction of the field's geometric-init surface (a sphere of radius 0.5) on a
+    512^3 lattice in 128^3 blocks: lattice SDF kernel + GPU marching cubes per block,
+    each block's mesh copied to the host as the reference does (mesh.py:33-46)."""
+    import torch
+    from neuralangelo_gb300.mesh import FieldSDF, extract_mesh
+    f = FieldSDF(model.neural_sdf, sign=-1.0)
+    intv = 2.0 / res
+    bounds = [(-1.0, 1.0)] * 3
+    extract_mesh(f, [(-1.0, -0.5)] * 3, intv, block_res, device=device)   # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mesh = extract_mesh(f, bounds, intv, block_res, device=device)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    pts = (res + (res // block_res - 1)) ** 3          # lattice points incl. the block overlaps
+    return dict(resolution=res, block_res=block_res, seconds=round(dt, 4), lattice_points=pts,
+                points_per_s=round(pts / dt, 1), vertices=int(mesh.vertices.shape[0]),
+                faces=int(mesh.faces.shape[0]))
 
 
 # --------------------------------------------------------------------------- CPU baseline
@@ -300,6 +370,13 @@ def main():
                         launches_per_step=calls / args.steps,
                         peak_source="MEASURED_PEAKS.json hbm_gbs (burst, of measured)")
     launches = int(sum(c for c, _ in ksum.values()) / args.steps)
+    extras = {}
+    if not args.no_extras and fused is not None:
+        fused.release()
+        torch.cuda.empty_cache()
+        extras["ragged"] = bench_ragged(model, device, max(3, args.steps // 2), args.warmup)
+        extras["sampler"] = bench_sampler(model, device)
+        extras["mesh"] = bench_mesh(model, device)
     cb = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_port_sample()
@@ -320,7 +397,8 @@ def main():
                     roofline=roof, cpu_baseline=cb, gpu_launches=launches, clocks=clock,
                     flops_per_sample=flops_per_sample(model.cfg, ACTIVE),
                     encoder_bytes_per_sample=encoder_bytes_per_sample(ACTIVE, 8, 4),
-                    kernel_ms_per_step={k: round(v[1] / args.steps, 4) for k, v in ksum.items()})
+                    kernel_ms_per_step={k: round(v[1] / args.steps, 4) for k, v in ksum.items()},
+                    **extras)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

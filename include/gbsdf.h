@@ -164,13 +164,16 @@ typedef struct gbsdf_field_args {
     const void* table;       /* fp16 [entries, F] */
     const void* w0e;         /* fp16 [256, K0] */
     const void* w0eT;        /* fp16 [K0, 256] */
+    const void* w0b;         /* fp16 [256, K0 + 16]: w0e | position and bias columns as hi/lo pairs
+                                (x hi, b hi, x lo, b lo, x-weight lo; see the x0ext tail) */
     const float* w0x;        /* [256, 3] */
     const float* b0;         /* [256] */
     const float* whead;      /* [256] */
     const float* bhead;      /* [1] */
     float beta, eps, two_eps, eps2, outside_val;
     int32_t pad1;
-    void* xc;                /* fp16 [Ns, ldxc] colour input; columns >= 256 written by the forward */
+    void* xc;                /* fp16 [Ns, ldxc] colour input; columns >= 256 written by the forward:
+                                x, SH(d), normal, app, zeros, and 1 in the last column */
     int32_t ldxc;
     int32_t app_dim;
     const float* app_table;  /* [n_images, app_dim] */
@@ -188,7 +191,8 @@ typedef struct gbsdf_field_args {
     float* d_table;          /* [entries, F] accumulated */
     void* d_pre0;            /* fp16 [126 T, 256], T = ceil(Ns / 18) tiles, tile-major rows (backward) */
     void* x0ext;             /* fp16 [126 T, 2 K0 + 16] tile-major rows: features hi | x,y,z hi, 1,
-                                x,y,z lo, 0 | features lo; written by the forward, read by the backward */
+                                x,y,z lo, 1, x,y,z hi, 0 x 5 | features lo; written by the forward,
+                                read by the backward */
     float* d_enc;            /* [126 T, K0] gradient of the encoder features (backward workspace) */
     float* d_whead;          /* [256] accumulated */
     float* d_bhead;          /* [1] accumulated */
@@ -298,6 +302,48 @@ int gbsdf_mc_block(const float* vol, int nx, int ny, int nz, double iso, const d
  * the array: calls that overlap on the GPU race and must be serialised. */
 int gbsdf_mc_block_noalloc(const float* vol, int nx, int ny, int nz, double iso, const double* origin, double intv,
                            double* V, int64_t V_cap, int64_t* F, int64_t F_cap, int64_t* counts, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Hierarchical importance sampler (the no-grad pre-pass placing the training
+ * samples): Model.sample_dists_all / sample_dists_hierarchical
+ * (projects/neuralangelo/model.py:232-267), nerf_util.sample_dists and
+ * sample_dists_from_pdf (projects/nerf/utils/nerf_util.py:20-68).
+ * Per-ray lists are rows of [R, ld] float32 arrays, updated in place. */
+#define GBSDF_SAMPLER_MAX_LIST 512
+
+typedef struct gbsdf_sampler_args {
+    int64_t R;                 /* rays */
+    int32_t ld;                /* row stride of dists / sdfs (>= the longest list) */
+    int32_t n_list;            /* entries already in each row */
+    int32_t n_merge;           /* fine samples of the previous round sorted in first (0..32) */
+    int32_t n_fine;            /* new distances to draw (0 = merge only) */
+    float   inv_s;             /* sharpness of this round: 64 * 2^h (model.py:240) */
+    int32_t robust;            /* 1: interval slope = min(previous, current) (model.py:256-258) */
+    const float* center;       /* [R, 3] camera centres */
+    const float* ray_unit;     /* [R, 3] unit directions */
+    float* dists;              /* [R, ld] sample distances (in / out) */
+    float* sdfs;               /* [R, ld] their SDF values (in / out); NULL once no round needs them */
+    const float* merge_d;      /* [R, n_merge] previous fine distances (may alias fine_d) */
+    const float* merge_s;      /* [R, n_merge] their SDF values (read when sdfs != NULL) */
+    float* fine_d;             /* [R, n_fine] new distances (out) */
+    float* fine_pts;           /* [R * n_fine, 3] their points c + d t (out), or NULL */
+} gbsdf_sampler_args;
+
+size_t gbsdf_sampler_args_size(void);
+
+/* Stratified coarse distances dists[r, k] = (u[r, k] + k) / n * (far - near) + near
+ * for k < n (nerf_util.sample_dists, nerf_util.py:20-38; u NULL = 0.5, the
+ * non-stratified case) and their points pts [R * n, 3] (or NULL).
+ * Reads R, ld, center, ray_unit, dists of args; near, far [R]. */
+int gbsdf_sampler_coarse(const gbsdf_sampler_args* args, int n, const float* u, int ldu, const float* near,
+                         const float* far, float* pts, void* stream);
+
+/* One hierarchical round (model.py:237-247, 250-267): sort the previous round's
+ * n_merge fine samples into each row (concatenate + sort, SDF values follow),
+ * then draw n_fine distances by inverting the CDF of the NeuS interval weights
+ * at sharpness inv_s (FP32 visibility product, nerf_util.py:41-68).  With
+ * n_fine = 0 the call only merges (the final round). */
+int gbsdf_sampler_round(const gbsdf_sampler_args* args, void* stream);
 
 /* Weight gradient dW [N, K] = alpha * dZ[M, N]^T X[M, K] + beta * dW (fp16 in,
  * fp32 out; cuBLAS).  dW of every MLP layer of the fused step. */

@@ -60,14 +60,17 @@ __device__ __forceinline__ void grid_pos(float scale, float x, uint32_t& base, f
     frac = __fsub_rn(p, f);
 }
 
+// Same result as idx % size without a division in the common cases: a hashed
+// level's size is the power of two 2^log2_hashmap_size (it is hashed exactly when
+// res^3 exceeds that), and a dense index of an in-range corner is already below
+// the level size (size >= res^3).
 __device__ __forceinline__ uint32_t grid_index(const LevelDesc& d, uint32_t cx, uint32_t cy, uint32_t cz) {
-    uint32_t idx;
     if (d.hashed) {
-        idx = (cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u);
-    } else {
-        idx = cx + cy * d.res + cz * (d.res * d.res);
+        const uint32_t idx = (cx * 1u) ^ (cy * 2654435761u) ^ (cz * 805459861u);
+        return (d.size & (d.size - 1u)) == 0u ? (idx & (d.size - 1u)) : idx % d.size;
     }
-    return idx % d.size;
+    const uint32_t idx = cx + cy * d.res + cz * (d.res * d.res);
+    return idx < d.size ? idx : idx % d.size;
 }
 
 // Corner c (0..7) selects +1 in dimension d when bit d of c is set.
@@ -131,6 +134,24 @@ __device__ __forceinline__ float warp_column_sum32(float* v, int lane) {
         }
     }
     return v[0];
+}
+
+// Column sums of a 32 x 16 block held one row per lane (v[j] = element (lane, j)):
+// four halving exchanges leave lane L with column L % 16 summed over the 16 lanes
+// that share L's bit 4; one more exchange adds the other half.  Lanes L and L + 16
+// both return the sum of column L % 16 (15 + 1 shuffles).
+__device__ __forceinline__ float warp_column_sum16(float* v, int lane) {
+#pragma unroll
+    for (int h = 8; h >= 1; h >>= 1) {
+        const bool upper = (lane & h) != 0;
+#pragma unroll
+        for (int i = 0; i < h; ++i) {
+            const float send = upper ? v[i] : v[i + h];
+            const float keep = upper ? v[i + h] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+        }
+    }
+    return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 16);
 }
 
 __device__ __forceinline__ float warp_sum(float v) {

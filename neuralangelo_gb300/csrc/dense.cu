@@ -41,8 +41,14 @@ struct DenseParams {
     int* err;
 };
 
-template <int N_TILE>
-__global__ void __launch_bounds__(DENSE_THREADS, 1) k_dense(DenseParams p) {
+// 16 warps: four per TMEM lane quadrant, each reading a quarter of the tile's
+// columns, so enough warps are in flight to hide the tcgen05.ld and MUFU latency
+// of the epilogue.  The epilogue kind is a template parameter.
+constexpr int DENSE_WARPS = 16;
+constexpr int DENSE_TPB = DENSE_WARPS * 32;
+
+template <int N_TILE, int EPI>
+__global__ void __launch_bounds__(DENSE_TPB, 1) k_dense(DenseParams p) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t* w_s = smem;                                              // [N_TILE x K]
     uint8_t* a_s = w_s + (size_t)N_TILE * p.K * 2;                    // [128 x K]
@@ -57,8 +63,8 @@ __global__ void __launch_bounds__(DENSE_THREADS, 1) k_dense(DenseParams p) {
     const int n0 = ns * N_TILE;
 
     // resident weight slice and bias
-    stage_rows_kmajor(w_s, p.W, n0, p.N_total, p.K, p.K, tid, DENSE_THREADS, N_TILE);
-    for (int i = tid; i < N_TILE; i += DENSE_THREADS) bias_s[i] = p.bias ? p.bias[n0 + i] : 0.0f;
+    stage_rows_kmajor(w_s, p.W, n0, p.N_total, p.K, p.K, tid, DENSE_TPB, N_TILE);
+    for (int i = tid; i < N_TILE; i += DENSE_TPB) bias_s[i] = p.bias ? p.bias[n0 + i] : 0.0f;
     if (tid == 0) {
         umma::mbar_init(mbar, 1);
         umma::fence_mbar_init();
@@ -79,22 +85,24 @@ __global__ void __launch_bounds__(DENSE_THREADS, 1) k_dense(DenseParams p) {
 
     const float inv_beta = 1.0f / p.beta;
     const int q = warp & 3;                 // TMEM lane quadrant of this warp
-    const int half = warp >> 2;             // which half of the columns this warp reads
+    const int part = warp >> 2;             // which quarter of the columns this warp reads
     const int row = q * 32 + lane;
-    constexpr int COLS_PER_WARP = N_TILE / 2;
+    constexpr int COLS_PER_WARP = N_TILE / 4;
+    constexpr int CHUNK = COLS_PER_WARP < 32 ? COLS_PER_WARP : 32;
 
     // Software pipeline: the A tile of tile t+1 is loaded (cp.async) while the
     // epilogue of tile t reads TMEM; A's shared memory is free as soon as tile t's
     // MMAs have completed.
     auto stage = [&](int64_t t) {
-        stage_rows_kmajor(a_s, p.X, t * TILE_M, p.M, p.ldx, p.K, tid, DENSE_THREADS);
-        if (p.Xlo) stage_rows_kmajor(a2_s, p.Xlo, t * TILE_M, p.M, p.ldx, p.K, tid, DENSE_THREADS);
+        stage_rows_kmajor(a_s, p.X, t * TILE_M, p.M, p.ldx, p.K, tid, DENSE_TPB);
+        if (p.Xlo) stage_rows_kmajor(a2_s, p.Xlo, t * TILE_M, p.M, p.ldx, p.K, tid, DENSE_TPB);
     };
     auto issue = [&]() {
         if (tid == 0) {
             umma::fence_after_sync();
-            issue_tile_mma(tmem, a_addr, w_addr, p.K, idesc);
-            if (p.Xlo) issue_tile_mma(tmem, a2_addr, w_addr, p.K, idesc, true);
+            // the low half first: small addends keep their bits in the FP32 accumulator
+            if (p.Xlo) issue_tile_mma(tmem, a2_addr, w_addr, p.K, idesc);
+            issue_tile_mma(tmem, a_addr, w_addr, p.K, idesc, p.Xlo != nullptr);
             umma::mma_commit(mbar);
         }
     };
@@ -120,47 +128,49 @@ __global__ void __launch_bounds__(DENSE_THREADS, 1) k_dense(DenseParams p) {
         const int64_t grow = m0 + row;
         const bool live = grow < p.M;
 #pragma unroll 1
-        for (int c0 = half * COLS_PER_WARP; c0 < (half + 1) * COLS_PER_WARP; c0 += 32) {
-            float v[32];
-            umma::tmem_ld32(umma::taddr(tmem, q * 32, c0), v);
-            if (!live) continue;
-            if (p.epi == EPI_DRELU || p.epi == EPI_DSOFTPLUS) {
-                const __half* gp = p.G + grow * (int64_t)p.ldg + n0 + c0;
+        for (int c0 = part * COLS_PER_WARP; c0 < (part + 1) * COLS_PER_WARP; c0 += CHUNK) {
+            float v[CHUNK];
+            if constexpr (CHUNK == 32) umma::tmem_ld32(umma::taddr(tmem, q * 32, c0), v);
+            else umma::tmem_ld16(umma::taddr(tmem, q * 32, c0), v);
+            if (live) {
+                if constexpr (EPI == EPI_DRELU || EPI == EPI_DSOFTPLUS) {
+                    const __half* gp = p.G + grow * (int64_t)p.ldg + n0 + c0;
 #pragma unroll
-                for (int j = 0; j < 32; j += 8) {
-                    float g[8];
-                    load_half8(gp + j, g);
+                    for (int j = 0; j < CHUNK; j += 8) {
+                        float g[8];
+                        load_half8(gp + j, g);
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        const float d = (p.epi == EPI_DRELU) ? (g[i] > 0.0f ? 1.0f : 0.0f)
-                                                             : (1.0f - __expf(-p.beta * g[i]));
-                        v[j + i] *= d;
+                        for (int i = 0; i < 8; ++i) {
+                            if constexpr (EPI == EPI_DRELU) v[j + i] = g[i] > 0.0f ? v[j + i] : 0.0f;
+                            else v[j + i] *= 1.0f - __expf(-p.beta * g[i]);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < CHUNK; ++j) {
+                        const float z = v[j] + bias_s[c0 + j];
+                        if constexpr (EPI == EPI_RELU) v[j] = fmaxf(z, 0.0f);
+                        else if constexpr (EPI == EPI_SOFTPLUS) v[j] = softplus_fast_h(z, p.beta, inv_beta);
+                        else v[j] = z;
                     }
                 }
-            } else {
+                if (p.y_f32) {
+                    float* yp = reinterpret_cast<float*>(p.Y) + grow * (int64_t)p.ldy + n0 + c0;
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const float z = v[j] + bias_s[c0 + j];
-                    v[j] = (p.epi == EPI_RELU) ? fmaxf(z, 0.0f)
-                         : (p.epi == EPI_SOFTPLUS) ? softplus_fast_h(z, p.beta, inv_beta) : z;
-                }
-            }
-            if (p.y_f32) {
-                float* yp = reinterpret_cast<float*>(p.Y) + grow * (int64_t)p.ldy + n0 + c0;
+                    for (int j = 0; j < CHUNK; j += 4) *reinterpret_cast<float4*>(yp + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                } else {
+                    __half* yp = reinterpret_cast<__half*>(p.Y) + grow * (int64_t)p.ldy + n0 + c0;
 #pragma unroll
-                for (int j = 0; j < 32; j += 4) *reinterpret_cast<float4*>(yp + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
-            } else {
-                __half* yp = reinterpret_cast<__half*>(p.Y) + grow * (int64_t)p.ldy + n0 + c0;
+                    for (int j = 0; j < CHUNK; j += 8) store_half8(yp + j, v + j);
+                    if (p.Ylo) {
+                        __half* lp = reinterpret_cast<__half*>(p.Ylo) + grow * (int64_t)p.ldy + n0 + c0;
 #pragma unroll
-                for (int j = 0; j < 32; j += 8) store_half8(yp + j, v + j);
-                if (p.Ylo) {
-                    __half* lp = reinterpret_cast<__half*>(p.Ylo) + grow * (int64_t)p.ldy + n0 + c0;
+                        for (int j = 0; j < CHUNK; j += 8) {
+                            float lo[8];
 #pragma unroll
-                    for (int j = 0; j < 32; j += 8) {
-                        float lo[8];
-#pragma unroll
-                        for (int i = 0; i < 8; ++i) lo[i] = v[j + i] - __half2float(__float2half_rn(v[j + i]));
-                        store_half8(lp + j, lo);
+                            for (int i = 0; i < 8; ++i) lo[i] = v[j + i] - __half2float(__float2half_rn(v[j + i]));
+                            store_half8(lp + j, lo);
+                        }
                     }
                 }
             }
@@ -193,27 +203,38 @@ static size_t dense_smem(int n_tile, int K, bool split) {
     return (size_t)n_tile * K * 2 + (split ? 2 : 1) * (size_t)TILE_M * K * 2 + n_tile * 4 + 16;
 }
 
-template <int N_TILE>
+template <int N_TILE, int EPI>
 static int launch_dense(const DenseParams& p, cudaStream_t s) {
     const size_t smem = dense_smem(N_TILE, p.K, p.Xlo != nullptr);
     if (smem > 227 * 1024) {
         set_error("dense layer K=%d N_TILE=%d needs %zu B of shared memory", p.K, N_TILE, smem);
         return GBSDF_ERR_UNSUPPORTED;
     }
-    cudaFuncSetAttribute(k_dense<N_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_dense<N_TILE, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int64_t ntiles = (p.M + TILE_M - 1) / TILE_M;
     int64_t groups = sm_count() / p.n_split;
     if (groups < 1) groups = 1;
     if (groups > ntiles) groups = ntiles;
-    k_dense<N_TILE><<<(unsigned)(groups * p.n_split), DENSE_THREADS, smem, s>>>(p);
+    k_dense<N_TILE, EPI><<<(unsigned)(groups * p.n_split), DENSE_TPB, smem, s>>>(p);
     return launch_status("dense");
+}
+
+template <int N_TILE>
+static int launch_dense_epi(const DenseParams& p, cudaStream_t s) {
+    switch (p.epi) {
+        case EPI_IDENTITY: return launch_dense<N_TILE, EPI_IDENTITY>(p, s);
+        case EPI_RELU: return launch_dense<N_TILE, EPI_RELU>(p, s);
+        case EPI_SOFTPLUS: return launch_dense<N_TILE, EPI_SOFTPLUS>(p, s);
+        case EPI_DRELU: return launch_dense<N_TILE, EPI_DRELU>(p, s);
+        default: return launch_dense<N_TILE, EPI_DSOFTPLUS>(p, s);
+    }
 }
 
 int dense_launch(const DenseParams& p, int n_tile, cudaStream_t s) {
     switch (n_tile) {
-        case 64: return launch_dense<64>(p, s);
-        case 128: return launch_dense<128>(p, s);
-        case 256: return launch_dense<256>(p, s);
+        case 64: return launch_dense_epi<64>(p, s);
+        case 128: return launch_dense_epi<128>(p, s);
+        case 256: return launch_dense_epi<256>(p, s);
         default: set_error("unsupported n_tile %d", n_tile); return GBSDF_ERR_UNSUPPORTED;
     }
 }

@@ -63,6 +63,18 @@ __device__ __forceinline__ void issue_tile_mma(uint32_t d_tmem, uint32_t a_saddr
     }
 }
 
+// the same with different row widths of the A and B tiles (a K-column prefix of a wider tile)
+__device__ __forceinline__ void issue_tile_mma_strided(uint32_t d_tmem, uint32_t a_saddr, int a_kcols,
+                                                       uint32_t b_saddr, int b_kcols, int K, uint32_t idesc,
+                                                       bool accumulate_first = false) {
+    const uint32_t sbo_a = (uint32_t)a_kcols * 16u, sbo_b = (uint32_t)b_kcols * 16u;
+    for (int ks = 0; ks < K / 16; ++ks) {
+        const uint64_t ad = umma::make_desc(a_saddr + ks * 256u, 128u, sbo_a);
+        const uint64_t bd = umma::make_desc(b_saddr + ks * 256u, 128u, sbo_b);
+        umma::mma_f16(d_tmem, ad, bd, idesc, (ks > 0 || accumulate_first) ? 1u : 0u);
+    }
+}
+
 __device__ __forceinline__ void store_half8(__half* dst, const float* v) {
     __half2 h[4];
 #pragma unroll

@@ -152,18 +152,19 @@ __device__ void stage_encoding(const FieldParams& p, int64_t s0, uint8_t* a_s, u
 
 // x0ext row t*126 + r (r = e*18 + sl) of every tile: the features of level l in
 // columns [l F, l F + F) as fp16 hi and, at K0 + 16 + l F, the fp16 residual lo;
-// the level-0 thread also writes the tail (x, y, z hi, 1, x, y, z lo) and zeroes
-// the padding columns.  Rows of samples past the end are zeros.
+// the level-0 thread also writes the 16-column tail after the hi features and
+// zeroes the padding columns.  Rows of samples past the end are zeros.
 template <int F>
 __global__ void __launch_bounds__(256) k_field_gather(FieldParams p, int64_t ntiles) {
     const int A = p.active, K0 = p.K0, KX = 2 * K0 + 16;
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t rows = ntiles * (SPT * EVALS);
-    if (i >= rows * A) return;
-    const int64_t grow = i / A;
-    const int l = (int)(i % A);
+    // 32-bit index arithmetic: the launcher checks rows * A < 2^32
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t rows = (uint32_t)(ntiles * (SPT * EVALS));
+    if (i >= rows * (uint32_t)A) return;
+    const uint32_t grow = i / (uint32_t)A;
+    const int l = (int)(i - grow * (uint32_t)A);
     const int64_t t = grow / (SPT * EVALS);
-    const int r = (int)(grow % (SPT * EVALS));
+    const int r = (int)(grow - (uint32_t)t * (SPT * EVALS));
     const int e = r / SPT, sl = r % SPT;
     const int64_t s = t * SPT + sl;
     __half* dst = (__half*)p.x0ext + grow * KX;
@@ -186,10 +187,14 @@ __global__ void __launch_bounds__(256) k_field_gather(FieldParams p, int64_t nti
     write_half_row<F>(reinterpret_cast<uint8_t*>(dst + l * F), v);
     write_half_row<F>(reinterpret_cast<uint8_t*>(dst + K0 + 16 + l * F), lo);
     if (l == 0) {
+        // tail (multiplied by w0b's position and bias columns in the forward MMA):
+        // x hi, 1, x lo, 1, x hi, zeros -- w0x x + b0 as fp16 hi/lo products
         float tail[16] = {0.f};
         if (live) {
             tail[0] = x[0]; tail[1] = x[1]; tail[2] = x[2]; tail[3] = 1.0f;
             for (int k = 0; k < 3; ++k) tail[4 + k] = x[k] - __half2float(__float2half_rn(x[k]));
+            tail[7] = 1.0f;
+            tail[8] = x[0]; tail[9] = x[1]; tail[10] = x[2];
         }
         store_half8(dst + K0, tail);
         store_half8(dst + K0 + 8, tail + 8);
@@ -206,13 +211,16 @@ __global__ void __launch_bounds__(256) k_field_gather(FieldParams p, int64_t nti
 template <int F>
 __global__ void __launch_bounds__(256) k_field_scatter(FieldParams p) {
     const int A = p.active, K0 = p.K0;
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= p.Ns * A * 8) return;
-    const int cc = (int)(i & 7);
-    const int l = (int)((i >> 3) % A);
-    const int64_t s = (i >> 3) / A;
-    const int64_t t = s / SPT;
-    const int sl = (int)(s % SPT);
+    // 32-bit index arithmetic: the launcher checks Ns * A * 8 < 2^32
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint32_t)p.Ns * (uint32_t)A * 8u) return;
+    const int cc = (int)(i & 7u);
+    const uint32_t sl_ = i >> 3;
+    const uint32_t s32 = sl_ / (uint32_t)A;
+    const int l = (int)(sl_ - s32 * (uint32_t)A);
+    const int64_t s = s32;
+    const int64_t t = s32 / SPT;
+    const int sl = (int)(s32 - (uint32_t)t * SPT);
     float c[3];
     sample_point(p, s, c);
     const LevelDesc d = level_desc(p.grid, l);
@@ -261,30 +269,31 @@ __global__ void __launch_bounds__(256) k_field_scatter(FieldParams p) {
 // ---------------------------------------------------------------------------
 // forward
 
+// Two CTAs per SM: one CTA's epilogue overlaps the other's staging, MMAs and
+// per-sample phase.  The pre-activation comes out of the MMA complete: the A
+// tile is x0ext's [features hi | tail] columns and B = w0b = [W0e | position and
+// bias columns], so the epilogue reads W0x x + b0 + W0e f from TMEM and adds
+// nothing; the fp16 residual of the features is a second MMA over the W0e prefix.
+constexpr int FWD_CTAS_PER_SM = 2;
+
 template <int F>
-__global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
+__global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(FieldParams p) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int K0 = p.K0;
-    uint8_t* w_s = smem;                                        // [256 x K0]
-    uint8_t* a_s = w_s + HID * K0 * 2;                          // [128 x K0] features, fp16 hi
-    uint8_t* a2_s = a_s + TILE_M * K0 * 2;                      // [128 x K0] features, fp16 lo
-    float* w0x_s = reinterpret_cast<float*>(a2_s + TILE_M * K0 * 2);   // [256*3]
-    float* b0_s = w0x_s + HID * 3;
-    float* wh_s = b0_s + HID;
+    const int KB = K0 + 16;                                     // features hi + tail
+    const int KX = 2 * K0 + 16;                                 // x0ext row width
+    uint8_t* w_s = smem;                                        // [256 x KB]  w0b
+    uint8_t* a_s = w_s + HID * KB * 2;                          // [128 x KB]  features hi | tail
+    uint8_t* a2_s = a_s + TILE_M * KB * 2;                      // [128 x K0]  features lo
+    float* wh_s = reinterpret_cast<float*>(a2_s + TILE_M * K0 * 2);   // [256]
     float* part_s = wh_s + HID;                                 // [2][128] partial head sums
     float* sdf_s = part_s + 2 * TILE_M;                         // [7][18]
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sdf_s + EVALS * SPT + 2);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    stage_rows_kmajor(w_s, (const __half*)p.w0e, 0, HID, K0, K0, tid, FIELD_THREADS, HID);
-    for (int i = tid; i < HID * 3; i += FIELD_THREADS) w0x_s[i] = p.w0x[i];
-    for (int i = tid; i < HID; i += FIELD_THREADS) {
-        b0_s[i] = p.b0[i];
-        wh_s[i] = p.whead[i];
-    }
-    for (int i = tid; i < 2 * TILE_M * K0 / 8; i += FIELD_THREADS)
-        reinterpret_cast<uint4*>(a_s)[i] = make_uint4(0, 0, 0, 0);
+    stage_rows_kmajor(w_s, (const __half*)p.w0b, 0, HID, KB, KB, tid, FIELD_THREADS, HID);
+    for (int i = tid; i < HID; i += FIELD_THREADS) wh_s[i] = p.whead[i];
     if (tid == 0) {
         umma::mbar_init(mbar, 1);
         umma::fence_mbar_init();
@@ -306,19 +315,22 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
     const int e_row = row / SPT, sl_row = row % SPT;
     uint32_t phase = 0;
 
-    // features of a tile, gathered by k_field_gather into x0ext (hi | tail | lo); the
-    // next tile's load overlaps this tile's epilogue (A is free once its MMAs completed)
+    // features of a tile, gathered by k_field_gather into x0ext; the next tile's
+    // load overlaps this tile's epilogue (A is free once its MMAs completed)
     const int64_t xrows = ntiles * (int64_t)(SPT * EVALS);
     auto stage = [&](int64_t tt) {
         const __half* xb = (const __half*)p.x0ext;
-        stage_rows_kmajor(a_s, xb, tt * (SPT * EVALS), xrows, 2 * K0 + 16, K0, tid, FIELD_THREADS);
-        stage_rows_kmajor(a2_s, xb + K0 + 16, tt * (SPT * EVALS), xrows, 2 * K0 + 16, K0, tid, FIELD_THREADS);
+        stage_rows_kmajor(a_s, xb, tt * (SPT * EVALS), xrows, KX, KB, tid, FIELD_THREADS);
+        stage_rows_kmajor(a2_s, xb + K0 + 16, tt * (SPT * EVALS), xrows, KX, K0, tid, FIELD_THREADS);
     };
     auto issue = [&]() {
         if (tid == 0) {
             umma::fence_after_sync();
-            issue_tile_mma(tmem, a_addr, w_addr, K0, idesc);
-            issue_tile_mma(tmem, a2_addr, w_addr, K0, idesc, true);
+            // smallest terms first: the tensor core's FP32 accumulation drops low
+            // bits of addends much smaller than the running sum, so the fp16
+            // residuals go in before the hi features and the large position/bias tail
+            issue_tile_mma_strided(tmem, a2_addr, K0, w_addr, KB, K0, idesc);
+            issue_tile_mma(tmem, a_addr, w_addr, KB, idesc, true);
             umma::mma_commit(mbar);
         }
     };
@@ -341,15 +353,9 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
         umma::fence_after_sync();
         const int64_t tn = t + gridDim.x;
         if (tn < ntiles) stage(tn);
-        // epilogue: pre = acc + W0x x + b0 ; h = softplus ; partial head dot
+        // epilogue: h = softplus(pre) ; partial head dot ; centre rows keep h in h0c
         const int64_t s = s0 + sl_row;
-        const bool live = row < SPT * EVALS && s < p.Ns;
-        float x[3] = {0.f, 0.f, 0.f};
-        if (live) {
-            float c[3];
-            sample_point(p, s, c);
-            eval_point(c, e_row, p.eps, x);
-        }
+        const bool keep = row < SPT * EVALS && s < p.Ns && e_row == 0;
         float part4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         const float inv_beta = 1.0f / p.beta;
 #pragma unroll 1
@@ -358,13 +364,11 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
             umma::tmem_ld32(umma::taddr(tmem, q * 32, c0), v);
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
-                const int n = c0 + j;
-                float z = v[j] + w0x_s[3 * n] * x[0] + w0x_s[3 * n + 1] * x[1] + w0x_s[3 * n + 2] * x[2] + b0_s[n];
-                const float h = softplus_fast_h(z, p.beta, inv_beta);
+                const float h = softplus_fast_h(v[j], p.beta, inv_beta);
                 v[j] = h;
-                part4[j & 3] = fmaf(wh_s[n], h, part4[j & 3]);
+                part4[j & 3] = fmaf(wh_s[c0 + j], h, part4[j & 3]);
             }
-            if (live && e_row == 0) {
+            if (keep) {
                 __half* dst = (__half*)p.h0c + s * HID + c0;
 #pragma unroll
                 for (int j = 0; j < 32; j += 8) store_half8(dst + j, v + j);
@@ -433,6 +437,9 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
                     }
                     __half* dst = (__half*)p.xc + ss * (int64_t)p.ldxc + HID;
                     const int ncol = p.ldxc - HID;
+                    // the last (padding) column is a constant 1: the colour layer-0 weight
+                    // gradient dZ^T xc then carries the bias gradient in that column
+                    col[ncol - 1] = 1.0f;
                     for (int k = 0; k < ncol; k += 8) store_half8(dst + k, col + k);
                 }
             }
@@ -452,37 +459,44 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_fwd(FieldParams p) {
 // ---------------------------------------------------------------------------
 // backward
 
+// One 128-row tile (18 samples x 7 evaluations) per iteration:
+//   MMA1 recomputes the pre-activations (A = x0ext's features hi | tail, B = w0b;
+//        plus the features lo against the W0e prefix), exactly as the forward;
+//   the epilogue forms d_pre = (d f w_head + [centre] d_h0c) softplus'(pre) and the
+//        head-weight gradient, writes d_pre as an fp16 hi + lo pair into TMEM (the A
+//        operand of MMA2) and its hi half to global for the layer-0 weight gradient;
+//   MMA2 d_enc = d_pre W0e (A from TMEM, B = W0e^T in shared memory) goes to global
+//        for k_field_scatter.
+// The +eps and -eps taps of a sample carry large, nearly cancelling d_pre, so a
+// single fp16 rounding of d_pre would dominate the table-gradient error: hence the pair.
+// TMEM (512 columns, one CTA per SM): [0, 256) MMA1's accumulator, reused for
+// MMA2's [128 x K0] result; [256, 384) d_pre hi, [384, 512) d_pre lo.
+constexpr size_t BWD_SMEM_FLOOR = 120 * 1024;   // > half an SM's shared memory: one CTA per SM
+constexpr int BWD_THREADS = 512;                 // 16 warps: 4 lane quadrants x 4 quarters of the hidden units
+
 template <int F>
-__global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
+__global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int K0 = p.K0;
+    const int KB = K0 + 16;                                     // features hi + tail
     const int KX = 2 * K0 + 16;                                 // x0ext row width
-    uint8_t* w_s = smem;                                        // [256 x K0]   B of MMA1
-    uint8_t* wt_s = w_s + HID * K0 * 2;                         // [K0 x 256]   B of MMA2
-    uint8_t* a_s = wt_s + K0 * HID * 2;                         // [128 x K0]   encoding tile, fp16 hi
-    uint8_t* a3_s = a_s + TILE_M * K0 * 2;                      // [128 x K0]   encoding tile, fp16 lo
-    // d_pre is split into fp16 hi + lo tiles (d_pre = hi + lo to ~2^-22) when both fit:
-    // the +eps and -eps taps of a sample carry large, nearly cancelling gradients,
-    // so a single fp16 rounding of d_pre would dominate the table-gradient error.
-    const bool split = K0 <= 64;
-    uint8_t* p_s = a3_s + TILE_M * K0 * 2;                      // [128 x 256]  d_pre hi (fp16); reused as fp32 d_enc
-    uint8_t* p2_s = p_s + TILE_M * HID * 2;                     // [128 x 256]  d_pre lo (fp16), when split
-    // W0's position columns, bias and the head weights are read through L1 (__ldg):
-    // shared memory is full with the operand tiles.
-    const float* w0x_s = p.w0x;
-    const float* b0_s = p.b0;
-    const float* wh_s = p.whead;
-    float* dwh_s = reinterpret_cast<float*>(p2_s + (split ? TILE_M * HID * 2 : 0));   // [256] d_whead accumulator
+    uint8_t* w_s = smem;                                        // [256 x KB]  w0b: B of MMA1
+    uint8_t* wt_s = w_s + HID * KB * 2;                         // [K0 x 256]  W0e^T: B of MMA2
+    uint8_t* a_s = wt_s + K0 * HID * 2;                         // [128 x KB]  features hi | tail
+    uint8_t* a3_s = a_s + TILE_M * KB * 2;                      // [128 x K0]  features lo
+    float* wh_s = reinterpret_cast<float*>(a3_s + TILE_M * K0 * 2);   // [256] head weights
+    float* dwh_s = wh_s + HID;                                  // [256] d_whead accumulator
     float* df_s = dwh_s + HID;                                  // [7][18] d f per evaluation
     uint64_t* mbar = reinterpret_cast<uint64_t*>(df_s + EVALS * SPT + 2);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    stage_rows_kmajor(w_s, (const __half*)p.w0e, 0, HID, K0, K0, tid, FIELD_THREADS, HID);
-    stage_rows_kmajor(wt_s, (const __half*)p.w0eT, 0, K0, HID, HID, tid, FIELD_THREADS, K0);
-    for (int i = tid; i < HID; i += FIELD_THREADS) dwh_s[i] = 0.0f;
-    for (int i = tid; i < 2 * TILE_M * K0 / 8; i += FIELD_THREADS)
-        reinterpret_cast<uint4*>(a_s)[i] = make_uint4(0, 0, 0, 0);
+    stage_rows_kmajor(w_s, (const __half*)p.w0b, 0, HID, KB, KB, tid, BWD_THREADS, HID);
+    stage_rows_kmajor(wt_s, (const __half*)p.w0eT, 0, K0, HID, HID, tid, BWD_THREADS, K0);
+    for (int i = tid; i < HID; i += BWD_THREADS) {
+        wh_s[i] = p.whead[i];
+        dwh_s[i] = 0.0f;
+    }
     if (tid == 0) {
         umma::mbar_init(mbar, 1);
         umma::fence_mbar_init();
@@ -495,14 +509,13 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
     __syncthreads();
     umma::fence_after_sync();
     const uint32_t tmem = *tslot;
-    const uint32_t tmem2 = tmem + HID;                          // D2 columns [256, 256 + K0)
+    const uint32_t t_hi = tmem + HID, t_lo = tmem + HID + HID / 2;
     const uint32_t idesc1 = umma::idesc_f16(TILE_M, HID);
     const uint32_t idesc2 = umma::idesc_f16(TILE_M, K0);
     const uint32_t a_addr = umma::smem_u32(a_s), w_addr = umma::smem_u32(w_s);
-    const uint32_t p_addr = umma::smem_u32(p_s), wt_addr = umma::smem_u32(wt_s), p2_addr = umma::smem_u32(p2_s);
-    const uint32_t a3_addr = umma::smem_u32(a3_s);
+    const uint32_t wt_addr = umma::smem_u32(wt_s), a3_addr = umma::smem_u32(a3_s);
     const int64_t ntiles = (p.Ns + SPT - 1) / SPT;
-    const int q = warp & 3, half = warp >> 2;
+    const int q = warp & 3, part = warp >> 2;                   // lane quadrant, quarter of the hidden units
     const int row = q * 32 + lane;
     const int e_row = row / SPT, sl_row = row % SPT;
     uint32_t phase = 0;
@@ -559,14 +572,14 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
     const int64_t xrows = ntiles * (int64_t)(SPT * EVALS);
     auto stage = [&](int64_t tt) {
         const __half* xb = (const __half*)p.x0ext;
-        stage_rows_kmajor(a_s, xb, tt * (SPT * EVALS), xrows, KX, K0, tid, FIELD_THREADS);
-        stage_rows_kmajor(a3_s, xb + K0 + 16, tt * (SPT * EVALS), xrows, KX, K0, tid, FIELD_THREADS);
+        stage_rows_kmajor(a_s, xb, tt * (SPT * EVALS), xrows, KX, KB, tid, BWD_THREADS);
+        stage_rows_kmajor(a3_s, xb + K0 + 16, tt * (SPT * EVALS), xrows, KX, K0, tid, BWD_THREADS);
     };
     auto issue1 = [&]() {
         if (tid == 0) {
             umma::fence_after_sync();
-            issue_tile_mma(tmem, a_addr, w_addr, K0, idesc1);
-            issue_tile_mma(tmem, a3_addr, w_addr, K0, idesc1, true);
+            issue_tile_mma_strided(tmem, a3_addr, K0, w_addr, KB, K0, idesc1);   // residuals first
+            issue_tile_mma(tmem, a_addr, w_addr, KB, idesc1, true);
             umma::mma_commit(mbar);
         }
     };
@@ -590,77 +603,75 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
         const int64_t tn = t + gridDim.x;
         if (tn < ntiles) stage(tn);                  // A is free: MMA1 of tile t completed
         umma::fence_after_sync();
-        // (2) d_pre = (d f * w_head + [centre] d_h0c) * softplus'(pre)
+        // (2) d_pre = (d f * w_head + [centre] d_h0c) * softplus'(pre) -> TMEM (hi, lo) and d_pre0
         {
             const int64_t s = s0 + sl_row;
             const bool live = row < SPT * EVALS && s < p.Ns;
-            float x[3] = {0.f, 0.f, 0.f};
-            float df = 0.0f;
-            if (live) {
-                float c[3];
-                sample_point(p, s, c);
-                eval_point(c, e_row, p.eps, x);
-                df = df_s[row];
-            }
+            const float df = live ? df_s[row] : 0.0f;
             const bool centre = live && e_row == 0;
             const float inv_beta = 1.0f / p.beta;
 #pragma unroll 1
-            for (int c0 = half * 128; c0 < half * 128 + 128; c0 += 32) {
-                float v[32];
-                umma::tmem_ld32(umma::taddr(tmem, q * 32, c0), v);
-                float dh0[32];
+            for (int c0 = part * 64; c0 < part * 64 + 64; c0 += 16) {
+                float v[16];
+                umma::tmem_ld16(umma::taddr(tmem, q * 32, c0), v);
+                float dh0[16];
                 if (centre) {
                     const float4* src = reinterpret_cast<const float4*>(p.d_h0c + s * HID + c0);
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
+                    for (int j = 0; j < 4; ++j) {
                         const float4 f = src[j];
                         dh0[4 * j] = f.x; dh0[4 * j + 1] = f.y; dh0[4 * j + 2] = f.z; dh0[4 * j + 3] = f.w;
                     }
                 } else {
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) dh0[j] = 0.0f;
+                    for (int j = 0; j < 16; ++j) dh0[j] = 0.0f;
                 }
-                float hc[32];   // d f * h per column: d w_head = sum over rows
+                float hc[16];   // d f * h per column: d w_head = sum over rows
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int n = c0 + j;
-                    const float z = v[j] + __ldg(&w0x_s[3 * n]) * x[0] + __ldg(&w0x_s[3 * n + 1]) * x[1] +
-                                    __ldg(&w0x_s[3 * n + 2]) * x[2] + __ldg(&b0_s[n]);
+                for (int j = 0; j < 16; ++j) {
                     float hval, sg;
-                    softplus_fast(z, p.beta, inv_beta, hval, sg);
-                    v[j] = live ? (df * __ldg(&wh_s[n]) + dh0[j]) * sg : 0.0f;
+                    softplus_fast(v[j], p.beta, inv_beta, hval, sg);
+                    v[j] = live ? (df * wh_s[c0 + j] + dh0[j]) * sg : 0.0f;
                     hc[j] = live ? df * hval : 0.0f;
                 }
                 {
-                    const float colsum = warp_column_sum32(hc, lane);
-                    if (colsum != 0.0f) atomicAdd(&dwh_s[c0 + lane], colsum);
+                    const float colsum = warp_column_sum16(hc, lane);
+                    if (lane < 16 && colsum != 0.0f) atomicAdd(&dwh_s[c0 + lane], colsum);
                 }
-                // d_pre into the MMA2 A tile(s) (K-major over the 256 hidden units) and to global
+                uint32_t hi[8], lo[8];
 #pragma unroll
-                for (int j = 0; j < 32; j += 8) {
-                    store_half8(reinterpret_cast<__half*>(p_s + umma::kmajor_offset(row, c0 + j, HID)), v + j);
-                    if (split) {
-                        float lo[8];
-#pragma unroll
-                        for (int i = 0; i < 8; ++i) lo[i] = v[j + i] - __half2float(__float2half_rn(v[j + i]));
-                        store_half8(reinterpret_cast<__half*>(p2_s + umma::kmajor_offset(row, c0 + j, HID)), lo);
-                    }
+                for (int i = 0; i < 8; ++i) {
+                    const __half2 h2 = __floats2half2_rn(v[2 * i], v[2 * i + 1]);
+                    const float2 b = __half22float2(h2);
+                    const __half2 l2 = __floats2half2_rn(v[2 * i] - b.x, v[2 * i + 1] - b.y);
+                    hi[i] = *reinterpret_cast<const uint32_t*>(&h2);
+                    lo[i] = *reinterpret_cast<const uint32_t*>(&l2);
                 }
+                umma::tmem_st8(umma::taddr(t_hi, q * 32, c0 / 2), hi);
+                umma::tmem_st8(umma::taddr(t_lo, q * 32, c0 / 2), lo);
                 if (row < SPT * EVALS) {   // dead samples store zeros (their x0ext rows are zero too)
-                    __half* dst = (__half*)p.d_pre0 + (t * (SPT * EVALS) + row) * (int64_t)HID + c0;
-#pragma unroll
-                    for (int j = 0; j < 32; j += 8) store_half8(dst + j, v + j);
+                    uint4* dst = reinterpret_cast<uint4*>((__half*)p.d_pre0 + (t * (SPT * EVALS) + row) * (int64_t)HID +
+                                                          c0);
+                    dst[0] = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+                    dst[1] = make_uint4(hi[4], hi[5], hi[6], hi[7]);
                 }
             }
         }
+        umma::tmem_wait_st();
         umma::fence_before_sync();
-        umma::fence_proxy_async_smem();
         __syncthreads();
-        // (3) d_enc = d_pre * W0e  (MMA2: A = d_pre [128 x 256], B = W0e^T [K0 x 256])
+        // (3) d_enc = d_pre * W0e  (MMA2: A = d_pre [128 x 256] in TMEM, B = W0e^T [K0 x 256])
         if (tid == 0) {
             umma::fence_after_sync();
-            issue_tile_mma(tmem2, p_addr, wt_addr, HID, idesc2);
-            if (split) issue_tile_mma(tmem2, p2_addr, wt_addr, HID, idesc2, true);
+            const uint32_t sbo = (uint32_t)HID * 16u;
+            for (int ks = 0; ks < HID / 16; ++ks) {          // the lo half first (smaller addends)
+                const uint64_t bd = umma::make_desc(wt_addr + ks * 256u, 128u, sbo);
+                umma::mma_f16_ta(tmem, t_lo + ks * 8, bd, idesc2, ks > 0 ? 1u : 0u);
+            }
+            for (int ks = 0; ks < HID / 16; ++ks) {
+                const uint64_t bd = umma::make_desc(wt_addr + ks * 256u, 128u, sbo);
+                umma::mma_f16_ta(tmem, t_hi + ks * 8, bd, idesc2, 1u);
+            }
             umma::mma_commit(mbar);
         }
         ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
@@ -670,20 +681,20 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
             break;
         }
         umma::fence_after_sync();
-        {   // (4) d_enc rows to global for k_field_scatter
-            const int cols = K0 / 2;                            // each half of the warps stores half the columns
-            for (int c0 = half * cols; c0 < half * cols + cols; c0 += 16) {
-                float v[16];
-                umma::tmem_ld16(umma::taddr(tmem2, q * 32, c0), v);
-                if (row < SPT * EVALS) {
-                    float* dst = p.d_enc + (t * (SPT * EVALS) + row) * (int64_t)K0 + c0;
+        // (4) d_enc rows to global for k_field_scatter: 16-column chunks dealt in turn
+        // to the four warps of a lane quadrant
+        for (int c0 = part * 16; c0 < K0; c0 += 64) {
+            float v[16];
+            umma::tmem_ld16(umma::taddr(tmem, q * 32, c0), v);
+            if (row < SPT * EVALS) {
+                float* dst = p.d_enc + (t * (SPT * EVALS) + row) * (int64_t)K0 + c0;
 #pragma unroll
-                    for (int j = 0; j < 16; j += 4) *reinterpret_cast<float4*>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
-                }
+                for (int j = 0; j < 16; j += 4)
+                    *reinterpret_cast<float4*>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
             }
         }
         umma::fence_before_sync();
-        __syncthreads();                              // df_s of tile t fully read
+        __syncthreads();                              // df_s and the TMEM accumulator of tile t fully read
         if (tn < ntiles) {
             prologue(tn);
             cp_async_wait_all();
@@ -694,7 +705,7 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_field_bwd(FieldParams p) {
     }
     umma::fence_before_sync();
     __syncthreads();
-    for (int i = tid; i < HID; i += FIELD_THREADS)
+    for (int i = tid; i < HID; i += BWD_THREADS)
         if (dwh_s[i] != 0.0f) atomicAdd(&p.d_whead[i], dwh_s[i]);
     dbh = warp_sum(dbh);
     if (lane == 0 && dbh != 0.0f) atomicAdd(p.d_bhead, dbh);
@@ -790,8 +801,8 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_sdf_points(FieldParams p, 
         __syncthreads();
         if (tid == 0) {
             umma::fence_after_sync();
-            issue_tile_mma(tmem, a_addr, w_addr, K0, idesc);
-            issue_tile_mma(tmem, a2_addr, w_addr, K0, idesc, true);
+            issue_tile_mma(tmem, a2_addr, w_addr, K0, idesc);          // residuals first
+            issue_tile_mma(tmem, a_addr, w_addr, K0, idesc, true);
             umma::mma_commit(mbar);
         }
         const bool ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
@@ -835,13 +846,14 @@ static int num_sms() {
 }
 
 static size_t fwd_smem(int K0) {
-    return (size_t)HID * K0 * 2 + 2 * (size_t)TILE_M * K0 * 2 + (HID * 3 + 2 * HID + 2 * TILE_M + EVALS * SPT + 2) * 4 +
-           16;
+    const size_t KB = (size_t)K0 + 16;
+    return (size_t)HID * KB * 2 + (size_t)TILE_M * (KB + K0) * 2 + (HID + 2 * TILE_M + EVALS * SPT + 2) * 4 + 16;
 }
 static size_t bwd_smem(int K0) {
-    const size_t ptiles = K0 <= 64 ? 2 : 1;
-    return (size_t)HID * K0 * 2 * 2 + 2 * (size_t)TILE_M * K0 * 2 + ptiles * TILE_M * HID * 2 +
-           (HID + EVALS * SPT + 2) * 4 + 16;
+    const size_t KB = (size_t)K0 + 16;
+    const size_t need = (size_t)HID * KB * 2 + (size_t)K0 * HID * 2 + (size_t)TILE_M * (KB + K0) * 2 +
+                        (2 * HID + EVALS * SPT + 2) * 4 + 16;
+    return need > BWD_SMEM_FLOOR ? need : BWD_SMEM_FLOOR;
 }
 
 template <int F>
@@ -852,11 +864,19 @@ static int launch_field(const FieldParams& p, bool backward, cudaStream_t s) {
         return GBSDF_ERR_UNSUPPORTED;
     }
     const int64_t ntiles = (p.Ns + SPT - 1) / SPT;
-    int64_t grid = num_sms();
+    int64_t grid = num_sms() * (backward ? 1 : FWD_CTAS_PER_SM);
     if (grid > ntiles) grid = ntiles;
+    // largest thread index: gather ntiles * 126 * active, scatter Ns * active * 8
+    const int64_t gather_items = ntiles * (SPT * EVALS) * (int64_t)p.active;
+    const int64_t scatter_items = p.Ns * (int64_t)p.active * 8;
+    if ((gather_items > scatter_items ? gather_items : scatter_items) >= ((int64_t)1 << 32)) {
+        set_error("%lld samples x %d levels exceed the 32-bit index range of one launch", (long long)p.Ns,
+                  p.active);
+        return GBSDF_ERR_UNSUPPORTED;
+    }
     if (backward) {
         cudaFuncSetAttribute(k_field_bwd<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_field_bwd<F><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p);
+        k_field_bwd<F><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p);
         const int64_t items = p.Ns * p.active * 8;
         k_field_scatter<F><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p);
     } else {
@@ -899,8 +919,9 @@ extern "C" int gbsdf_field_fwd(const gbsdf_field_args* params, void* stream) {
     if (int st = check_field(p)) return st;
     if (p.Ns == 0) return GBSDF_OK;
     GBSDF_CHECK_ARG(p.sdf && p.grad && p.hess && p.h0c && p.x0ext, "NULL output");
-    GBSDF_CHECK_ARG(!p.xc || (p.ldxc % 16 == 0 && p.ldxc - HID >= 22 + p.app_dim && p.ldxc - HID <= 48),
-                    "xc leading dimension %d (needs 256 + 22 + app_dim <= ldxc <= 304, multiple of 16)", p.ldxc);
+    GBSDF_CHECK_ARG(p.w0b && aligned(p.w0b, 16), "w0b (fp16 [256, K0 + 16]) missing or misaligned");
+    GBSDF_CHECK_ARG(!p.xc || (p.ldxc % 16 == 0 && p.ldxc - HID >= 23 + p.app_dim && p.ldxc - HID <= 48),
+                    "xc leading dimension %d (needs 256 + 23 + app_dim <= ldxc <= 304, multiple of 16)", p.ldxc);
     GBSDF_CHECK_ARG(!p.xc || p.app_dim == 0 || (p.app_table && p.app_idx), "appearance table / index missing");
     switch (p.grid.n_features) {
         case 2: return launch_field<2>(p, false, as_stream(stream));
@@ -915,6 +936,7 @@ extern "C" int gbsdf_field_bwd(const gbsdf_field_args* params, void* stream) {
     const FieldParams& p = *params;
     if (int st = check_field(p)) return st;
     if (p.Ns == 0) return GBSDF_OK;
+    GBSDF_CHECK_ARG(p.w0b && aligned(p.w0b, 16), "w0b (fp16 [256, K0 + 16]) missing or misaligned");
     GBSDF_CHECK_ARG(p.w0eT && p.grad && p.d_sdf && p.d_grad && p.d_hess && p.d_xc && p.d_h0c && p.d_table &&
                         p.d_pre0 && p.x0ext && p.d_enc && p.d_whead && p.d_bhead,
                     "NULL pointer");

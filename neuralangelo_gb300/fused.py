@@ -34,7 +34,7 @@ class FieldArgs(ctypes.Structure):
     _fields_ = [("Ns", c_i64), ("S", c_i32), ("pad0", c_i32), ("sample_ray", c_vp), ("center", c_vp),
                 ("ray_unit", c_vp), ("dists", c_vp), ("outside", c_vp), ("app_idx", c_vp),
                 ("grid", _lib.GridStruct), ("active", c_i32), ("K0", c_i32), ("table", c_vp), ("w0e", c_vp),
-                ("w0eT", c_vp), ("w0x", c_vp), ("b0", c_vp), ("whead", c_vp), ("bhead", c_vp),
+                ("w0eT", c_vp), ("w0b", c_vp), ("w0x", c_vp), ("b0", c_vp), ("whead", c_vp), ("bhead", c_vp),
                 ("beta", c_f32), ("eps", c_f32), ("two_eps", c_f32), ("eps2", c_f32), ("outside_val", c_f32),
                 ("pad1", c_i32), ("xc", c_vp), ("ldxc", c_i32), ("app_dim", c_i32), ("app_table", c_vp),
                 ("sdf", c_vp), ("grad", c_vp), ("hess", c_vp), ("h0c", c_vp), ("d_sdf", c_vp), ("d_grad", c_vp),
@@ -107,13 +107,35 @@ def pack_sdf(sdf):
         W0 = sdf.mlp.linears[0].weight                           # [256, 3 + L F]
         w0e = torch.zeros(H, K0, device=W0.device, dtype=torch.float16)
         w0e[:, :A * F] = W0[:, 3:3 + A * F]
+        w0x = W0[:, :3].contiguous().float()
+        b0 = sdf.mlp.linears[0].bias.detach().float()
         pk = dict(
             table=sdf.tcnn_encoding.params.detach().half(),
-            w0e=w0e, w0eT=w0e.t().contiguous(),
-            w0x=W0[:, :3].contiguous().float(), b0=sdf.mlp.linears[0].bias.detach().float(),
+            w0e=w0e, w0eT=w0e.t().contiguous(), w0b=w0_with_tail(w0e, w0x, b0),
+            w0x=w0x, b0=b0,
             whead=sdf.mlp.linear_sdf.weight.detach()[0].contiguous().float(),
             bhead=sdf.mlp.linear_sdf.bias.detach().float())
     return pk, A, K0
+
+
+def w0_with_tail(w0e, w0x, b0):
+    """B operand [256, K0 + 16] of the forward field MMA: the fp16 encoding columns, then
+    the position columns and bias as fp16 hi/lo pairs matched to the x0ext tail
+    (x hi, 1, x lo, 1, x hi): w hi, b hi, w hi, b lo, w lo.  The products sum to
+    w0x x + b0 to ~2^-20 relative, so the pre-activation keeps FP32 accuracy."""
+    H, K0 = w0e.shape
+    hi = w0x.half()
+    lo = (w0x - hi.float()).half()
+    bh = b0.half()
+    bl = (b0 - bh.float()).half()
+    t = torch.zeros(H, K0 + 16, device=w0e.device, dtype=torch.float16)
+    t[:, :K0] = w0e
+    t[:, K0:K0 + 3] = hi
+    t[:, K0 + 3] = bh
+    t[:, K0 + 4:K0 + 7] = hi
+    t[:, K0 + 7] = bl
+    t[:, K0 + 8:K0 + 11] = lo
+    return t
 
 
 def sdf_weight_args(sdf, pk, A, K0, err=None):
@@ -121,7 +143,7 @@ def sdf_weight_args(sdf, pk, A, K0, err=None):
     fa = FieldArgs()
     fa.grid = sdf.tcnn_encoding.layout.struct
     fa.active, fa.K0 = A, K0
-    fa.table, fa.w0e, fa.w0eT = _p(pk['table']), _p(pk['w0e']), _p(pk['w0eT'])
+    fa.table, fa.w0e, fa.w0eT, fa.w0b = _p(pk['table']), _p(pk['w0e']), _p(pk['w0eT']), _p(pk['w0b'])
     fa.w0x, fa.b0, fa.whead, fa.bhead = _p(pk['w0x']), _p(pk['b0']), _p(pk['whead']), _p(pk['bhead'])
     fa.beta = float(sdf.cfg_sdf.mlp.activ_params.beta)
     fa.err = _p(err)
@@ -156,7 +178,7 @@ class FusedField:
         self.n_rgb_hidden = rgb.mlp.num_layers
         self.app_dim = cfg.appear_embed.dim if cfg.appear_embed.enabled else 0
         self.tail = 22 + self.app_dim                  # x 3, SH 16, normal 3, app
-        self.Kc0 = 256 + _round16(self.tail)
+        self.Kc0 = 256 + _round16(self.tail + 1)       # + a padding column of ones (bias gradient)
         self.F = sdf.tcnn_encoding.layout.n_features
         self.L = sdf.tcnn_encoding.layout.n_levels
         self.ws = None
@@ -205,18 +227,20 @@ class FusedField:
         key = (R, S, Ns, self.K0)
         if self.ws is not None and self.ws['key'] == key:
             return self.ws
+        self.ws = None                      # release the previous shape's buffers first
         rows0 = (Ns + 17) // 18 * 126      # layer-0 rows: 18 samples x 7 evaluations per tile
         f16, f32 = torch.float16, torch.float32
         e = lambda *s, dt=f32: torch.empty(*s, device=device, dtype=dt)  # noqa: E731
         Hc = self.Hc
         ws = dict(key=key)
         ws.update(sdf=e(Ns), grad=e(Ns, 3), hess=e(Ns, 3), h0c=e(Ns, 256, dt=f16), xc=e(Ns, self.Kc0, dt=f16),
-                  ys=[e(Ns, Hc, dt=f16) for _ in range(self.n_rgb_hidden)], rgbs=e(Ns, 3), rgb=e(R, 3),
+                  ys=[self._with_ones(e(Ns, Hc + 8, dt=f16), Hc) for _ in range(self.n_rgb_hidden)],
+                  rgbs=e(Ns, 3), rgb=e(R, 3),
                   weights=e(Ns), d_rgbs=e(Ns, 3), d_sdf=e(Ns), d_grad=e(Ns, 3), d_hess=e(Ns, 3),
                   loss_sums=torch.zeros(4, device=device, dtype=torch.float64), d_s_var=torch.zeros(1, device=device),
                   d_pre_last=e(Ns, 8, dt=f16), dzs=[e(Ns, Hc, dt=f16) for _ in range(2)],
-                  dzs_lo=[e(Ns, Hc, dt=f16) for _ in range(2)], dzfeat=e(Ns, 256, dt=f16),
-                  dzfeat_lo=e(Ns, 256, dt=f16),
+                  dzs_lo=[e(Ns, Hc, dt=f16) for _ in range(2)] if self.split else None,
+                  dzfeat=e(Ns, 256, dt=f16), dzfeat_lo=e(Ns, 256, dt=f16) if self.split else None,
                   dxc_tail=e(Ns, 64), d_h0c=e(Ns, 256), d_pre0=e(rows0, 256, dt=f16),
                   x0ext=e(rows0, 2 * self.K0 + 16, dt=f16), d_enc=e(rows0, self.K0),
                   d_whead=torch.zeros(256, device=device),
@@ -224,6 +248,14 @@ class FusedField:
                   err=torch.zeros(1, device=device, dtype=torch.int32))
         self.ws = ws
         return ws
+
+    @staticmethod
+    def _with_ones(t, col):
+        """Activation buffer [Ns, H + 8] whose column H is a constant 1 (written once): the
+        weight-gradient GEMM dZ^T [y | 1] then yields the next layer's bias gradient too."""
+        t[:, col:] = 0
+        t[:, col] = 1
+        return t
 
     # ------------------------------------------------------------------ step
     def step(self, batch, compute_loss=True):
@@ -271,7 +303,7 @@ class FusedField:
         fa.app_idx = _p(app_idx)
         fa.grid = lay.struct
         fa.active, fa.K0 = self.A, self.K0
-        fa.table, fa.w0e, fa.w0eT = _p(pk['table']), _p(pk['w0e']), _p(pk['w0eT'])
+        fa.table, fa.w0e, fa.w0eT, fa.w0b = _p(pk['table']), _p(pk['w0e']), _p(pk['w0eT']), _p(pk['w0b'])
         fa.w0x, fa.b0, fa.whead, fa.bhead = _p(pk['w0x']), _p(pk['b0']), _p(pk['whead']), _p(pk['bhead'])
         fa.beta = float(m.cfg.sdf.mlp.activ_params.beta)
         fa.eps = eps
@@ -293,7 +325,7 @@ class FusedField:
             _dense(X, pk['wc'][i], Hc, K, ws['ys'][i], bias=pk['bc'][i], epi=EPI_RELU, err=ws['err'])
             X, K = ws['ys'][i], Hc
         ylast = ws['ys'][-1]
-        _lib.call("gbsdf_rgb_head_fwd", Ns, c_vp(ylast.data_ptr()), Hc, Hc, c_vp(pk['wl'].data_ptr()),
+        _lib.call("gbsdf_rgb_head_fwd", Ns, c_vp(ylast.data_ptr()), ylast.stride(0), Hc, c_vp(pk['wl'].data_ptr()),
                   c_vp(pk['bl'].data_ptr()), c_vp(ws['rgbs'].data_ptr()), stream)
         # ---------------- render + losses, fwd + bwd ----------------
         lw = m.cfg.loss_weight
@@ -321,7 +353,7 @@ class FusedField:
         # ---------------- colour MLP backward ----------------
         ws['d_bl'].zero_()
         dz = ws['dzs'][0]
-        _lib.call("gbsdf_rgb_head_bwd", Ns, c_vp(ylast.data_ptr()), Hc, Hc, c_vp(pk['wl'].data_ptr()),
+        _lib.call("gbsdf_rgb_head_bwd", Ns, c_vp(ylast.data_ptr()), ylast.stride(0), Hc, c_vp(pk['wl'].data_ptr()),
                   c_vp(ws['rgbs'].data_ptr()), c_vp(ws['d_rgbs'].data_ptr()), c_vp(ws['d_pre_last'].data_ptr()),
                   c_vp(dz.data_ptr()), c_vp(_p(ws['dzs_lo'][0] if self.split else None)), c_vp(ws['d_bl'].data_ptr()),
                   stream)
@@ -335,9 +367,9 @@ class FusedField:
         cur = 0
         for i in range(n - 1, 0, -1):
             dzi = ws['dzs'][cur]
-            gw = torch.empty(Hc, Hc, **dev32)
-            _wgrad(dzi, ws['ys'][i - 1], Hc, Hc, gw)
-            grads[f'wc{i}'], grads[f'bc{i}'] = gw, torch.sum(dzi, 0, dtype=torch.float32)
+            gw = torch.empty(Hc, Hc + 8, **dev32)
+            _wgrad(dzi, ws['ys'][i - 1], Hc, Hc + 8, gw)          # column Hc: the bias gradient
+            grads[f'wc{i}'], grads[f'bc{i}'] = gw[:, :Hc], gw[:, Hc]
             nxt = ws['dzs'][1 - cur]
             _dense(dzi, pk['wcT'][i], Hc, Hc, nxt, epi=EPI_DRELU, G=ws['ys'][i - 1], err=ws['err'],
                    X_lo=ws['dzs_lo'][cur] if self.split else None,
@@ -346,8 +378,8 @@ class FusedField:
         dz0 = ws['dzs'][cur]
         dz0_lo = ws['dzs_lo'][cur] if self.split else None
         gw0 = torch.empty(Hc, self.Kc0, **dev32)
-        _wgrad(dz0, ws['xc'], Hc, self.Kc0, gw0)
-        grads['wc0'], grads['bc0'] = gw0, torch.sum(dz0, 0, dtype=torch.float32)
+        _wgrad(dz0, ws['xc'], Hc, self.Kc0, gw0)               # last column: the bias gradient
+        grads['wc0'], grads['bc0'] = gw0, gw0[:, self.Kc0 - 1]
         # input gradient of colour layer 0: feature part through softplus', tail (x, SH, n, app) as is
         _dense(dz0, pk['wc0T_feat'], 256, Hc, ws['dzfeat'], epi=EPI_DSOFTPLUS, beta=fa.beta, G=ws['xc'],
                err=ws['err'], X_lo=dz0_lo, out_lo=ws['dzfeat_lo'] if self.split else None)
@@ -379,16 +411,25 @@ class FusedField:
         grads['w0ext'] = gw0x
         grads['table'] = d_table
         self._scatter_grads(grads)
-        out = {}
-        if compute_loss:
-            sums = ws['loss_sums'].tolist()
-            l_render = 3.0 * sums[0] / (3.0 * R)
-            l_eik = sums[1] / n_mean
-            l_curv = sums[2] / n_mean
-            loss = lw.render * l_render + lw.eikonal * l_eik + (m.w_curv or 0.0) * l_curv
-            out = dict(loss=loss, l_render=l_render, l_eik=l_eik, l_curv=l_curv)
+        self._loss_norm = (R, n_mean, float(lw.render), float(lw.eikonal), float(m.w_curv or 0.0))
+        out = self.losses() if compute_loss else {}
         out['rgb'] = ws['rgb']
         return out
+
+    def losses(self):
+        """Loss terms of the last step (reads the FP64 device sums: synchronises)."""
+        R, n_mean, w_r, w_e, w_c = self._loss_norm
+        sums = self.ws['loss_sums'].tolist()
+        l_render = 3.0 * sums[0] / (3.0 * R)
+        l_eik = sums[1] / n_mean
+        l_curv = sums[2] / n_mean
+        loss = w_r * l_render + w_e * l_eik + w_c * l_curv
+        return dict(loss=loss, l_render=l_render, l_eik=l_eik, l_curv=l_curv)
+
+    def release(self):
+        """Drop the workspace (its memory returns to torch's caching allocator)."""
+        self.ws = None
+        self.pk = None
 
     def check_device_errors(self):
         """Non-zero when a bounded device wait timed out or a ray was too long."""
@@ -456,3 +497,50 @@ def _acc(param, grad):
         param.grad = grad
     else:
         param.grad.add_(grad)
+
+
+class CapturedStep:
+    """One training step of a FusedField -- zero the master gradients, forward,
+    backward -- captured once in a CUDA graph and replayed.
+
+    The batch is copied into static device buffers at capture time; ``replay(batch)``
+    copies a new batch of the same shapes into them (host tensors are copied from
+    pinned memory asynchronously) and launches the whole step as one graph.  The
+    gradients land in the masters' ``.grad`` tensors, which must not be replaced
+    (zero_grad(set_to_none=True) between replays would detach them from the graph).
+    """
+
+    def __init__(self, fused, batch, warmup=2):
+        self.fused = fused
+        model = fused.model
+        dev = batch['center'].device
+        self.static = {k: v.clone() for k, v in batch.items() if torch.is_tensor(v)}
+        self.static.update({k: v for k, v in batch.items() if not torch.is_tensor(v)})
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            for _ in range(warmup):
+                model.zero_grad(set_to_none=False)
+                fused.step(self.static, compute_loss=False)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        self.params = [p for p in model.parameters() if p.requires_grad]
+        for p in self.params:
+            if p.grad is None:
+                p.grad = torch.zeros_like(p)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            for p in self.params:
+                p.grad.zero_()
+            self.out = fused.step(self.static, compute_loss=False)
+
+    def replay(self, batch=None):
+        if batch is not None:
+            for k, v in batch.items():
+                if torch.is_tensor(v):
+                    self.static[k].copy_(v, non_blocking=True)
+        self.graph.replay()
+        return self.out
+
+    def losses(self):
+        return self.fused.losses()

@@ -42,6 +42,51 @@ def make_rays(R, N, seed=0, miss_frac=0.0, n_images=0, device="cpu"):
     return {k: v.to(device) for k, v in b.items()}
 
 
+def make_ragged_rays(R, seed=0, zero_frac=0.3, lo=16, hi=256, n_images=0, device="cpu"):
+    """Ragged batch after sphere culling and importance sampling: a ``zero_frac`` share of
+    the rays miss the unit sphere and keep no samples; every other ray gets a count
+    uniform in [lo, hi] of stratified samples in its [near, far].  Ray r owns the flat
+    samples [ray_offsets[r], ray_offsets[r+1]); ``sample_ray`` maps a sample to its ray."""
+    g = torch.Generator().manual_seed(seed)
+    c = torch.randn(R, 3, generator=g)
+    c = 3.0 * c / c.norm(dim=-1, keepdim=True)
+    d = -c + 0.3 * torch.randn(R, 3, generator=g)
+    miss = torch.rand(R, generator=g) < zero_frac
+    side = torch.linalg.cross(c, torch.randn(R, 3, generator=g), dim=-1)   # perpendicular: misses the sphere
+    d = torch.where(miss[:, None], side, d)
+    d = d / d.norm(dim=-1, keepdim=True)
+    near, far, outside = sphere_bounds(c, d)
+    counts = torch.randint(lo, hi + 1, (R,), generator=g)
+    counts = torch.where(outside[:, 0], torch.zeros_like(counts), counts)
+    offs = torch.zeros(R + 1, dtype=torch.int64)
+    offs[1:] = torch.cumsum(counts, 0)
+    Ns = int(offs[-1])
+    sample_ray = torch.repeat_interleave(torch.arange(R), counts)
+    k = torch.arange(Ns) - offs[:-1][sample_ray]                 # index within the ray
+    u = torch.rand(Ns, generator=g)
+    n = counts[sample_ray].float()
+    dists = (k.float() + u) / n * (far[sample_ray, 0] - near[sample_ray, 0]) + near[sample_ray, 0]
+    target = torch.rand(R, 3, generator=g)
+    app_idx = torch.randint(0, max(n_images, 1), (R,), generator=g)
+    b = dict(center=c, ray_unit=d, dists=dists, far=far, outside=outside, target=target, app_idx=app_idx,
+             ray_offsets=offs, sample_ray=sample_ray.to(torch.int32), near=near)
+    return {k_: v.to(device) for k_, v in b.items()}
+
+
+def padded(batch, S=128, seed=0):
+    """The rays of a ragged batch in the reference's dense [R, S] layout: every ray,
+    misses included, gets S stratified samples in [near, far] (model.py:232-236, 163)."""
+    near, far = batch['near'], batch['far']
+    R = near.shape[0]
+    g = torch.Generator().manual_seed(seed)
+    u = torch.rand(R, S, generator=g).to(near.device)
+    dists = (torch.arange(S, dtype=torch.float32, device=near.device)[None] + u) / S * (far - near) + near
+    keep = ('center', 'ray_unit', 'far', 'outside', 'target', 'app_idx')
+    out = {k: batch[k] for k in keep}
+    out['dists'] = dists
+    return out
+
+
 def init_field_params(model, seed=0, enc_perturb=1e-2):
     """Reference initialisation (geometric init already applied by the modules) plus a
     seeded N(0, enc_perturb) on SDF layer 0's encoding columns: geometric init zeroes

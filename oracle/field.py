@@ -23,7 +23,7 @@ def make_config(n_levels=16, n_features=8, log2_hashmap_size=22, base_resolution
                 per_level_scale=None, max_resolution=2048, active_levels=None,
                 sdf_hidden=256, rgb_hidden=256, rgb_layers=4, app_dim=0, n_images=0,
                 softplus_beta=100.0, out_bias=0.5, inside_out=False, s_var_init=3.0,
-                anneal_end=0.1, taps=6, vol_range=(-2.0, 2.0), sh_levels=3):
+                anneal_end=0.1, taps=6, vol_range=(-2.0, 2.0), sh_levels=3, f32_positions=False):
     if per_level_scale is None:
         # modules.py:39-41
         per_level_scale = float(np.exp((np.log(max_resolution) - np.log(base_resolution)) / (n_levels - 1)))
@@ -33,7 +33,7 @@ def make_config(n_levels=16, n_features=8, log2_hashmap_size=22, base_resolution
                 sdf_hidden=sdf_hidden, rgb_hidden=rgb_hidden, rgb_layers=rgb_layers, app_dim=app_dim,
                 n_images=n_images, softplus_beta=softplus_beta, out_bias=out_bias, inside_out=inside_out,
                 s_var_init=s_var_init, anneal_end=anneal_end, taps=taps, vol_range=vol_range,
-                sh_levels=sh_levels)
+                sh_levels=sh_levels, f32_positions=f32_positions)
 
 
 def eps_resolutions(cfg):
@@ -198,19 +198,28 @@ def compute_gradients(p, cfg, layout, pts, eps, sdf_centre, training=True):
     where sdf is the caller's (post-overwrite) centre value (model.py:163-166).
     """
     dt = pts.dtype
+    f32 = cfg.get('f32_positions', False)
+
+    def shifted(k, sign):
+        # the tap point x + sign * k, formed in float32 like the reference's float32
+        # tensors (modules.py:135-143) when f32_positions, else in the oracle's dtype
+        if f32:
+            return (pts.float() + sign * k.float()).to(dt)
+        return pts + sign * k
+
     if cfg['taps'] == 6:
         fs = []
         for d in range(3):
             e = torch.zeros(3, dtype=dt)
             e[d] = eps
-            fs.append((neural_sdf(p, cfg, layout, pts + e, False)[0],
-                       neural_sdf(p, cfg, layout, pts - e, False)[0]))
+            fs.append((neural_sdf(p, cfg, layout, shifted(e, 1), False)[0],
+                       neural_sdf(p, cfg, layout, shifted(e, -1), False)[0]))
         grad = torch.cat([(fp - fm) / (2 * eps) for fp, fm in fs], dim=-1)
         hess = torch.cat([(fp + fm - 2 * sdf_centre) / (eps ** 2) for fp, fm in fs], dim=-1) if training else None
         return grad, hess
     e = eps / np.sqrt(3)
     ks = [torch.tensor(k, dtype=dt) for k in ((1, -1, -1), (-1, -1, 1), (-1, 1, -1), (1, 1, 1))]
-    sd = [neural_sdf(p, cfg, layout, pts + k * e, False)[0] for k in ks]
+    sd = [neural_sdf(p, cfg, layout, shifted(k * e, 1), False)[0] for k in ks]
     grad = sum(k * s for k, s in zip(ks, sd)) / (4.0 * e)
     hess = None
     if training:
@@ -330,6 +339,8 @@ def render_step(p, cfg, layout, batch, eps, progress, w_eik, w_curv, training=Tr
     c, d, dists = batch['center'], batch['ray_unit'], batch['dists']
     R, N = dists.shape
     pts = c[:, None, :] + d[:, None, :] * dists[..., None]                # camera.py:314-320
+    if cfg.get('f32_positions', False):   # the points as the reference's float32 tensors hold them
+        pts = (c.float()[:, None, :] + d.float()[:, None, :] * dists.float()[..., None]).to(c.dtype)
     sdf, feat = neural_sdf(p, cfg, layout, pts, with_feat=True)
     outside = batch['outside']
     out_val = 1000.0 * (-1 if cfg['inside_out'] else 1)                   # model.py:33
@@ -358,3 +369,55 @@ def render_step(p, cfg, layout, batch, eps, progress, w_eik, w_curv, training=Tr
     return dict(loss=loss, l_render=l_render, l_eik=l_eik, l_curv=l_curv, rgb=rgb, rgbs=rgbs,
                 sdf=sdf[..., 0], feat=feat, grads=grads, hess=hess, alphas=alphas, weights=weights,
                 normals=normals, sdf_full=sdf)
+
+
+def render_step_ragged(p, cfg, layout, batch, eps, progress, w_eik, w_curv, mean_count=None):
+    """render_step on a ragged batch: ray r owns the flat samples [ray_offsets[r],
+    ray_offsets[r+1]) of ``dists`` [Ns] (the ray-major layout of the reference's
+    [B, R, N] tensors with per-ray N).  Each ray is rendered exactly as
+    render_rays_object + render_rays do for its own samples (model.py:124-190); a ray
+    without samples composites to 0.  The loss keeps the reference's composition
+    (trainer.py:40-52): L1 x 3 averaged over rays and channels, eikonal and curvature
+    summed over every sample and divided by ``mean_count`` (the number of samples the
+    reference's mean runs over: Ns by default, R x N for a padded batch).
+    Rays with the same count are evaluated together."""
+    offs = batch['ray_offsets']
+    counts = (offs[1:] - offs[:-1]).tolist()
+    R = len(counts)
+    Ns = int(offs[-1])
+    mean_count = Ns if mean_count is None else mean_count
+    dt = batch['center'].dtype
+    rgb_rows = [None] * R
+    eik_sum = torch.zeros((), dtype=dt)
+    curv_sum = torch.zeros((), dtype=dt)
+    sdf_flat = [None] * R
+    for n in sorted(set(counts)):
+        rays = [r for r in range(R) if counts[r] == n]
+        if n == 0:
+            for r in rays:
+                rgb_rows[r] = torch.zeros(3, dtype=dt)
+                sdf_flat[r] = torch.zeros(0, dtype=dt)
+            continue
+        idx = torch.tensor(rays)
+        d = torch.stack([batch['dists'][offs[r]:offs[r + 1]] for r in rays])
+        sub = dict(center=batch['center'][idx], ray_unit=batch['ray_unit'][idx], dists=d,
+                   far=batch['far'][idx], outside=batch['outside'][idx], target=batch['target'][idx],
+                   app_idx=batch['app_idx'][idx] if batch.get('app_idx') is not None else None)
+        out = render_step(p, cfg, layout, sub, eps, progress, w_eik, w_curv)
+        ins = (~sub['outside']).to(dt).expand(len(rays), n)
+        eik = ((out['grads'].norm(dim=-1) - 1.0) ** 2).nan_to_num(nan=0.0, posinf=0.0, neginf=0.0)
+        eik_sum = eik_sum + (eik * ins).sum()
+        if out['hess'] is not None:
+            lap = out['hess'].sum(dim=-1).abs().nan_to_num(nan=0.0, posinf=0.0, neginf=0.0)
+            curv_sum = curv_sum + (lap * ins).sum()
+        for j, r in enumerate(rays):
+            rgb_rows[r] = out['rgb'][j]
+            sdf_flat[r] = out['sdf'][j]
+    rgb = torch.stack(rgb_rows)
+    l_render = (rgb - batch['target']).abs().mean() * 3.0
+    l_eik = eik_sum / mean_count
+    l_curv = curv_sum / mean_count
+    loss = l_render + w_eik * l_eik
+    if w_curv:
+        loss = loss + w_curv * l_curv
+    return dict(loss=loss, l_render=l_render, l_eik=l_eik, l_curv=l_curv, rgb=rgb, sdf=torch.cat(sdf_flat))

@@ -60,3 +60,20 @@ def test_null_pointer_rejected_without_gpu(lib):
     st = lib.gbsdf_hashgrid_fwd(ctypes.byref(g), 4, None, 10, None, 0, None, 0, None)
     assert st == 1 and b"NULL" in lib.gbsdf_last_error()
     assert lib.gbsdf_hashgrid_fwd(ctypes.byref(g), 9, None, 10, None, 0, None, 0, None) == 1
+
+
+def test_sampler_args_layout_and_validation_without_gpu(lib):
+    from neuralangelo_gb300.sampler import SamplerArgs, check_struct_size
+    check_struct_size()
+    a = SamplerArgs()
+    a.R, a.ld, a.n_list, a.n_merge, a.n_fine = 4, 64, 64, 16, 16
+    a.center = a.ray_unit = a.dists = 16            # non-NULL placeholders: validation runs first
+    assert lib.gbsdf_sampler_round(ctypes.byref(a), None) == 1
+    assert b"row stride" in lib.gbsdf_last_error()
+    a.ld, a.n_list, a.n_merge = 600, 560, 16
+    assert lib.gbsdf_sampler_round(ctypes.byref(a), None) == 1
+    assert b"exceeds 512" in lib.gbsdf_last_error()
+    a.n_list, a.n_merge, a.n_fine = 64, 0, 16
+    a.fine_d = 16
+    assert lib.gbsdf_sampler_round(ctypes.byref(a), None) == 1
+    assert b"SDF values" in lib.gbsdf_last_error()
