@@ -44,6 +44,27 @@ def parse():
     return p.parse_args()
 
 
+# --------------------------------------------------------------------------- ncu-measured traffic
+
+def profiled_traffic(kernel):
+    """DRAM bytes per sample of a C-ABI call's kernels from the committed ncu summaries
+    (a line 'roofline-traffic <call> bytes_per_sample=<v> source=<capture>' in profiles/*.md),
+    or (None, None).  bench.py cannot run ncu itself; the figure comes from one capture of
+    the same kernels on a smaller case, scaled by the samples processed."""
+    import glob
+    import re
+    for f in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        for line in open(f):
+            m = re.match(r"\s*roofline-traffic\s+(\S+)\s+bytes_per_sample=([0-9.eE+-]+)\s+source=(.*)", line)
+            if m and m.group(1) == kernel:
+                return float(m.group(2)), os.path.basename(f) + ": " + m.group(3).strip()
+    return None, None
+
+
+# kernels of this library launched by one call of each entry point (cuBLAS excluded)
+KERNELS_PER_CALL = {"gbsdf_field_fwd": 2, "gbsdf_field_bwd": 2, "gbsdf_gemm_wgrad": 0}
+
+
 # --------------------------------------------------------------------------- extra workloads
 
 def bench_ragged(model, device, steps, warmup, rays=65536, seed=0):
@@ -363,13 +384,17 @@ def main():
         if name in work:
             by, fl = work[name]
             ach = by / (per_launch_ms * 1e-3) / 1e9
+            tps, tsrc = profiled_traffic(name)
+            traffic = round(tps * n_samples) if tps is not None else None
             roof = dict(kernel=name, bound="hbm", achieved=round(ach, 1), peak=hbm_peak, unit="GB/s",
-                        frac=round(ach / hbm_peak, 4), traffic=None, per_launch_ms=round(per_launch_ms, 4),
+                        frac=round(ach / hbm_peak, 4), traffic=traffic, traffic_source=tsrc,
+                        dram_gbs=round(traffic / (per_launch_ms * 1e-3) / 1e9, 1) if traffic else None,
+                        per_launch_ms=round(per_launch_ms, 4),
                         algorithmic_bytes_per_launch=by, flops_per_launch=fl,
                         tensor_tflops=round(fl / (per_launch_ms * 1e-3) / 1e12, 2),
                         launches_per_step=calls / args.steps,
                         peak_source="MEASURED_PEAKS.json hbm_gbs (burst, of measured)")
-    launches = int(sum(c for c, _ in ksum.values()) / args.steps)
+    launches = int(sum(c * KERNELS_PER_CALL.get(k, 1) for k, (c, _) in ksum.items()) / args.steps)
     extras = {}
     if not args.no_extras and fused is not None:
         fused.release()
