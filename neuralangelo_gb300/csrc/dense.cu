@@ -8,6 +8,9 @@
 // These are the colour-MLP layers of NeuralRGB (projects/neuralangelo/utils/
 // modules.py:199-220 via projects/nerf/utils/nerf_util.py:158-196) and the SDF
 // feature layer (utils/mlp.py:55-69), forward and input-gradient.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "dense.cuh"
 
 namespace gbsdf {
@@ -39,153 +42,215 @@ struct DenseParams {
     int epi;
     float beta;
     int* err;
+    int nslots;          // A-chunk slots of the shared-memory ring
 };
 
-// 16 warps: four per TMEM lane quadrant, each reading a quarter of the tile's
-// columns, so enough warps are in flight to hide the tcgen05.ld and MUFU latency
-// of the epilogue.  The epilogue kind is a template parameter.
-constexpr int DENSE_WARPS = 16;
-constexpr int DENSE_TPB = DENSE_WARPS * 32;
+// Warp-specialised pipeline (one persistent CTA per SM):
+//   warp 16 (producer)  one lane streams the A tiles in 64-column K chunks into a ring
+//                       of shared-memory slots, one TMA box per chunk (128-byte swizzle,
+//                       rows past M zero-filled), completing on full[slot]'s byte count;
+//   warp 17 (MMA)       one lane issues the tcgen05.mma of each chunk into one of two
+//                       TMEM accumulators, frees the slot with tcgen05.commit ->
+//                       empty[slot] and signals a finished tile on tfull[buf];
+//   warps 0-15          the epilogue: four warps per TMEM lane quadrant, each reading a
+//                       quarter of the columns of the finished accumulator, then
+//                       tempty[buf] so the MMA warp can reuse it.
+// The weight slice [N_TILE x K] stays resident.  Tile t+1's MMAs run while tile t's
+// epilogue drains the other accumulator, and the loads run ahead of both.  With a
+// low operand half (Xlo) its chunks come first: small addends keep their bits in
+// the FP32 accumulator.  Every wait is bounded; a timed-out wait sets *err and the
+// roles leave their loops.
+constexpr int DENSE_EPI_WARPS = 16;
+constexpr int DENSE_TPB = (DENSE_EPI_WARPS + 2) * 32;
+constexpr int KCH = 64;                                   // A columns per chunk
+constexpr int CHUNK_BYTES = TILE_M * KCH * 2;             // 16 KB
+constexpr int MAX_SLOTS = 6;
+constexpr int MIN_SLOTS = 3;
 
 template <int N_TILE, int EPI>
-__global__ void __launch_bounds__(DENSE_TPB, 1) k_dense(DenseParams p) {
+__global__ void __launch_bounds__(DENSE_TPB, 1) k_dense(const __grid_constant__ CUtensorMap tm_x,
+                                                        const __grid_constant__ CUtensorMap tm_xlo, DenseParams p) {
     extern __shared__ __align__(1024) uint8_t smem[];
+    const int K = p.K, nslots = p.nslots;
     uint8_t* w_s = smem;                                              // [N_TILE x K]
-    uint8_t* a_s = w_s + (size_t)N_TILE * p.K * 2;                    // [128 x K]
-    uint8_t* a2_s = a_s + (size_t)TILE_M * p.K * 2;                   // [128 x K] low half, when Xlo
-    float* bias_s = reinterpret_cast<float*>(a2_s + (p.Xlo ? (size_t)TILE_M * p.K * 2 : 0));
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(bias_s + N_TILE);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+    uint8_t* ring = w_s + (size_t)N_TILE * K * 2;                     // nslots x [128 x 64]
+    float* bias_s = reinterpret_cast<float*>(ring + (size_t)nslots * CHUNK_BYTES);
+    uint64_t* full = reinterpret_cast<uint64_t*>(bias_s + N_TILE);   // [MAX_SLOTS]
+    uint64_t* empty = full + MAX_SLOTS;                               // [MAX_SLOTS]
+    uint64_t* tfull = empty + MAX_SLOTS;                              // [2]
+    uint64_t* tempty = tfull + 2;                                     // [2]
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(tempty + 2);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ns = blockIdx.x % p.n_split;
     const int group = blockIdx.x / p.n_split, ngroups = gridDim.x / p.n_split;
     const int n0 = ns * N_TILE;
 
-    // resident weight slice and bias
-    stage_rows_kmajor(w_s, p.W, n0, p.N_total, p.K, p.K, tid, DENSE_TPB, N_TILE);
+    // resident weight slice and bias (all threads)
+    stage_rows_kmajor(w_s, p.W, n0, p.N_total, K, K, tid, DENSE_TPB, N_TILE);
     for (int i = tid; i < N_TILE; i += DENSE_TPB) bias_s[i] = p.bias ? p.bias[n0 + i] : 0.0f;
     if (tid == 0) {
-        umma::mbar_init(mbar, 1);
+        for (int i = 0; i < nslots; ++i) {
+            umma::mbar_init(&full[i], 1);
+            umma::mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            umma::mbar_init(&tfull[i], 1);
+            umma::mbar_init(&tempty[i], DENSE_EPI_WARPS);
+        }
         umma::fence_mbar_init();
     }
     if (warp == 0) {
-        umma::tmem_alloc(tslot, N_TILE);
+        umma::tmem_alloc(tslot, 2 * N_TILE);
         umma::tmem_relinquish();
     }
     cp_async_wait_all();
+    umma::fence_proxy_async_smem();
     __syncthreads();
     umma::fence_after_sync();
     const uint32_t tmem = *tslot;
-    const uint32_t idesc = umma::idesc_f16(TILE_M, N_TILE);
-    const uint32_t a_addr = umma::smem_u32(a_s), w_addr = umma::smem_u32(w_s), a2_addr = umma::smem_u32(a2_s);
     const int64_t ntiles = (p.M + TILE_M - 1) / TILE_M;
-    uint32_t phase = 0;
-    bool ok = true;
+    const int nk = (K + KCH - 1) / KCH;                 // chunks per operand half
+    const int nchunks = p.Xlo ? 2 * nk : nk;
 
-    const float inv_beta = 1.0f / p.beta;
-    const int q = warp & 3;                 // TMEM lane quadrant of this warp
-    const int part = warp >> 2;             // which quarter of the columns this warp reads
-    const int row = q * 32 + lane;
-    constexpr int COLS_PER_WARP = N_TILE / 4;
-    constexpr int CHUNK = COLS_PER_WARP < 32 ? COLS_PER_WARP : 32;
-
-    // Software pipeline: the A tile of tile t+1 is loaded (cp.async) while the
-    // epilogue of tile t reads TMEM; A's shared memory is free as soon as tile t's
-    // MMAs have completed.
-    auto stage = [&](int64_t t) {
-        stage_rows_kmajor(a_s, p.X, t * TILE_M, p.M, p.ldx, p.K, tid, DENSE_TPB);
-        if (p.Xlo) stage_rows_kmajor(a2_s, p.Xlo, t * TILE_M, p.M, p.ldx, p.K, tid, DENSE_TPB);
-    };
-    auto issue = [&]() {
-        if (tid == 0) {
-            umma::fence_after_sync();
-            // the low half first: small addends keep their bits in the FP32 accumulator
-            if (p.Xlo) issue_tile_mma(tmem, a2_addr, w_addr, p.K, idesc);
-            issue_tile_mma(tmem, a_addr, w_addr, p.K, idesc, p.Xlo != nullptr);
-            umma::mma_commit(mbar);
-        }
-    };
-    int64_t t = group;
-    if (t < ntiles) {
-        stage(t);
-        cp_async_wait_all();
-        umma::fence_proxy_async_smem();
-    }
-    __syncthreads();
-    if (t < ntiles) issue();
-    for (; t < ntiles; t += ngroups) {
-        const int64_t m0 = t * TILE_M;
-        ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
-        phase ^= 1u;
-        if (!ok) {
-            flag_timeout(p.err, 1);
-            break;
-        }
-        umma::fence_after_sync();
-        const int64_t tn = t + ngroups;
-        if (tn < ntiles) stage(tn);                 // overlaps the epilogue below
-        const int64_t grow = m0 + row;
-        const bool live = grow < p.M;
-#pragma unroll 1
-        for (int c0 = part * COLS_PER_WARP; c0 < (part + 1) * COLS_PER_WARP; c0 += CHUNK) {
-            float v[CHUNK];
-            if constexpr (CHUNK == 32) umma::tmem_ld32(umma::taddr(tmem, q * 32, c0), v);
-            else umma::tmem_ld16(umma::taddr(tmem, q * 32, c0), v);
-            if (live) {
-                if constexpr (EPI == EPI_DRELU || EPI == EPI_DSOFTPLUS) {
-                    const __half* gp = p.G + grow * (int64_t)p.ldg + n0 + c0;
-#pragma unroll
-                    for (int j = 0; j < CHUNK; j += 8) {
-                        float g[8];
-                        load_half8(gp + j, g);
-#pragma unroll
-                        for (int i = 0; i < 8; ++i) {
-                            if constexpr (EPI == EPI_DRELU) v[j + i] = g[i] > 0.0f ? v[j + i] : 0.0f;
-                            else v[j + i] *= 1.0f - __expf(-p.beta * g[i]);
-                        }
+    if (warp == DENSE_EPI_WARPS) {
+        // ---------------- producer: one TMA box (64 columns x 128 rows, 128-byte swizzle) per chunk ----------------
+        if (lane == 0) {
+            uint32_t n = 0;
+            bool ok = true;
+            for (int64_t t = group; t < ntiles && ok; t += ngroups) {
+                for (int c = 0; c < nchunks; ++c, ++n) {
+                    const uint32_t slot = n % (uint32_t)nslots, use = n / (uint32_t)nslots;
+                    if (use > 0 && !umma::mbar_wait(&empty[slot], (use - 1) & 1u)) {
+                        ok = false;
+                        break;
                     }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < CHUNK; ++j) {
-                        const float z = v[j] + bias_s[c0 + j];
-                        if constexpr (EPI == EPI_RELU) v[j] = fmaxf(z, 0.0f);
-                        else if constexpr (EPI == EPI_SOFTPLUS) v[j] = softplus_fast_h(z, p.beta, inv_beta);
-                        else v[j] = z;
-                    }
+                    const bool lo = p.Xlo && c < nk;
+                    const int kidx = p.Xlo ? (lo ? c : c - nk) : c;
+                    umma::mbar_arrive_expect_tx(&full[slot], CHUNK_BYTES);
+                    umma::tma_load_2d(ring + (size_t)slot * CHUNK_BYTES, lo ? (const void*)&tm_xlo : (const void*)&tm_x,
+                                      kidx * KCH, (int)(t * TILE_M), &full[slot]);
                 }
-                if (p.y_f32) {
-                    float* yp = reinterpret_cast<float*>(p.Y) + grow * (int64_t)p.ldy + n0 + c0;
-#pragma unroll
-                    for (int j = 0; j < CHUNK; j += 4) *reinterpret_cast<float4*>(yp + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
-                } else {
-                    __half* yp = reinterpret_cast<__half*>(p.Y) + grow * (int64_t)p.ldy + n0 + c0;
-#pragma unroll
-                    for (int j = 0; j < CHUNK; j += 8) store_half8(yp + j, v + j);
-                    if (p.Ylo) {
-                        __half* lp = reinterpret_cast<__half*>(p.Ylo) + grow * (int64_t)p.ldy + n0 + c0;
+            }
+            if (!ok) flag_timeout(p.err, 1);
+        }
+        __syncwarp();
+    } else if (warp == DENSE_EPI_WARPS + 1) {
+        // ---------------- MMA issue ----------------
+        if (lane == 0) {
+            const uint32_t idesc = umma::idesc_f16(TILE_M, N_TILE);
+            const uint32_t w_addr = umma::smem_u32(w_s), r_addr = umma::smem_u32(ring);
+            uint32_t n = 0;
+            bool ok = true;
+            int i = 0;
+            for (int64_t t = group; t < ntiles && ok; t += ngroups, ++i) {
+                const int buf = i & 1;
+                const uint32_t ub = (uint32_t)(i >> 1);
+                if (ub > 0 && !umma::mbar_wait(&tempty[buf], (ub - 1) & 1u)) {
+                    ok = false;
+                    break;
+                }
+                umma::fence_after_sync();
+                const uint32_t d_tmem = tmem + (uint32_t)(buf * N_TILE);
+                for (int c = 0; c < nchunks; ++c, ++n) {
+                    const uint32_t slot = n % (uint32_t)nslots, use = n / (uint32_t)nslots;
+                    if (!umma::mbar_wait(&full[slot], use & 1u)) {
+                        ok = false;
+                        break;
+                    }
+                    umma::fence_after_sync();
+                    const int kidx = p.Xlo ? (c < nk ? c : c - nk) : c;
+                    const int col0 = kidx * KCH, kc = min(KCH, K - col0);
+                    for (int j = 0; j < kc / 16; ++j) {
+                        const uint64_t ad = umma::make_desc_sw128(r_addr + slot * CHUNK_BYTES + j * 32u);
+                        const uint64_t bd = umma::make_desc(w_addr + (uint32_t)(col0 / 16 + j) * 256u, 128u,
+                                                            (uint32_t)K * 16u);
+                        umma::mma_f16(d_tmem, ad, bd, idesc, (c > 0 || j > 0) ? 1u : 0u);
+                    }
+                    umma::mma_commit(&empty[slot]);
+                }
+                if (!ok) break;
+                umma::mma_commit(&tfull[buf]);
+            }
+            if (!ok) flag_timeout(p.err, 1);
+        }
+        __syncwarp();
+    } else {
+        // ---------------- epilogue ----------------
+        const float inv_beta = 1.0f / p.beta;
+        const int q = warp & 3;                 // TMEM lane quadrant of this warp
+        const int part = warp >> 2;             // which quarter of the columns this warp reads
+        const int row = q * 32 + lane;
+        constexpr int COLS_PER_WARP = N_TILE / 4;
+        constexpr int CHUNK = COLS_PER_WARP < 32 ? COLS_PER_WARP : 32;
+        int i = 0;
+        for (int64_t t = group; t < ntiles; t += ngroups, ++i) {
+            const int buf = i & 1;
+            if (!umma::mbar_wait(&tfull[buf], (uint32_t)(i >> 1) & 1u)) {
+                if (lane == 0) flag_timeout(p.err, 1);
+                break;
+            }
+            umma::fence_after_sync();
+            const int64_t grow = t * TILE_M + row;
+            const bool live = grow < p.M;
+            const uint32_t tcol = (uint32_t)(buf * N_TILE);
+#pragma unroll 1
+            for (int c0 = part * COLS_PER_WARP; c0 < (part + 1) * COLS_PER_WARP; c0 += CHUNK) {
+                float v[CHUNK];
+                if constexpr (CHUNK == 32) umma::tmem_ld32(umma::taddr(tmem, q * 32, tcol + c0), v);
+                else umma::tmem_ld16(umma::taddr(tmem, q * 32, tcol + c0), v);
+                if (live) {
+                    if constexpr (EPI == EPI_DRELU || EPI == EPI_DSOFTPLUS) {
+                        const __half* gp = p.G + grow * (int64_t)p.ldg + n0 + c0;
 #pragma unroll
                         for (int j = 0; j < CHUNK; j += 8) {
-                            float lo[8];
+                            float g[8];
+                            load_half8(gp + j, g);
 #pragma unroll
-                            for (int i = 0; i < 8; ++i) lo[i] = v[j + i] - __half2float(__float2half_rn(v[j + i]));
-                            store_half8(lp + j, lo);
+                            for (int k = 0; k < 8; ++k) {
+                                if constexpr (EPI == EPI_DRELU) v[j + k] = g[k] > 0.0f ? v[j + k] : 0.0f;
+                                else v[j + k] *= 1.0f - __expf(-p.beta * g[k]);
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < CHUNK; ++j) {
+                            const float z = v[j] + bias_s[c0 + j];
+                            if constexpr (EPI == EPI_RELU) v[j] = fmaxf(z, 0.0f);
+                            else if constexpr (EPI == EPI_SOFTPLUS) v[j] = softplus_fast_h(z, p.beta, inv_beta);
+                            else v[j] = z;
+                        }
+                    }
+                    if (p.y_f32) {
+                        float* yp = reinterpret_cast<float*>(p.Y) + grow * (int64_t)p.ldy + n0 + c0;
+#pragma unroll
+                        for (int j = 0; j < CHUNK; j += 4)
+                            *reinterpret_cast<float4*>(yp + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                    } else {
+                        __half* yp = reinterpret_cast<__half*>(p.Y) + grow * (int64_t)p.ldy + n0 + c0;
+#pragma unroll
+                        for (int j = 0; j < CHUNK; j += 8) store_half8(yp + j, v + j);
+                        if (p.Ylo) {
+                            __half* lp = reinterpret_cast<__half*>(p.Ylo) + grow * (int64_t)p.ldy + n0 + c0;
+#pragma unroll
+                            for (int j = 0; j < CHUNK; j += 8) {
+                                float lo[8];
+#pragma unroll
+                                for (int k = 0; k < 8; ++k) lo[k] = v[j + k] - __half2float(__float2half_rn(v[j + k]));
+                                store_half8(lp + j, lo);
+                            }
                         }
                     }
                 }
             }
+            umma::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) umma::mbar_arrive(&tempty[buf]);
         }
-        umma::fence_before_sync();
-        if (tn < ntiles) {
-            cp_async_wait_all();
-            umma::fence_proxy_async_smem();
-        }
-        __syncthreads();
-        if (tn < ntiles) issue();
     }
-    umma::fence_before_sync();
     __syncthreads();
-    if (warp == 0) umma::tmem_dealloc(tmem, N_TILE);
+    umma::fence_after_sync();
+    if (warp == 0) umma::tmem_dealloc(tmem, 2 * N_TILE);
 }
 
 static int sm_count() {
@@ -199,14 +264,62 @@ static int sm_count() {
     return n;
 }
 
-static size_t dense_smem(int n_tile, int K, bool split) {
-    return (size_t)n_tile * K * 2 + (split ? 2 : 1) * (size_t)TILE_M * K * 2 + n_tile * 4 + 16;
+constexpr size_t DENSE_SMEM_MAX = 227 * 1024;
+
+// shared memory of a launch with `slots` ring slots
+static size_t dense_smem_slots(int n_tile, int K, int slots) {
+    return (size_t)n_tile * K * 2 + (size_t)slots * CHUNK_BYTES + n_tile * 4 + (2 * MAX_SLOTS + 4) * 8 + 16;
+}
+static size_t dense_smem(int n_tile, int K, bool) { return dense_smem_slots(n_tile, K, MIN_SLOTS); }
+static int dense_slots(int n_tile, int K) {
+    int s = MAX_SLOTS;
+    while (s > MIN_SLOTS && dense_smem_slots(n_tile, K, s) > DENSE_SMEM_MAX) --s;
+    return s;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link)
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }
+    return fn;
+}
+
+// TMA map of an fp16 matrix [rows x cols] with row stride ld elements: boxes of
+// 64 columns x 128 rows, 128-byte swizzle, out-of-range elements read as zero
+static int a_tensor_map(CUtensorMap* map, const void* base, int64_t rows, int cols, int ld) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) {
+        set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return GBSDF_ERR_CUDA;
+    }
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {KCH, TILE_M};
+    const cuuint32_t es[2] = {1, 1};
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return GBSDF_ERR_CUDA;
+    }
+    return GBSDF_OK;
 }
 
 template <int N_TILE, int EPI>
-static int launch_dense(const DenseParams& p, cudaStream_t s) {
-    const size_t smem = dense_smem(N_TILE, p.K, p.Xlo != nullptr);
-    if (smem > 227 * 1024) {
+static int launch_dense(DenseParams p, cudaStream_t s) {
+    p.nslots = dense_slots(N_TILE, p.K);
+    const size_t smem = dense_smem_slots(N_TILE, p.K, p.nslots);
+    if (smem > DENSE_SMEM_MAX) {
         set_error("dense layer K=%d N_TILE=%d needs %zu B of shared memory", p.K, N_TILE, smem);
         return GBSDF_ERR_UNSUPPORTED;
     }
@@ -215,7 +328,10 @@ static int launch_dense(const DenseParams& p, cudaStream_t s) {
     int64_t groups = sm_count() / p.n_split;
     if (groups < 1) groups = 1;
     if (groups > ntiles) groups = ntiles;
-    k_dense<N_TILE, EPI><<<(unsigned)(groups * p.n_split), DENSE_TPB, smem, s>>>(p);
+    CUtensorMap tm_x, tm_xlo;
+    if (int st = a_tensor_map(&tm_x, p.X, p.M, p.K, p.ldx)) return st;
+    if (int st = a_tensor_map(&tm_xlo, p.Xlo ? p.Xlo : p.X, p.M, p.K, p.ldx)) return st;
+    k_dense<N_TILE, EPI><<<(unsigned)(groups * p.n_split), DENSE_TPB, smem, s>>>(tm_x, tm_xlo, p);
     return launch_status("dense");
 }
 
@@ -269,7 +385,7 @@ extern "C" int gbsdf_dense(int64_t M, int K, int N, const void* X, const void* X
     p.beta = beta; p.err = err;
     // largest N tile whose weight slice + A tile fit in shared memory
     int n_tile = 256;
-    while (n_tile > 64 && (dense_smem(n_tile, K, Xlo != nullptr) + 2048 > 227 * 1024 || N % n_tile != 0))
+    while (n_tile > 64 && (dense_smem(n_tile, K, Xlo != nullptr) > DENSE_SMEM_MAX || N % n_tile != 0))
         n_tile >>= 1;
     p.n_split = N / n_tile;
     return dense_launch(p, n_tile, as_stream(stream));

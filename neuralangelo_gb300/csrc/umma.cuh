@@ -36,6 +36,20 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint
     return d;
 }
 
+// The same for a K-major operand written by TMA with 128-byte swizzle: rows of 64
+// fp16 (128 B), 8-row atoms of 1024 B (SBO), LBO unused (encoded 1), layout type 2
+// (SWIZZLE_128B) in bits 61-63.  The atom base must be 1024-byte aligned; the K = 16
+// steps inside a row advance the start address by 32 B.
+__device__ __forceinline__ uint64_t make_desc_sw128(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(1024u >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
 // Instruction descriptor for kind::f16: D = f32 (bits 4-5 = 1), A = B = f16
 // (bits 7-9 = 0, 10-12 = 0), both K-major (bits 15, 16 = 0), N >> 3 in bits
 // 17-22, M >> 4 in bits 24-28.
@@ -104,6 +118,26 @@ __device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
 }
 __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// arrive on an mbarrier and add `bytes` to the transaction count its phase waits for
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+}
+// 2D TMA tile load global -> shared, completing on an mbarrier's transaction count.
+// x (innermost, elements) must be a multiple of 16 bytes; y may run past the tensor
+// (those rows are zero-filled).
+__device__ __forceinline__ void tma_load_2d(void* smem_dst, const void* tmap, int x, int y, uint64_t* mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(smem_u32(smem_dst)),
+        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(smem_u32(mbar))
+        : "memory");
+}
+
+// arrive (release, CTA scope) on an mbarrier
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
 }
 __device__ __forceinline__ uint32_t mbar_try_wait(uint64_t* mbar, uint32_t parity) {
     uint32_t ok;
