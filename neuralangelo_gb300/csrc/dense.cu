@@ -43,6 +43,7 @@ struct DenseParams {
     float beta;
     int* err;
     int nslots;          // A-chunk slots of the shared-memory ring
+    int tma_store;       // fp16 output written back through shared memory and TMA
 };
 
 // Warp-specialised pipeline (one persistent CTA per SM):
@@ -66,15 +67,18 @@ constexpr int KCH = 64;                                   // A columns per chunk
 constexpr int CHUNK_BYTES = TILE_M * KCH * 2;             // 16 KB
 constexpr int MAX_SLOTS = 6;
 constexpr int MIN_SLOTS = 3;
+constexpr int STAGE_BYTES = DENSE_EPI_WARPS * 32 * 32 * 2;  // per-warp output staging of the TMA store
 
 template <int N_TILE, int EPI>
 __global__ void __launch_bounds__(DENSE_TPB, 1) k_dense(const __grid_constant__ CUtensorMap tm_x,
-                                                        const __grid_constant__ CUtensorMap tm_xlo, DenseParams p) {
+                                                        const __grid_constant__ CUtensorMap tm_xlo,
+                                                        const __grid_constant__ CUtensorMap tm_y, DenseParams p) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int K = p.K, nslots = p.nslots;
     uint8_t* w_s = smem;                                              // [N_TILE x K]
     uint8_t* ring = w_s + (size_t)N_TILE * K * 2;                     // nslots x [128 x 64]
-    float* bias_s = reinterpret_cast<float*>(ring + (size_t)nslots * CHUNK_BYTES);
+    uint8_t* stage_s = ring + (size_t)nslots * CHUNK_BYTES;              // 16 x [32 x 32] fp16, when tma_store
+    float* bias_s = reinterpret_cast<float*>(stage_s + (p.tma_store ? STAGE_BYTES : 0));
     uint64_t* full = reinterpret_cast<uint64_t*>(bias_s + N_TILE);   // [MAX_SLOTS]
     uint64_t* empty = full + MAX_SLOTS;                               // [MAX_SLOTS]
     uint64_t* tfull = empty + MAX_SLOTS;                              // [2]
@@ -221,7 +225,9 @@ __global__ void __launch_bounds__(DENSE_TPB, 1) k_dense(const __grid_constant__ 
                             else v[j] = z;
                         }
                     }
-                    if (p.y_f32) {
+                    if (p.tma_store) {
+                        // handled below, for the whole warp
+                    } else if (p.y_f32) {
                         float* yp = reinterpret_cast<float*>(p.Y) + grow * (int64_t)p.ldy + n0 + c0;
 #pragma unroll
                         for (int j = 0; j < CHUNK; j += 4)
@@ -242,12 +248,37 @@ __global__ void __launch_bounds__(DENSE_TPB, 1) k_dense(const __grid_constant__ 
                         }
                     }
                 }
+                if constexpr (CHUNK == 32) {
+                    if (p.tma_store) {
+                        // coalesced write-back: the warp's 32 x 32 block goes through shared memory
+                        // (64-byte swizzle: 16-byte chunk j of row r at chunk j ^ ((r >> 1) & 3))
+                        // and leaves as one TMA store; rows past M are clipped by the TMA unit
+                        uint8_t* stg = stage_s + warp * (32 * 32 * 2);
+                        if (lane == 0) umma::bulk_wait_read0();      // the previous store has read it
+                        __syncwarp();
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            __half2 h[4];
+#pragma unroll
+                            for (int k = 0; k < 4; ++k) h[k] = __floats2half2_rn(v[8 * j + 2 * k], v[8 * j + 2 * k + 1]);
+                            *reinterpret_cast<uint4*>(stg + lane * 64 + ((j ^ ((lane >> 1) & 3)) * 16)) =
+                                *reinterpret_cast<const uint4*>(h);
+                        }
+                        umma::fence_proxy_async_smem();
+                        __syncwarp();
+                        if (lane == 0) {
+                            umma::tma_store_2d(&tm_y, n0 + c0, (int)(t * TILE_M) + q * 32, stg);
+                            umma::bulk_commit();
+                        }
+                    }
+                }
             }
             umma::fence_before_sync();
             __syncwarp();
             if (lane == 0) umma::mbar_arrive(&tempty[buf]);
         }
     }
+    if (p.tma_store && warp < DENSE_EPI_WARPS && lane == 0) umma::bulk_wait0();
     __syncthreads();
     umma::fence_after_sync();
     if (warp == 0) umma::tmem_dealloc(tmem, 2 * N_TILE);
@@ -266,14 +297,15 @@ static int sm_count() {
 
 constexpr size_t DENSE_SMEM_MAX = 227 * 1024;
 
-// shared memory of a launch with `slots` ring slots
-static size_t dense_smem_slots(int n_tile, int K, int slots) {
-    return (size_t)n_tile * K * 2 + (size_t)slots * CHUNK_BYTES + n_tile * 4 + (2 * MAX_SLOTS + 4) * 8 + 16;
+// shared memory of a launch with `slots` ring slots (and the output staging when `stage`)
+static size_t dense_smem_slots(int n_tile, int K, int slots, bool stage) {
+    return (size_t)n_tile * K * 2 + (size_t)slots * CHUNK_BYTES + (stage ? STAGE_BYTES : 0) + n_tile * 4 +
+           (2 * MAX_SLOTS + 4) * 8 + 16;
 }
-static size_t dense_smem(int n_tile, int K, bool) { return dense_smem_slots(n_tile, K, MIN_SLOTS); }
-static int dense_slots(int n_tile, int K) {
+static size_t dense_smem(int n_tile, int K, bool stage) { return dense_smem_slots(n_tile, K, MIN_SLOTS, stage); }
+static int dense_slots(int n_tile, int K, bool stage) {
     int s = MAX_SLOTS;
-    while (s > MIN_SLOTS && dense_smem_slots(n_tile, K, s) > DENSE_SMEM_MAX) --s;
+    while (s > MIN_SLOTS && dense_smem_slots(n_tile, K, s, stage) > DENSE_SMEM_MAX) --s;
     return s;
 }
 
@@ -315,10 +347,35 @@ static int a_tensor_map(CUtensorMap* map, const void* base, int64_t rows, int co
     return GBSDF_OK;
 }
 
+// TMA map of the fp16 output [rows x cols] (row stride ld): boxes of 32 columns x 32 rows, 64-byte swizzle
+static int y_tensor_map(CUtensorMap* map, void* base, int64_t rows, int cols, int ld) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) {
+        set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return GBSDF_ERR_CUDA;
+    }
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {32, 32};
+    const cuuint32_t es[2] = {1, 1};
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, base, dims, strides, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled (output) failed (%d)", (int)r);
+        return GBSDF_ERR_CUDA;
+    }
+    return GBSDF_OK;
+}
+
 template <int N_TILE, int EPI>
 static int launch_dense(DenseParams p, cudaStream_t s) {
-    p.nslots = dense_slots(N_TILE, p.K);
-    const size_t smem = dense_smem_slots(N_TILE, p.K, p.nslots);
+    // the TMA write-back needs 32-column chunks, an fp16 output without a low half, and the
+    // staging buffers next to at least MIN_SLOTS ring slots
+    p.tma_store = (N_TILE / 4 >= 32 && !p.y_f32 && !p.Ylo &&
+                   dense_smem_slots(N_TILE, p.K, MIN_SLOTS, true) <= DENSE_SMEM_MAX) ? 1 : 0;
+    p.nslots = dense_slots(N_TILE, p.K, p.tma_store != 0);
+    const size_t smem = dense_smem_slots(N_TILE, p.K, p.nslots, p.tma_store != 0);
     if (smem > DENSE_SMEM_MAX) {
         set_error("dense layer K=%d N_TILE=%d needs %zu B of shared memory", p.K, N_TILE, smem);
         return GBSDF_ERR_UNSUPPORTED;
@@ -328,10 +385,15 @@ static int launch_dense(DenseParams p, cudaStream_t s) {
     int64_t groups = sm_count() / p.n_split;
     if (groups < 1) groups = 1;
     if (groups > ntiles) groups = ntiles;
-    CUtensorMap tm_x, tm_xlo;
+    CUtensorMap tm_x, tm_xlo, tm_y;
     if (int st = a_tensor_map(&tm_x, p.X, p.M, p.K, p.ldx)) return st;
     if (int st = a_tensor_map(&tm_xlo, p.Xlo ? p.Xlo : p.X, p.M, p.K, p.ldx)) return st;
-    k_dense<N_TILE, EPI><<<(unsigned)(groups * p.n_split), DENSE_TPB, smem, s>>>(tm_x, tm_xlo, p);
+    if (p.tma_store) {
+        if (int st = y_tensor_map(&tm_y, p.Y, p.M, p.N_total, p.ldy)) return st;
+    } else {
+        tm_y = tm_x;                                       // unused
+    }
+    k_dense<N_TILE, EPI><<<(unsigned)(groups * p.n_split), DENSE_TPB, smem, s>>>(tm_x, tm_xlo, tm_y, p);
     return launch_status("dense");
 }
 

@@ -205,19 +205,19 @@ __global__ void __launch_bounds__(256) k_field_gather(FieldParams p, int64_t nti
     }
 }
 
-// Table gradient of one (sample, level, corner) over the sample's 7 evaluations,
-// merging consecutive evaluations that hit the same entry (the taps are eps
-// apart: at coarse levels all 7 usually share the corner) before the atomics.
+// Table gradient of one (sample, level) over the sample's 7 evaluations: each
+// evaluation's grid position is computed once and its 8 corners are accumulated in
+// registers, merging consecutive evaluations that hit the same entry of a corner
+// (the taps are eps apart: at coarse levels all 7 usually share the cell) before the
+// vector atomics.
 template <int F>
 __global__ void __launch_bounds__(256) k_field_scatter(FieldParams p) {
     const int A = p.active, K0 = p.K0;
-    // 32-bit index arithmetic: the launcher checks Ns * A * 8 < 2^32
+    // 32-bit index arithmetic: the launcher checks Ns * active * 8 < 2^32
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (uint32_t)p.Ns * (uint32_t)A * 8u) return;
-    const int cc = (int)(i & 7u);
-    const uint32_t sl_ = i >> 3;
-    const uint32_t s32 = sl_ / (uint32_t)A;
-    const int l = (int)(sl_ - s32 * (uint32_t)A);
+    if (i >= (uint32_t)p.Ns * (uint32_t)A) return;
+    const uint32_t s32 = i / (uint32_t)A;
+    const int l = (int)(i - s32 * (uint32_t)A);
     const int64_t s = s32;
     const int64_t t = s32 / SPT;
     const int sl = (int)(s32 - (uint32_t)t * SPT);
@@ -225,10 +225,14 @@ __global__ void __launch_bounds__(256) k_field_scatter(FieldParams p) {
     sample_point(p, s, c);
     const LevelDesc d = level_desc(p.grid, l);
     float* base = p.d_table + d.offset * F;
-    uint32_t pidx = 0xffffffffu;
-    float pacc[F];
+    uint32_t pidx[8];
+    float pacc[8][F];
 #pragma unroll
-    for (int f = 0; f < F; ++f) pacc[f] = 0.0f;
+    for (int cc = 0; cc < 8; ++cc) {
+        pidx[cc] = 0xffffffffu;
+#pragma unroll
+        for (int f = 0; f < F; ++f) pacc[cc][f] = 0.0f;
+    }
 #pragma unroll 1
     for (int e = 0; e < EVALS; ++e) {
         float x[3], xu[3];
@@ -240,14 +244,6 @@ __global__ void __launch_bounds__(256) k_field_scatter(FieldParams p) {
         grid_pos(d.scale, xu[0], bx, fx);
         grid_pos(d.scale, xu[1], by, fy);
         grid_pos(d.scale, xu[2], bz, fz);
-        const uint32_t idx = grid_index(d, bx + (cc & 1), by + ((cc >> 1) & 1), bz + ((cc >> 2) & 1));
-        const float w = corner_weight(cc, fx, fy, fz);
-        if (idx != pidx) {
-            if (pidx != 0xffffffffu) scatter_add<F>(base + (uint64_t)pidx * F, pacc);
-            pidx = idx;
-#pragma unroll
-            for (int f = 0; f < F; ++f) pacc[f] = 0.0f;
-        }
         const float* dv = p.d_enc + (t * (SPT * EVALS) + e * SPT + sl) * (int64_t)K0 + l * F;
         float g[F];
         if constexpr (F % 4 == 0) {
@@ -261,9 +257,21 @@ __global__ void __launch_bounds__(256) k_field_scatter(FieldParams p) {
             for (int f = 0; f < F; ++f) g[f] = __ldg(dv + f);
         }
 #pragma unroll
-        for (int f = 0; f < F; ++f) pacc[f] = fmaf(w, g[f], pacc[f]);
+        for (int cc = 0; cc < 8; ++cc) {
+            const uint32_t idx = grid_index(d, bx + (cc & 1), by + ((cc >> 1) & 1), bz + ((cc >> 2) & 1));
+            const float w = corner_weight(cc, fx, fy, fz);
+            if (idx != pidx[cc]) {
+                if (pidx[cc] != 0xffffffffu) scatter_add<F>(base + (uint64_t)pidx[cc] * F, pacc[cc]);
+                pidx[cc] = idx;
+#pragma unroll
+                for (int f = 0; f < F; ++f) pacc[cc][f] = 0.0f;
+            }
+#pragma unroll
+            for (int f = 0; f < F; ++f) pacc[cc][f] = fmaf(w, g[f], pacc[cc][f]);
+        }
     }
-    scatter_add<F>(base + (uint64_t)pidx * F, pacc);
+#pragma unroll
+    for (int cc = 0; cc < 8; ++cc) scatter_add<F>(base + (uint64_t)pidx[cc] * F, pacc[cc]);
 }
 
 // ---------------------------------------------------------------------------
@@ -877,7 +885,7 @@ static int launch_field(const FieldParams& p, bool backward, cudaStream_t s) {
     if (backward) {
         cudaFuncSetAttribute(k_field_bwd<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_field_bwd<F><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p);
-        const int64_t items = p.Ns * p.active * 8;
+        const int64_t items = p.Ns * p.active;
         k_field_scatter<F><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p);
     } else {
         const int64_t items = ntiles * (SPT * EVALS) * p.active;
