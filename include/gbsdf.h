@@ -151,7 +151,7 @@ int gbsdf_dense(int64_t M, int K, int N, const void* X, const void* Xlo, int ldx
 typedef struct gbsdf_field_args {
     int64_t Ns;
     int32_t S;
-    int32_t pad0;
+    int32_t ld_h0c;          /* row stride of h0c in elements (0 = 256); columns past 255 are not written */
     const int32_t* sample_ray;
     const float* center;
     const float* ray_unit;
@@ -171,7 +171,7 @@ typedef struct gbsdf_field_args {
     const float* whead;      /* [256] */
     const float* bhead;      /* [1] */
     float beta, eps, two_eps, eps2, outside_val;
-    int32_t pad1;
+    float d_table_scale;     /* factor on the table-gradient contributions (0 = 1), e.g. 1 / loss scale */
     void* xc;                /* fp16 [Ns, ldxc] colour input; columns >= 256 written by the forward:
                                 x, SH(d), normal, app, zeros, and 1 in the last column */
     int32_t ldxc;

@@ -25,8 +25,9 @@ constexpr int HID = 256;         // SDF hidden width (base.yaml:41)
 
 typedef gbsdf_field_args FieldParams;   // layout and field meanings: include/gbsdf.h
 
+// ray of sample s (32-bit division: the launchers keep the sample count below 2^32)
 __device__ __forceinline__ int ray_of(const FieldParams& p, int64_t s) {
-    return p.S > 0 ? (int)(s / p.S) : p.sample_ray[s];
+    return p.S > 0 ? (int)((uint32_t)s / (uint32_t)p.S) : p.sample_ray[s];
 }
 
 // float32 centre point c + d t (camera.py:314-320: one multiply, one add)
@@ -225,6 +226,7 @@ __global__ void __launch_bounds__(256) k_field_scatter(FieldParams p) {
     sample_point(p, s, c);
     const LevelDesc d = level_desc(p.grid, l);
     float* base = p.d_table + d.offset * F;
+    const float gscale = p.d_table_scale != 0.0f ? p.d_table_scale : 1.0f;
     uint32_t pidx[8];
     float pacc[8][F];
 #pragma unroll
@@ -256,6 +258,8 @@ __global__ void __launch_bounds__(256) k_field_scatter(FieldParams p) {
 #pragma unroll
             for (int f = 0; f < F; ++f) g[f] = __ldg(dv + f);
         }
+#pragma unroll
+        for (int f = 0; f < F; ++f) g[f] *= gscale;
 #pragma unroll
         for (int cc = 0; cc < 8; ++cc) {
             const uint32_t idx = grid_index(d, bx + (cc & 1), by + ((cc >> 1) & 1), bz + ((cc >> 2) & 1));
@@ -377,7 +381,7 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
                 part4[j & 3] = fmaf(wh_s[c0 + j], h, part4[j & 3]);
             }
             if (keep) {
-                __half* dst = (__half*)p.h0c + s * HID + c0;
+                __half* dst = (__half*)p.h0c + s * (int64_t)(p.ld_h0c > 0 ? p.ld_h0c : HID) + c0;
 #pragma unroll
                 for (int j = 0; j < 32; j += 8) store_half8(dst + j, v + j);
             }
@@ -389,27 +393,32 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
             sdf_s[tid] = part_s[tid] + part_s[TILE_M + tid] + bhead;
         }
         __syncthreads();
-        // per-sample: gradient, Hessian diagonal, outside overwrite, colour-input columns
-        if (tid < SPT) {
-            const int64_t ss = s0 + tid;
+        // per-sample: gradient, Hessian diagonal, outside overwrite, colour-input columns;
+        // six threads per sample, each storing one 8-column chunk of the colour-input tail
+        // (the first of them also the SDF, gradient and Hessian)
+        if (tid < SPT * 6) {
+            const int js = tid / 6, kc8 = tid - 6 * js;
+            const int64_t ss = s0 + js;
             if (ss < p.Ns) {
                 const int r = ray_of(p, ss);
                 const bool out = p.outside && p.outside[r];
-                const float fc = out ? p.outside_val : sdf_s[tid];
+                const float fc = out ? p.outside_val : sdf_s[js];
                 float g[3], hh[3];
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
-                    const float fp = sdf_s[(1 + 2 * d) * SPT + tid], fm = sdf_s[(2 + 2 * d) * SPT + tid];
+                    const float fp = sdf_s[(1 + 2 * d) * SPT + js], fm = sdf_s[(2 + 2 * d) * SPT + js];
                     g[d] = __fdiv_rn(__fsub_rn(fp, fm), p.two_eps);
                     hh[d] = __fdiv_rn(__fsub_rn(__fadd_rn(fp, fm), __fmul_rn(2.0f, fc)), p.eps2);
                 }
-                p.sdf[ss] = fc;
+                if (kc8 == 0) {
+                    p.sdf[ss] = fc;
 #pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    p.grad[3 * ss + d] = g[d];
-                    p.hess[3 * ss + d] = hh[d];
+                    for (int d = 0; d < 3; ++d) {
+                        p.grad[3 * ss + d] = g[d];
+                        p.hess[3 * ss + d] = hh[d];
+                    }
                 }
-                if (p.xc) {
+                if (p.xc && 8 * kc8 < p.ldxc - HID) {
                     // NeuralRGB input tail (modules.py:209-213): x, SH(d), normalize(g), app
                     float c[3];
                     sample_point(p, ss, c);
@@ -448,7 +457,8 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
                     // the last (padding) column is a constant 1: the colour layer-0 weight
                     // gradient dZ^T xc then carries the bias gradient in that column
                     col[ncol - 1] = 1.0f;
-                    for (int k = 0; k < ncol; k += 8) store_half8(dst + k, col + k);
+                    store_half8(dst + 8 * kc8, col + 8 * kc8);
+                    (void)ncol;
                 }
             }
         }
@@ -928,6 +938,7 @@ extern "C" int gbsdf_field_fwd(const gbsdf_field_args* params, void* stream) {
     if (p.Ns == 0) return GBSDF_OK;
     GBSDF_CHECK_ARG(p.sdf && p.grad && p.hess && p.h0c && p.x0ext, "NULL output");
     GBSDF_CHECK_ARG(p.w0b && aligned(p.w0b, 16), "w0b (fp16 [256, K0 + 16]) missing or misaligned");
+    GBSDF_CHECK_ARG(p.ld_h0c == 0 || (p.ld_h0c >= HID && p.ld_h0c % 8 == 0), "ld_h0c %d", p.ld_h0c);
     GBSDF_CHECK_ARG(!p.xc || (p.ldxc % 16 == 0 && p.ldxc - HID >= 23 + p.app_dim && p.ldxc - HID <= 48),
                     "xc leading dimension %d (needs 256 + 23 + app_dim <= ldxc <= 304, multiple of 16)", p.ldxc);
     GBSDF_CHECK_ARG(!p.xc || p.app_dim == 0 || (p.app_table && p.app_idx), "appearance table / index missing");

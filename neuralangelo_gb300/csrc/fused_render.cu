@@ -10,7 +10,7 @@
 //   nerf_util.py:187-196) forward and backward.
 // gbsdf_app_grad     : gradient of the per-image appearance embedding
 //   (model.py:215-230 gathers Embedding(idx) per ray).
-#include "common.cuh"
+#include "dense.cuh"
 
 namespace gbsdf {
 
@@ -197,7 +197,9 @@ __global__ void __launch_bounds__(RENDER_WARPS * 32) k_render_fused(gbsdf_render
     if (lane == 0 && ds_acc != 0.0f) atomicAdd(p.d_s_var, ds_acc);
 }
 
-// rgbs = sigmoid(Y W^T + b) for the 3 colour channels; one thread per sample; W [3, H]
+
+// rgbs = sigmoid(Y W^T + b) for the 3 colour channels; one thread per row (cheaper here than a
+// warp per row, which needs three warp reductions per row); W [3, H]
 __global__ void k_rgb_head_fwd(int64_t Ns, const __half* __restrict__ Y, int ldy, int H, const float* __restrict__ W,
                                const float* __restrict__ b, float* __restrict__ rgbs) {
     __shared__ float w_s[3 * 256];
@@ -224,52 +226,72 @@ __global__ void k_rgb_head_fwd(int64_t Ns, const __half* __restrict__ Y, int ldy
     rgbs[3 * s + 2] = sigmoidf_(a2);
 }
 
-// d_pre = d_rgb * rgb (1 - rgb);  dZ = (d_pre W) * [Y > 0]
-__global__ void k_rgb_head_bwd(int64_t Ns, const __half* __restrict__ Y, int ldy, int H, const float* __restrict__ W,
-                               const float* __restrict__ rgbs, const float* __restrict__ d_rgbs,
-                               __half* __restrict__ d_pre, __half* __restrict__ dZ, __half* __restrict__ dZlo,
-                               float* __restrict__ d_b) {
-    __shared__ float w_s[3 * 256];
-    for (int i = threadIdx.x; i < 3 * H; i += blockDim.x) w_s[(i / H) * 256 + i % H] = W[i];
-    __syncthreads();
-    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    float g0 = 0.f, g1 = 0.f, g2 = 0.f;
-    if (s < Ns) {
+// d_pre = d_rgb * rgb (1 - rgb);  dZ = (d_pre W) * [Y > 0];  d_b += d_pre.
+// One warp per row at a time: lane j owns hidden columns [8j, 8j + 8) (H <= 256)
+// and keeps its slice of W [3, H] in registers, so every row's activations and
+// gradients move as one coalesced 512-byte access.
+__global__ void __launch_bounds__(256) k_rgb_head_bwd(int64_t Ns, const __half* __restrict__ Y, int ldy, int H,
+                                                      const float* __restrict__ W, const float* __restrict__ rgbs,
+                                                      const float* __restrict__ d_rgbs, __half* __restrict__ d_pre,
+                                                      __half* __restrict__ dZ, __half* __restrict__ dZlo,
+                                                      float* __restrict__ d_b) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int c0 = lane * 8;
+    const bool act = c0 < H;
+    float wr[3][8];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int i = 0; i < 8; ++i) wr[k][i] = act ? W[k * H + c0 + i] : 0.0f;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+    for (int64_t s = w0; s < Ns; s += nw) {
         const float r0 = rgbs[3 * s], r1 = rgbs[3 * s + 1], r2 = rgbs[3 * s + 2];
-        g0 = d_rgbs[3 * s] * r0 * (1.0f - r0);
-        g1 = d_rgbs[3 * s + 1] * r1 * (1.0f - r1);
-        g2 = d_rgbs[3 * s + 2] * r2 * (1.0f - r2);
-        __half2 hp[4] = {__floats2half2_rn(g0, g1), __floats2half2_rn(g2, 0.f), __floats2half2_rn(0.f, 0.f),
-                         __floats2half2_rn(0.f, 0.f)};
-        *reinterpret_cast<uint4*>(d_pre + s * 8) = *reinterpret_cast<const uint4*>(hp);
-        const __half* y = Y + s * ldy;
-        __half* z = dZ + s * H;
-        for (int j = 0; j < H; j += 8) {
-            const uint4 u = *reinterpret_cast<const uint4*>(y + j);
+        const float g0 = d_rgbs[3 * s] * r0 * (1.0f - r0);
+        const float g1 = d_rgbs[3 * s + 1] * r1 * (1.0f - r1);
+        const float g2 = d_rgbs[3 * s + 2] * r2 * (1.0f - r2);
+        if (lane == 0) {
+            __half2 hp[4] = {__floats2half2_rn(g0, g1), __floats2half2_rn(g2, 0.f), __floats2half2_rn(0.f, 0.f),
+                             __floats2half2_rn(0.f, 0.f)};
+            *reinterpret_cast<uint4*>(d_pre + s * 8) = *reinterpret_cast<const uint4*>(hp);
+            s0 += g0;
+            s1 += g1;
+            s2 += g2;
+        }
+        if (act) {
+            const uint4 u = *reinterpret_cast<const uint4*>(Y + s * ldy + c0);
             const __half2* h = reinterpret_cast<const __half2*>(&u);
             __half2 o[4], ol[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 const float2 f = __half22float2(h[i]);
-                const int c = j + 2 * i;
-                const float v0 = f.x > 0.0f ? g0 * w_s[c] + g1 * w_s[256 + c] + g2 * w_s[512 + c] : 0.0f;
-                const float v1 = f.y > 0.0f ? g0 * w_s[c + 1] + g1 * w_s[256 + c + 1] + g2 * w_s[512 + c + 1] : 0.0f;
+                const int c = 2 * i;
+                const float v0 = f.x > 0.0f ? g0 * wr[0][c] + g1 * wr[1][c] + g2 * wr[2][c] : 0.0f;
+                const float v1 = f.y > 0.0f ? g0 * wr[0][c + 1] + g1 * wr[1][c + 1] + g2 * wr[2][c + 1] : 0.0f;
                 o[i] = __floats2half2_rn(v0, v1);
                 const float2 r = __half22float2(o[i]);
                 ol[i] = __floats2half2_rn(v0 - r.x, v1 - r.y);
             }
-            *reinterpret_cast<uint4*>(z + j) = *reinterpret_cast<const uint4*>(o);
-            if (dZlo) *reinterpret_cast<uint4*>(dZlo + s * H + j) = *reinterpret_cast<const uint4*>(ol);
+            *reinterpret_cast<uint4*>(dZ + s * H + c0) = *reinterpret_cast<const uint4*>(o);
+            if (dZlo) *reinterpret_cast<uint4*>(dZlo + s * H + c0) = *reinterpret_cast<const uint4*>(ol);
         }
     }
-    g0 = warp_sum(g0);
-    g1 = warp_sum(g1);
-    g2 = warp_sum(g2);
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(d_b, g0);
-        atomicAdd(d_b + 1, g1);
-        atomicAdd(d_b + 2, g2);
+    if (lane == 0 && (s0 != 0.f || s1 != 0.f || s2 != 0.f)) {
+        atomicAdd(d_b, s0);
+        atomicAdd(d_b + 1, s1);
+        atomicAdd(d_b + 2, s2);
     }
+}
+
+static unsigned head_blocks(int64_t Ns) {
+    // eight 256-thread blocks per SM, or fewer when there are fewer rows than warps
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t want = (int64_t)(sms > 0 ? sms : 1) * 8;
+    const int64_t need = (Ns + 7) / 8;
+    return (unsigned)(need < want ? (need > 0 ? need : 1) : want);
 }
 
 // d_app[img(r)] += sum over ray r's samples of d_xc[s, col0:col0+D]; one warp per ray
@@ -332,7 +354,7 @@ extern "C" int gbsdf_rgb_head_bwd(int64_t Ns, const void* Y, int ldy, int H, con
     GBSDF_CHECK_ARG(H % 8 == 0 && H <= 256 && H > 0, "hidden width %d", H);
     GBSDF_CHECK_ARG(ldy % 8 == 0 && ldy >= H && aligned(Y, 16) && aligned(dZ, 16) && aligned(d_pre, 16), "layout");
     GBSDF_CHECK_ARG(!dZ_lo || aligned(dZ_lo, 16), "dZ_lo alignment");
-    k_rgb_head_bwd<<<(unsigned)((Ns + 255) / 256), 256, 0, as_stream(stream)>>>(
+    k_rgb_head_bwd<<<head_blocks(Ns), 256, 0, as_stream(stream)>>>(
         Ns, (const __half*)Y, ldy, H, W, rgbs, d_rgbs, (__half*)d_pre, (__half*)dZ, (__half*)dZ_lo, d_b);
     return launch_status("rgb_head_bwd");
 }

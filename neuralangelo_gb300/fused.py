@@ -31,12 +31,12 @@ c_i32, c_i64, c_f32, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctyp
 
 
 class FieldArgs(ctypes.Structure):
-    _fields_ = [("Ns", c_i64), ("S", c_i32), ("pad0", c_i32), ("sample_ray", c_vp), ("center", c_vp),
+    _fields_ = [("Ns", c_i64), ("S", c_i32), ("ld_h0c", c_i32), ("sample_ray", c_vp), ("center", c_vp),
                 ("ray_unit", c_vp), ("dists", c_vp), ("outside", c_vp), ("app_idx", c_vp),
                 ("grid", _lib.GridStruct), ("active", c_i32), ("K0", c_i32), ("table", c_vp), ("w0e", c_vp),
                 ("w0eT", c_vp), ("w0b", c_vp), ("w0x", c_vp), ("b0", c_vp), ("whead", c_vp), ("bhead", c_vp),
                 ("beta", c_f32), ("eps", c_f32), ("two_eps", c_f32), ("eps2", c_f32), ("outside_val", c_f32),
-                ("pad1", c_i32), ("xc", c_vp), ("ldxc", c_i32), ("app_dim", c_i32), ("app_table", c_vp),
+                ("d_table_scale", c_f32), ("xc", c_vp), ("ldxc", c_i32), ("app_dim", c_i32), ("app_table", c_vp),
                 ("sdf", c_vp), ("grad", c_vp), ("hess", c_vp), ("h0c", c_vp), ("d_sdf", c_vp), ("d_grad", c_vp),
                 ("d_hess", c_vp), ("d_xc", c_vp), ("ld_dxc", c_i32), ("normal_col", c_i32), ("d_h0c", c_vp),
                 ("d_table", c_vp), ("d_pre0", c_vp), ("x0ext", c_vp), ("d_enc", c_vp), ("d_whead", c_vp),
@@ -233,7 +233,8 @@ class FusedField:
         e = lambda *s, dt=f32: torch.empty(*s, device=device, dtype=dt)  # noqa: E731
         Hc = self.Hc
         ws = dict(key=key)
-        ws.update(sdf=e(Ns), grad=e(Ns, 3), hess=e(Ns, 3), h0c=e(Ns, 256, dt=f16), xc=e(Ns, self.Kc0, dt=f16),
+        ws.update(sdf=e(Ns), grad=e(Ns, 3), hess=e(Ns, 3), h0c=self._with_ones(e(Ns, 264, dt=f16), 256),
+                  xc=e(Ns, self.Kc0, dt=f16),
                   ys=[self._with_ones(e(Ns, Hc + 8, dt=f16), Hc) for _ in range(self.n_rgb_hidden)],
                   rgbs=e(Ns, 3), rgb=e(R, 3),
                   weights=e(Ns), d_rgbs=e(Ns, 3), d_sdf=e(Ns), d_grad=e(Ns, 3), d_hess=e(Ns, 3),
@@ -313,6 +314,7 @@ class FusedField:
         fa.xc, fa.ldxc = _p(ws['xc']), self.Kc0
         fa.app_dim, fa.app_table = self.app_dim, _p(pk['app'])
         fa.sdf, fa.grad, fa.hess, fa.h0c = _p(ws['sdf']), _p(ws['grad']), _p(ws['hess']), _p(ws['h0c'])
+        fa.ld_h0c = ws['h0c'].stride(0)
         fa.x0ext = _p(ws['x0ext'])
         fa.err = _p(ws['err'])
         # ---------------- forward ----------------
@@ -385,9 +387,9 @@ class FusedField:
                err=ws['err'], X_lo=dz0_lo, out_lo=ws['dzfeat_lo'] if self.split else None)
         _dense(dz0, pk['wc0T_tail'], 64, Hc, ws['dxc_tail'], epi=EPI_IDENTITY, err=ws['err'], X_lo=dz0_lo)
         # SDF feature layer
-        gw1 = torch.empty(256, 256, **dev32)
-        _wgrad(ws['dzfeat'], ws['h0c'], 256, 256, gw1)
-        grads['w1'], grads['b1'] = gw1, torch.sum(ws['dzfeat'], 0, dtype=torch.float32)
+        gw1 = torch.empty(256, 264, **dev32)
+        _wgrad(ws['dzfeat'], ws['h0c'], 256, 264, gw1)             # column 256: the bias gradient
+        grads['w1'], grads['b1'] = gw1[:, :256], gw1[:, 256]
         _dense(ws['dzfeat'], pk['w1T'], 256, 256, ws['d_h0c'], epi=EPI_IDENTITY, err=ws['err'],
                X_lo=ws['dzfeat_lo'] if self.split else None)
         if self.app_dim:
@@ -396,8 +398,17 @@ class FusedField:
                       c_vp(ws['dxc_tail'].data_ptr()), 64, 22, self.app_dim, c_vp(g_app.data_ptr()), stream)
             grads['app'] = g_app
         # ---------------- field backward ----------------
+        # the table gradient is scattered straight into the FP32 master's .grad (accumulating, as
+        # autograd does), already unscaled; an fp16 table gets a separate FP32 buffer
         table = sdfm.tcnn_encoding.params
-        d_table = torch.zeros(table.shape, device=dev, dtype=torch.float32)
+        self._table_in_place = table.dtype == torch.float32
+        if self._table_in_place:
+            if table.grad is None:
+                table.grad = torch.zeros_like(table)
+            d_table = table.grad
+        else:
+            d_table = torch.zeros(table.shape, device=dev, dtype=torch.float32)
+        fa.d_table_scale = 1.0 / self.loss_scale
         ws['d_whead'].zero_()
         ws['d_bhead'].zero_()
         fa.d_sdf, fa.d_grad, fa.d_hess = _p(ws['d_sdf']), _p(ws['d_grad']), _p(ws['d_hess'])
@@ -478,7 +489,8 @@ class FusedField:
             _acc(lin.bias, db * inv)
         _acc(sdf.mlp.linear_sdf.weight, (self.ws['d_whead'] * inv).reshape(1, -1))
         _acc(sdf.mlp.linear_sdf.bias, self.ws['d_bhead'] * inv)
-        _acc(sdf.tcnn_encoding.params, g['table'].mul_(inv).to(sdf.tcnn_encoding.params.dtype))
+        if not self._table_in_place:
+            _acc(sdf.tcnn_encoding.params, g['table'].to(sdf.tcnn_encoding.params.dtype))
         _acc(m.s_var, (self.ws['d_s_var'] * inv).reshape(()))
         if self.app_dim:
             _acc(m.appear_embed.weight, g['app'] * inv)
