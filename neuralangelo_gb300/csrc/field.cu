@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(256) k_field_gather(FieldParams p, int64_t nti
     const int r = (int)(grow - (uint32_t)t * (SPT * EVALS));
     const int e = r / SPT, sl = r % SPT;
     const int64_t s = t * SPT + sl;
-    __half* dst = (__half*)p.x0ext + grow * KX;
+    __half* dst = (__half*)p.x0ext + (int64_t)grow * KX;     // 64-bit: rows * KX can exceed 2^32
     float v[F], lo[F];
     float x[3] = {0.f, 0.f, 0.f};
     const bool live = s < p.Ns;
