@@ -250,25 +250,37 @@ __global__ void __launch_bounds__(DENSE_TPB, 1) k_dense(const __grid_constant__ 
                 }
                 if constexpr (CHUNK == 32) {
                     if (p.tma_store) {
-                        // coalesced write-back: the warp's 32 x 32 block goes through shared memory
-                        // (64-byte swizzle: 16-byte chunk j of row r at chunk j ^ ((r >> 1) & 3))
-                        // and leaves as one TMA store; rows past M are clipped by the TMA unit
+                        // coalesced write-back: the warp's block goes through a 2 KB staging
+                        // buffer of 64-byte rows (64-byte swizzle: 16-byte chunk j of row r at
+                        // chunk j ^ ((r >> 1) & 3)) and leaves as TMA stores; rows past M are
+                        // clipped by the TMA unit.  fp16: one 32 x 32 box; fp32: two 32 x 16 boxes.
                         uint8_t* stg = stage_s + warp * (32 * 32 * 2);
-                        if (lane == 0) umma::bulk_wait_read0();      // the previous store has read it
-                        __syncwarp();
+                        const int halves = p.y_f32 ? 2 : 1;
+                        for (int hh = 0; hh < halves; ++hh) {
+                            if (lane == 0) umma::bulk_wait_read0();      // the previous store has read it
+                            __syncwarp();
 #pragma unroll
-                        for (int j = 0; j < 4; ++j) {
-                            __half2 h[4];
+                            for (int j = 0; j < 4; ++j) {
+                                uint4 u;
+                                if (p.y_f32) {
+                                    const float* f = v + 16 * hh + 4 * j;
+                                    u = make_uint4(__float_as_uint(f[0]), __float_as_uint(f[1]), __float_as_uint(f[2]),
+                                                   __float_as_uint(f[3]));
+                                } else {
+                                    __half2 h[4];
 #pragma unroll
-                            for (int k = 0; k < 4; ++k) h[k] = __floats2half2_rn(v[8 * j + 2 * k], v[8 * j + 2 * k + 1]);
-                            *reinterpret_cast<uint4*>(stg + lane * 64 + ((j ^ ((lane >> 1) & 3)) * 16)) =
-                                *reinterpret_cast<const uint4*>(h);
-                        }
-                        umma::fence_proxy_async_smem();
-                        __syncwarp();
-                        if (lane == 0) {
-                            umma::tma_store_2d(&tm_y, n0 + c0, (int)(t * TILE_M) + q * 32, stg);
-                            umma::bulk_commit();
+                                    for (int k = 0; k < 4; ++k)
+                                        h[k] = __floats2half2_rn(v[8 * j + 2 * k], v[8 * j + 2 * k + 1]);
+                                    u = *reinterpret_cast<const uint4*>(h);
+                                }
+                                *reinterpret_cast<uint4*>(stg + lane * 64 + ((j ^ ((lane >> 1) & 3)) * 16)) = u;
+                            }
+                            umma::fence_proxy_async_smem();
+                            __syncwarp();
+                            if (lane == 0) {
+                                umma::tma_store_2d(&tm_y, n0 + c0 + 16 * hh, (int)(t * TILE_M) + q * 32, stg);
+                                umma::bulk_commit();
+                            }
                         }
                     }
                 }
@@ -347,18 +359,20 @@ static int a_tensor_map(CUtensorMap* map, const void* base, int64_t rows, int co
     return GBSDF_OK;
 }
 
-// TMA map of the fp16 output [rows x cols] (row stride ld): boxes of 32 columns x 32 rows, 64-byte swizzle
-static int y_tensor_map(CUtensorMap* map, void* base, int64_t rows, int cols, int ld) {
+// TMA map of the output [rows x cols] (row stride ld elements): boxes of 64-byte rows x 32 rows
+// (32 fp16 or 16 fp32 columns), 64-byte swizzle
+static int y_tensor_map(CUtensorMap* map, void* base, int64_t rows, int cols, int ld, bool f32) {
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
     if (!enc) {
         set_error("cuTensorMapEncodeTiled is not available from the driver");
         return GBSDF_ERR_CUDA;
     }
     const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-    const cuuint32_t box[2] = {32, 32};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * (f32 ? 4 : 2)};
+    const cuuint32_t box[2] = {f32 ? 16u : 32u, 32};
     const cuuint32_t es[2] = {1, 1};
-    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, base, dims, strides, box, es,
+    const CUresult r = enc(map, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, base, dims,
+                           strides, box, es,
                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
@@ -370,9 +384,9 @@ static int y_tensor_map(CUtensorMap* map, void* base, int64_t rows, int cols, in
 
 template <int N_TILE, int EPI>
 static int launch_dense(DenseParams p, cudaStream_t s) {
-    // the TMA write-back needs 32-column chunks, an fp16 output without a low half, and the
-    // staging buffers next to at least MIN_SLOTS ring slots
-    p.tma_store = (N_TILE / 4 >= 32 && !p.y_f32 && !p.Ylo &&
+    // the TMA write-back needs 32-column chunks, no low output half, 16-byte row strides and
+    // the staging buffers next to at least MIN_SLOTS ring slots
+    p.tma_store = (N_TILE / 4 >= 32 && !p.Ylo && aligned(p.Y, 16) && p.ldy % (p.y_f32 ? 4 : 8) == 0 &&
                    dense_smem_slots(N_TILE, p.K, MIN_SLOTS, true) <= DENSE_SMEM_MAX) ? 1 : 0;
     p.nslots = dense_slots(N_TILE, p.K, p.tma_store != 0);
     const size_t smem = dense_smem_slots(N_TILE, p.K, p.nslots, p.tma_store != 0);
@@ -389,7 +403,7 @@ static int launch_dense(DenseParams p, cudaStream_t s) {
     if (int st = a_tensor_map(&tm_x, p.X, p.M, p.K, p.ldx)) return st;
     if (int st = a_tensor_map(&tm_xlo, p.Xlo ? p.Xlo : p.X, p.M, p.K, p.ldx)) return st;
     if (p.tma_store) {
-        if (int st = y_tensor_map(&tm_y, p.Y, p.M, p.N_total, p.ldy)) return st;
+        if (int st = y_tensor_map(&tm_y, p.Y, p.M, p.N_total, p.ldy, p.y_f32 != 0)) return st;
     } else {
         tm_y = tm_x;                                       // unused
     }

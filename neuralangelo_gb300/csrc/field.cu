@@ -162,11 +162,16 @@ __global__ void __launch_bounds__(256) k_field_gather(FieldParams p, int64_t nti
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t rows = (uint32_t)(ntiles * (SPT * EVALS));
     if (i >= rows * (uint32_t)A) return;
-    const uint32_t grow = i / (uint32_t)A;
-    const int l = (int)(i - grow * (uint32_t)A);
-    const int64_t t = grow / (SPT * EVALS);
-    const int r = (int)(grow - (uint32_t)t * (SPT * EVALS));
-    const int e = r / SPT, sl = r % SPT;
+    // thread order (tile, sample, evaluation, level): the 7 evaluations of a sample are
+    // neighbouring threads, so at coarse levels (same cell for all taps) their corner
+    // rows come from L1; the output row is t * 126 + e * 18 + sl
+    const uint32_t q = i / (uint32_t)A;
+    const int l = (int)(i - q * (uint32_t)A);
+    const uint32_t se = q / EVALS;                   // tile-major sample slot
+    const int e = (int)(q - se * EVALS);
+    const int64_t t = se / SPT;
+    const int sl = (int)(se - (uint32_t)t * SPT);
+    const uint32_t grow = (uint32_t)t * (SPT * EVALS) + e * SPT + sl;
     const int64_t s = t * SPT + sl;
     __half* dst = (__half*)p.x0ext + (int64_t)grow * KX;     // 64-bit: rows * KX can exceed 2^32
     float v[F], lo[F];
@@ -274,8 +279,37 @@ __global__ void __launch_bounds__(256) k_field_scatter(FieldParams p) {
             for (int f = 0; f < F; ++f) pacc[cc][f] = fmaf(w, g[f], pacc[cc][f]);
         }
     }
+    // Final flush.  With 8 active levels the lanes l, l + 8, l + 16, l + 24 of a warp hold
+    // level l of four consecutive samples, which at coarse levels often end in the same
+    // cell.  Two xor-shuffle steps merge equal entries: two lanes merge only when both
+    // still own their sums, the lower lane absorbing the upper one's, so every
+    // contribution is written exactly once.  Only whole live warps take part (Ns * 8 a
+    // multiple of 32), so no lane has left the kernel.
+    const int lane = threadIdx.x & 31;
+    const bool grouped = A == 8 && (((uint32_t)p.Ns * 8u) & 31u) == 0u;
 #pragma unroll
-    for (int cc = 0; cc < 8; ++cc) scatter_add<F>(base + (uint64_t)pidx[cc] * F, pacc[cc]);
+    for (int cc = 0; cc < 8; ++cc) {
+        bool mine = true;
+        if (grouped) {
+#pragma unroll
+            for (int off = 8; off <= 16; off <<= 1) {
+                const uint32_t other_idx = __shfl_xor_sync(0xffffffffu, pidx[cc], off);
+                const bool other_mine = __shfl_xor_sync(0xffffffffu, mine ? 1 : 0, off) != 0;
+                float other[F];
+#pragma unroll
+                for (int f = 0; f < F; ++f) other[f] = __shfl_xor_sync(0xffffffffu, pacc[cc][f], off);
+                if (mine && other_mine && other_idx == pidx[cc]) {
+                    if ((lane & off) == 0) {
+#pragma unroll
+                        for (int f = 0; f < F; ++f) pacc[cc][f] += other[f];
+                    } else {
+                        mine = false;
+                    }
+                }
+            }
+        }
+        if (mine) scatter_add<F>(base + (uint64_t)pidx[cc] * F, pacc[cc]);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -504,8 +538,8 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
     uint8_t* a3_s = a_s + TILE_M * KB * 2;                      // [128 x K0]  features lo
     float* wh_s = reinterpret_cast<float*>(a3_s + TILE_M * K0 * 2);   // [256] head weights
     float* dwh_s = wh_s + HID;                                  // [256] d_whead accumulator
-    float* df_s = dwh_s + HID;                                  // [7][18] d f per evaluation
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(df_s + EVALS * SPT + 2);
+    float* df_s = dwh_s + HID;                                  // [2][7][18] d f per evaluation, double-buffered
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(df_s + 2 * EVALS * SPT + 4);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -540,9 +574,11 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
     float dbh = 0.0f;
     bool ok = true;
 
-    // per-sample output gradients -> d f of each evaluation (modules.py:144-156)
-    auto prologue = [&](int64_t tt) {
+    // per-sample output gradients -> d f of each evaluation (modules.py:144-156), into
+    // buffer `buf` of df_s: the next tile's are computed while this tile's are in use
+    auto prologue = [&](int64_t tt, int buf) {
         const int64_t s0 = tt * SPT;
+        float* dfb = df_s + buf * (EVALS * SPT);
         if (tid < SPT) {
             const int64_t s = s0 + tid;
             float df[EVALS] = {0, 0, 0, 0, 0, 0, 0};
@@ -579,7 +615,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
             }
 #pragma unroll
             for (int e = 0; e < EVALS; ++e) {
-                df_s[e * SPT + tid] = df[e];
+                dfb[e * SPT + tid] = df[e];
                 dbh += df[e];
             }
         }
@@ -603,14 +639,15 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
     };
     int64_t t = blockIdx.x;
     if (t < ntiles) {
-        prologue(t);
+        prologue(t, 0);
         stage(t);
         cp_async_wait_all();
         umma::fence_proxy_async_smem();
     }
     __syncthreads();
     if (t < ntiles) issue1();
-    for (; t < ntiles && ok; t += gridDim.x) {
+    int it = 0;
+    for (; t < ntiles && ok; t += gridDim.x, ++it) {
         const int64_t s0 = t * SPT;
         ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
         phase ^= 1u;
@@ -619,13 +656,16 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
             break;
         }
         const int64_t tn = t + gridDim.x;
-        if (tn < ntiles) stage(tn);                  // A is free: MMA1 of tile t completed
+        if (tn < ntiles) {
+            stage(tn);                               // A is free: MMA1 of tile t completed
+            prologue(tn, (it + 1) & 1);              // the other df buffer; read after the loop-end barrier
+        }
         umma::fence_after_sync();
         // (2) d_pre = (d f * w_head + [centre] d_h0c) * softplus'(pre) -> TMEM (hi, lo) and d_pre0
         {
             const int64_t s = s0 + sl_row;
             const bool live = row < SPT * EVALS && s < p.Ns;
-            const float df = live ? df_s[row] : 0.0f;
+            const float df = live ? df_s[(it & 1) * (EVALS * SPT) + row] : 0.0f;
             const bool centre = live && e_row == 0;
             const float inv_beta = 1.0f / p.beta;
 #pragma unroll 1
@@ -712,13 +752,11 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
             }
         }
         umma::fence_before_sync();
-        __syncthreads();                              // df_s and the TMEM accumulator of tile t fully read
         if (tn < ntiles) {
-            prologue(tn);
             cp_async_wait_all();
             umma::fence_proxy_async_smem();
         }
-        __syncthreads();
+        __syncthreads();   // the TMEM accumulator of tile t read; tile tn's A tile and d f in place
         if (tn < ntiles) issue1();
     }
     umma::fence_before_sync();
@@ -870,7 +908,7 @@ static size_t fwd_smem(int K0) {
 static size_t bwd_smem(int K0) {
     const size_t KB = (size_t)K0 + 16;
     const size_t need = (size_t)HID * KB * 2 + (size_t)K0 * HID * 2 + (size_t)TILE_M * (KB + K0) * 2 +
-                        (2 * HID + EVALS * SPT + 2) * 4 + 16;
+                        (2 * HID + 2 * EVALS * SPT + 4) * 4 + 16;
     return need > BWD_SMEM_FLOOR ? need : BWD_SMEM_FLOOR;
 }
 
