@@ -163,7 +163,7 @@ typedef struct gbsdf_field_args {
     int32_t K0;
     const void* table;       /* fp16 [entries, F] */
     const void* w0e;         /* fp16 [256, K0] */
-    const void* w0eT;        /* fp16 [K0, 256] */
+    const void* w0eT;        /* unused (the backward reads W0e from w0b); may be NULL */
     const void* w0b;         /* fp16 [256, K0 + 16]: w0e | position and bias columns as hi/lo pairs
                                 (x hi, b hi, x lo, b lo, x-weight lo; see the x0ext tail) */
     const float* w0x;        /* [256, 3] */

@@ -8,10 +8,9 @@
 // These are the colour-MLP layers of NeuralRGB (projects/neuralangelo/utils/
 // modules.py:199-220 via projects/nerf/utils/nerf_util.py:158-196) and the SDF
 // feature layer (utils/mlp.py:55-69), forward and input-gradient.
-#include <cuda.h>
-#include <cudaTypedefs.h>
 
 #include "dense.cuh"
+#include "tma.cuh"
 
 namespace gbsdf {
 
@@ -321,65 +320,18 @@ static int dense_slots(int n_tile, int K, bool stage) {
     return s;
 }
 
-// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link)
-static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
-        void* f = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
-    }
-    return fn;
-}
-
 // TMA map of an fp16 matrix [rows x cols] with row stride ld elements: boxes of
 // 64 columns x 128 rows, 128-byte swizzle, out-of-range elements read as zero
 static int a_tensor_map(CUtensorMap* map, const void* base, int64_t rows, int cols, int ld) {
-    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
-    if (!enc) {
-        set_error("cuTensorMapEncodeTiled is not available from the driver");
-        return GBSDF_ERR_CUDA;
-    }
-    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-    const cuuint32_t box[2] = {KCH, TILE_M};
-    const cuuint32_t es[2] = {1, 1};
-    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) {
-        set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
-        return GBSDF_ERR_CUDA;
-    }
-    return GBSDF_OK;
+    return tensor_map_2d(map, false, base, rows, cols, ld, KCH, TILE_M, CU_TENSOR_MAP_SWIZZLE_128B,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, "input");
 }
 
 // TMA map of the output [rows x cols] (row stride ld elements): boxes of 64-byte rows x 32 rows
 // (32 fp16 or 16 fp32 columns), 64-byte swizzle
 static int y_tensor_map(CUtensorMap* map, void* base, int64_t rows, int cols, int ld, bool f32) {
-    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
-    if (!enc) {
-        set_error("cuTensorMapEncodeTiled is not available from the driver");
-        return GBSDF_ERR_CUDA;
-    }
-    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    const cuuint64_t strides[1] = {(cuuint64_t)ld * (f32 ? 4 : 2)};
-    const cuuint32_t box[2] = {f32 ? 16u : 32u, 32};
-    const cuuint32_t es[2] = {1, 1};
-    const CUresult r = enc(map, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, base, dims,
-                           strides, box, es,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
-                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) {
-        set_error("cuTensorMapEncodeTiled (output) failed (%d)", (int)r);
-        return GBSDF_ERR_CUDA;
-    }
-    return GBSDF_OK;
+    return tensor_map_2d(map, f32, base, rows, cols, ld, f32 ? 16 : 32, 32, CU_TENSOR_MAP_SWIZZLE_64B,
+                         CU_TENSOR_MAP_L2_PROMOTION_NONE, "output");
 }
 
 template <int N_TILE, int EPI>

@@ -15,6 +15,7 @@
 // three position columns, bias, softplus and the SDF head run in fp32 in the
 // epilogue, so SDF values and the tap differences keep fp32 accuracy.
 #include "dense.cuh"
+#include "tma.cuh"
 
 namespace gbsdf {
 
@@ -517,34 +518,44 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
 //   the epilogue forms d_pre = (d f w_head + [centre] d_h0c) softplus'(pre) and the
 //        head-weight gradient, writes d_pre as an fp16 hi + lo pair into TMEM (the A
 //        operand of MMA2) and its hi half to global for the layer-0 weight gradient;
-//   MMA2 d_enc = d_pre W0e (A from TMEM, B = W0e^T in shared memory) goes to global
-//        for k_field_scatter.
+//   MMA2 d_enc = d_pre W0e (A from TMEM, B = the W0e part of MMA1's w0b tile read
+//        MN-major) goes to global for k_field_scatter.
 // The +eps and -eps taps of a sample carry large, nearly cancelling d_pre, so a
 // single fp16 rounding of d_pre would dominate the table-gradient error: hence the pair.
 // TMEM (512 columns, one CTA per SM): [0, 256) MMA1's accumulator, reused for
 // MMA2's [128 x K0] result; [256, 384) d_pre hi, [384, 512) d_pre lo.
+// d_pre0 and d_enc leave through a 4 KB staging buffer per warp and TMA stores
+// (one thread per row would touch 32 cache lines per store instruction); a tile has
+// 126 rows, so the last lane quadrant stores a 30-row box.
 constexpr size_t BWD_SMEM_FLOOR = 120 * 1024;   // > half an SM's shared memory: one CTA per SM
 constexpr int BWD_THREADS = 512;                 // 16 warps: 4 lane quadrants x 4 quarters of the hidden units
+constexpr int BWD_STAGE_BYTES = 4096;            // per warp: 32 rows x 128 bytes
+constexpr int TILE_ROWS = SPT * EVALS;           // 126
+constexpr int DH0_LD = HID + 4;                  // d_h0c rows in shared memory, padded against bank conflicts
 
 template <int F>
-__global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
+__global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
+                                                             const __grid_constant__ CUtensorMap tm_pre32,
+                                                             const __grid_constant__ CUtensorMap tm_pre30,
+                                                             const __grid_constant__ CUtensorMap tm_enc32,
+                                                             const __grid_constant__ CUtensorMap tm_enc30) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int K0 = p.K0;
     const int KB = K0 + 16;                                     // features hi + tail
     const int KX = 2 * K0 + 16;                                 // x0ext row width
-    uint8_t* w_s = smem;                                        // [256 x KB]  w0b: B of MMA1
-    uint8_t* wt_s = w_s + HID * KB * 2;                         // [K0 x 256]  W0e^T: B of MMA2
-    uint8_t* a_s = wt_s + K0 * HID * 2;                         // [128 x KB]  features hi | tail
+    uint8_t* stage_s = smem;                                    // [16 warps][4 KB] TMA store staging
+    uint8_t* w_s = stage_s + (BWD_THREADS / 32) * BWD_STAGE_BYTES;   // [256 x KB]  w0b: B of MMA1
+    uint8_t* a_s = w_s + HID * KB * 2;                          // [128 x KB]  features hi | tail
     uint8_t* a3_s = a_s + TILE_M * KB * 2;                      // [128 x K0]  features lo
     float* wh_s = reinterpret_cast<float*>(a3_s + TILE_M * K0 * 2);   // [256] head weights
     float* dwh_s = wh_s + HID;                                  // [256] d_whead accumulator
     float* df_s = dwh_s + HID;                                  // [2][7][18] d f per evaluation, double-buffered
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(df_s + 2 * EVALS * SPT + 4);
+    float* dh0_s = df_s + 2 * EVALS * SPT + 4;                  // [18][DH0_LD] d_h0c of the tile's samples
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(dh0_s + SPT * DH0_LD);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     stage_rows_kmajor(w_s, (const __half*)p.w0b, 0, HID, KB, KB, tid, BWD_THREADS, HID);
-    stage_rows_kmajor(wt_s, (const __half*)p.w0eT, 0, K0, HID, HID, tid, BWD_THREADS, K0);
     for (int i = tid; i < HID; i += BWD_THREADS) {
         wh_s[i] = p.whead[i];
         dwh_s[i] = 0.0f;
@@ -563,9 +574,9 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
     const uint32_t tmem = *tslot;
     const uint32_t t_hi = tmem + HID, t_lo = tmem + HID + HID / 2;
     const uint32_t idesc1 = umma::idesc_f16(TILE_M, HID);
-    const uint32_t idesc2 = umma::idesc_f16(TILE_M, K0);
+    const uint32_t idesc2 = umma::idesc_f16_bmn(TILE_M, K0);
     const uint32_t a_addr = umma::smem_u32(a_s), w_addr = umma::smem_u32(w_s);
-    const uint32_t wt_addr = umma::smem_u32(wt_s), a3_addr = umma::smem_u32(a3_s);
+    const uint32_t a3_addr = umma::smem_u32(a3_s);
     const int64_t ntiles = (p.Ns + SPT - 1) / SPT;
     const int q = warp & 3, part = warp >> 2;                   // lane quadrant, quarter of the hidden units
     const int row = q * 32 + lane;
@@ -574,22 +585,44 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
     float dbh = 0.0f;
     bool ok = true;
 
-    // per-sample output gradients -> d f of each evaluation (modules.py:144-156), into
-    // buffer `buf` of df_s: the next tile's are computed while this tile's are in use
-    auto prologue = [&](int64_t tt, int buf) {
-        const int64_t s0 = tt * SPT;
-        float* dfb = df_s + buf * (EVALS * SPT);
+    // per-sample output gradients -> d f of each evaluation (modules.py:144-156), for
+    // the next tile while this one is in flight, in three steps that keep the global
+    // loads off the tile's critical path: the per-sample loads at the top of the tile,
+    // the per-ray `outside` flag before MMA2, the arithmetic into df_s[buf] at the end
+    struct PrologueIn {
+        float g[3], dg[3], dh[3], n[3], dsdf;
+        int r;
+        bool out;
+    };
+    auto prologue_load = [&](int64_t tt, PrologueIn& in) {
+        const int64_t s = tt * SPT + tid;
+        if (tid < SPT && s < p.Ns) {
+            in.r = ray_of(p, s);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                in.g[d] = p.grad[3 * s + d];
+                in.dg[d] = p.d_grad[3 * s + d];
+                in.dh[d] = p.d_hess[3 * s + d];
+            }
+            // normals = g / max(|g|, 1e-12) feed the colour MLP (model.py:167)
+            const float* dn = p.d_xc + s * (int64_t)p.ld_dxc + p.normal_col;
+            in.n[0] = dn[0]; in.n[1] = dn[1]; in.n[2] = dn[2];
+            in.dsdf = p.d_sdf[s];
+        }
+    };
+    auto prologue_ray = [&](int64_t tt, PrologueIn& in) {
+        const int64_t s = tt * SPT + tid;
+        if (tid < SPT && s < p.Ns) in.out = p.outside && p.outside[in.r];
+    };
+    auto prologue_finish = [&](int64_t tt, const PrologueIn& in, int buf) {
         if (tid < SPT) {
-            const int64_t s = s0 + tid;
+            const int64_t s = tt * SPT + tid;
+            float* dfb = df_s + buf * (EVALS * SPT);
             float df[EVALS] = {0, 0, 0, 0, 0, 0, 0};
             if (s < p.Ns) {
-                const int r = ray_of(p, s);
-                const bool out = p.outside && p.outside[r];
-                const float g0 = p.grad[3 * s], g1 = p.grad[3 * s + 1], g2 = p.grad[3 * s + 2];
-                float dg[3] = {p.d_grad[3 * s], p.d_grad[3 * s + 1], p.d_grad[3 * s + 2]};
-                // normals = g / max(|g|, 1e-12) feed the colour MLP (model.py:167)
-                const float* dn = p.d_xc + s * (int64_t)p.ld_dxc + p.normal_col;
-                const float n0 = dn[0], n1 = dn[1], n2 = dn[2];
+                const float g0 = in.g[0], g1 = in.g[1], g2 = in.g[2];
+                const float n0 = in.n[0], n1 = in.n[1], n2 = in.n[2];
+                float dg[3] = {in.dg[0], in.dg[1], in.dg[2]};
                 const float len = sqrtf(g0 * g0 + g1 * g1 + g2 * g2);
                 if (len > 1e-12f) {
                     const float inv = 1.0f / len;
@@ -604,14 +637,13 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
                 float hsum = 0.0f;
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
-                    const float dh = p.d_hess[3 * s + d];
-                    const float a = dg[d] / p.two_eps, b = dh / p.eps2;
+                    const float a = dg[d] / p.two_eps, b = in.dh[d] / p.eps2;
                     df[1 + 2 * d] = a + b;
                     df[2 + 2 * d] = -a + b;
                     hsum += b;
                 }
                 // the centre feeds alpha and the Hessian only where it was not overwritten
-                df[0] = out ? 0.0f : (p.d_sdf[s] - 2.0f * hsum);
+                df[0] = in.out ? 0.0f : (in.dsdf - 2.0f * hsum);
             }
 #pragma unroll
             for (int e = 0; e < EVALS; ++e) {
@@ -622,12 +654,24 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
     };
     // encoder features of a tile, streamed back from the forward's x0ext rows (rows
     // 126-127 of a tile read the next tile's first rows or zeros; their MMA results
-    // are never used); the next tile's load overlaps this tile's epilogue
+    // are never used), and the d_h0c rows of its 18 samples; the next tile's load
+    // overlaps this tile's epilogue
     const int64_t xrows = ntiles * (int64_t)(SPT * EVALS);
-    auto stage = [&](int64_t tt) {
+    auto stage_a = [&](int64_t tt) {               // one cp.async group
         const __half* xb = (const __half*)p.x0ext;
         stage_rows_kmajor(a_s, xb, tt * (SPT * EVALS), xrows, KX, KB, tid, BWD_THREADS);
         stage_rows_kmajor(a3_s, xb + K0 + 16, tt * (SPT * EVALS), xrows, KX, K0, tid, BWD_THREADS);
+        cp_async_commit();
+    };
+    auto stage_dh0 = [&](int64_t tt) {             // one cp.async group
+        for (int c = tid; c < SPT * (HID / 4); c += BWD_THREADS) {
+            const int js = c / (HID / 4), k4 = c - js * (HID / 4);
+            const int64_t ss = tt * SPT + js;
+            float* dst = dh0_s + js * DH0_LD + 4 * k4;
+            if (ss < p.Ns) cp_async16(dst, p.d_h0c + ss * HID + 4 * k4);
+            else *reinterpret_cast<float4*>(dst) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        cp_async_commit();
     };
     auto issue1 = [&]() {
         if (tid == 0) {
@@ -638,9 +682,13 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
         }
     };
     int64_t t = blockIdx.x;
+    PrologueIn pin;
     if (t < ntiles) {
-        prologue(t, 0);
-        stage(t);
+        prologue_load(t, pin);
+        prologue_ray(t, pin);
+        prologue_finish(t, pin, 0);
+        stage_a(t);
+        stage_dh0(t);
         cp_async_wait_all();
         umma::fence_proxy_async_smem();
     }
@@ -649,6 +697,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
     int it = 0;
     for (; t < ntiles && ok; t += gridDim.x, ++it) {
         const int64_t s0 = t * SPT;
+        cp_async_wait_group<0>();                    // this tile's d_h0c rows
         ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
         phase ^= 1u;
         if (!ok) {
@@ -656,12 +705,18 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
             break;
         }
         const int64_t tn = t + gridDim.x;
-        if (tn < ntiles) {
-            stage(tn);                               // A is free: MMA1 of tile t completed
-            prologue(tn, (it + 1) & 1);              // the other df buffer; read after the loop-end barrier
-        }
         umma::fence_after_sync();
+        if (tn < ntiles) {
+            stage_a(tn);                             // A is free: MMA1 of tile t completed
+            prologue_load(tn, pin);                  // consumed at the end of the tile
+        }
         // (2) d_pre = (d f * w_head + [centre] d_h0c) * softplus'(pre) -> TMEM (hi, lo) and d_pre0
+        uint8_t* stg = stage_s + warp * BWD_STAGE_BYTES;
+        const CUtensorMap* tm_pre = q == 3 ? &tm_pre30 : &tm_pre32;
+        const CUtensorMap* tm_enc = q == 3 ? &tm_enc30 : &tm_enc32;
+        const int y0 = (int)(t * TILE_ROWS) + q * 32;
+        if (lane == 0) umma::bulk_wait_read0();      // the previous tile's d_enc store has read the buffer
+        __syncwarp();
         {
             const int64_t s = s0 + sl_row;
             const bool live = row < SPT * EVALS && s < p.Ns;
@@ -674,7 +729,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
                 umma::tmem_ld16(umma::taddr(tmem, q * 32, c0), v);
                 float dh0[16];
                 if (centre) {
-                    const float4* src = reinterpret_cast<const float4*>(p.d_h0c + s * HID + c0);
+                    const float4* src = reinterpret_cast<const float4*>(dh0_s + sl_row * DH0_LD + c0);
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
                         const float4 f = src[j];
@@ -707,30 +762,43 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
                 }
                 umma::tmem_st8(umma::taddr(t_hi, q * 32, c0 / 2), hi);
                 umma::tmem_st8(umma::taddr(t_lo, q * 32, c0 / 2), lo);
-                if (row < SPT * EVALS) {   // dead samples store zeros (their x0ext rows are zero too)
-                    uint4* dst = reinterpret_cast<uint4*>((__half*)p.d_pre0 + (t * (SPT * EVALS) + row) * (int64_t)HID +
-                                                          c0);
-                    dst[0] = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-                    dst[1] = make_uint4(hi[4], hi[5], hi[6], hi[7]);
-                }
+                // d_pre0 (hi) into the staging rows; dead samples store zeros (their x0ext
+                // rows are zero too).  128-byte swizzle: 16-byte unit u of row r sits at u ^ (r & 7)
+                const int u = (c0 - part * 64) >> 3;
+                *reinterpret_cast<uint4*>(stg + lane * 128 + ((u ^ (lane & 7)) * 16)) =
+                    make_uint4(hi[0], hi[1], hi[2], hi[3]);
+                *reinterpret_cast<uint4*>(stg + lane * 128 + (((u + 1) ^ (lane & 7)) * 16)) =
+                    make_uint4(hi[4], hi[5], hi[6], hi[7]);
             }
+        }
+        umma::fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) {
+            umma::tma_store_2d(tm_pre, part * 64, y0, stg);
+            umma::bulk_commit();
         }
         umma::tmem_wait_st();
         umma::fence_before_sync();
         __syncthreads();
-        // (3) d_enc = d_pre * W0e  (MMA2: A = d_pre [128 x 256] in TMEM, B = W0e^T [K0 x 256])
+        // (3) d_enc = d_pre * W0e  (MMA2: A = d_pre [128 x 256] in TMEM; B = W0e read
+        // MN-major from MMA1's w0b tile: the core matrix of hidden rows 8g..8g+7 and
+        // feature columns 8c..8c+7 sits at g * KB * 16 + c * 128 bytes)
         if (tid == 0) {
             umma::fence_after_sync();
-            const uint32_t sbo = (uint32_t)HID * 16u;
+            const uint32_t lbo = (uint32_t)KB * 16u;          // next 8 hidden units (K)
             for (int ks = 0; ks < HID / 16; ++ks) {          // the lo half first (smaller addends)
-                const uint64_t bd = umma::make_desc(wt_addr + ks * 256u, 128u, sbo);
+                const uint64_t bd = umma::make_desc(w_addr + ks * 2u * lbo, lbo, 128u);
                 umma::mma_f16_ta(tmem, t_lo + ks * 8, bd, idesc2, ks > 0 ? 1u : 0u);
             }
             for (int ks = 0; ks < HID / 16; ++ks) {
-                const uint64_t bd = umma::make_desc(wt_addr + ks * 256u, 128u, sbo);
+                const uint64_t bd = umma::make_desc(w_addr + ks * 2u * lbo, lbo, 128u);
                 umma::mma_f16_ta(tmem, t_hi + ks * 8, bd, idesc2, 1u);
             }
             umma::mma_commit(mbar);
+        }
+        if (tn < ntiles) {
+            stage_dh0(tn);                           // every warp has read this tile's d_h0c rows
+            prologue_ray(tn, pin);
         }
         ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
         phase ^= 1u;
@@ -740,25 +808,36 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p) {
         }
         umma::fence_after_sync();
         // (4) d_enc rows to global for k_field_scatter: 16-column chunks dealt in turn
-        // to the four warps of a lane quadrant
-        for (int c0 = part * 16; c0 < K0; c0 += 64) {
+        // to the four warps of a lane quadrant (K0 <= 128: at most two per warp, one
+        // 2 KB half of the staging buffer each; 64-byte swizzle: unit j of row r at j ^ ((r >> 1) & 3))
+        if (lane == 0) umma::bulk_wait_read0();      // the d_pre0 store has read the buffer
+        __syncwarp();
+        for (int c0 = part * 16, i = 0; c0 < K0; c0 += 64, ++i) {
             float v[16];
             umma::tmem_ld16(umma::taddr(tmem, q * 32, c0), v);
-            if (row < SPT * EVALS) {
-                float* dst = p.d_enc + (t * (SPT * EVALS) + row) * (int64_t)K0 + c0;
+            uint8_t* eb = stg + i * 2048;
 #pragma unroll
-                for (int j = 0; j < 16; j += 4)
-                    *reinterpret_cast<float4*>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+            for (int j = 0; j < 4; ++j)
+                *reinterpret_cast<float4*>(eb + lane * 64 + ((j ^ ((lane >> 1) & 3)) * 16)) =
+                    make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+            umma::fence_proxy_async_smem();
+            __syncwarp();
+            if (lane == 0) {
+                umma::tma_store_2d(tm_enc, c0, y0, eb);
+                umma::bulk_commit();
             }
         }
         umma::fence_before_sync();
         if (tn < ntiles) {
-            cp_async_wait_all();
+            prologue_finish(tn, pin, (it + 1) & 1);  // the other df buffer
+            cp_async_wait_group<1>();                // tile tn's A tile (its d_h0c group may still be in flight)
             umma::fence_proxy_async_smem();
         }
         __syncthreads();   // the TMEM accumulator of tile t read; tile tn's A tile and d f in place
         if (tn < ntiles) issue1();
     }
+    cp_async_wait_all();
+    if (lane == 0) umma::bulk_wait0();               // this warp's TMA stores have completed
     umma::fence_before_sync();
     __syncthreads();
     for (int i = tid; i < HID; i += BWD_THREADS)
@@ -907,8 +986,8 @@ static size_t fwd_smem(int K0) {
 }
 static size_t bwd_smem(int K0) {
     const size_t KB = (size_t)K0 + 16;
-    const size_t need = (size_t)HID * KB * 2 + (size_t)K0 * HID * 2 + (size_t)TILE_M * (KB + K0) * 2 +
-                        (2 * HID + 2 * EVALS * SPT + 4) * 4 + 16;
+    const size_t need = (size_t)(BWD_THREADS / 32) * BWD_STAGE_BYTES + (size_t)HID * KB * 2 +
+                        (size_t)TILE_M * (KB + K0) * 2 + (2 * HID + 2 * EVALS * SPT + 4 + SPT * DH0_LD) * 4 + 16;
     return need > BWD_SMEM_FLOOR ? need : BWD_SMEM_FLOOR;
 }
 
@@ -931,8 +1010,28 @@ static int launch_field(const FieldParams& p, bool backward, cudaStream_t s) {
         return GBSDF_ERR_UNSUPPORTED;
     }
     if (backward) {
+        // d_pre0 [126 T, 256] fp16 and d_enc [126 T, K0] fp32 as TMA store targets
+        const int64_t rows = ntiles * TILE_ROWS;
+        if (rows >= ((int64_t)1 << 31)) {
+            set_error("%lld backward rows exceed the TMA coordinate range", (long long)rows);
+            return GBSDF_ERR_UNSUPPORTED;
+        }
+        CUtensorMap tm_pre32, tm_pre30, tm_enc32, tm_enc30;
+        const CUtensorMapL2promotion l2n = CU_TENSOR_MAP_L2_PROMOTION_NONE;
+        if (int st = tensor_map_2d(&tm_pre32, false, p.d_pre0, rows, HID, HID, 64, 32, CU_TENSOR_MAP_SWIZZLE_128B,
+                                   l2n, "d_pre0"))
+            return st;
+        if (int st = tensor_map_2d(&tm_pre30, false, p.d_pre0, rows, HID, HID, 64, 30, CU_TENSOR_MAP_SWIZZLE_128B,
+                                   l2n, "d_pre0"))
+            return st;
+        if (int st = tensor_map_2d(&tm_enc32, true, p.d_enc, rows, p.K0, p.K0, 16, 32, CU_TENSOR_MAP_SWIZZLE_64B, l2n,
+                                   "d_enc"))
+            return st;
+        if (int st = tensor_map_2d(&tm_enc30, true, p.d_enc, rows, p.K0, p.K0, 16, 30, CU_TENSOR_MAP_SWIZZLE_64B, l2n,
+                                   "d_enc"))
+            return st;
         cudaFuncSetAttribute(k_field_bwd<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_field_bwd<F><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p);
+        k_field_bwd<F><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30);
         const int64_t items = p.Ns * p.active;
         k_field_scatter<F><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p);
     } else {
@@ -994,10 +1093,11 @@ extern "C" int gbsdf_field_bwd(const gbsdf_field_args* params, void* stream) {
     if (int st = check_field(p)) return st;
     if (p.Ns == 0) return GBSDF_OK;
     GBSDF_CHECK_ARG(p.w0b && aligned(p.w0b, 16), "w0b (fp16 [256, K0 + 16]) missing or misaligned");
-    GBSDF_CHECK_ARG(p.w0eT && p.grad && p.d_sdf && p.d_grad && p.d_hess && p.d_xc && p.d_h0c && p.d_table &&
+    GBSDF_CHECK_ARG(p.grad && p.d_sdf && p.d_grad && p.d_hess && p.d_xc && p.d_h0c && p.d_table &&
                         p.d_pre0 && p.x0ext && p.d_enc && p.d_whead && p.d_bhead,
                     "NULL pointer");
-    GBSDF_CHECK_ARG(aligned(p.d_table, 16) && aligned(p.d_enc, 16), "d_table / d_enc alignment");
+    GBSDF_CHECK_ARG(aligned(p.d_table, 16) && aligned(p.d_enc, 16) && aligned(p.d_pre0, 16),
+                    "d_table / d_enc / d_pre0 alignment");
     switch (p.grid.n_features) {
         case 2: return launch_field<2>(p, true, as_stream(stream));
         case 4: return launch_field<4>(p, true, as_stream(stream));

@@ -56,6 +56,11 @@ __device__ __forceinline__ uint64_t make_desc_sw128(uint32_t saddr) {
 __host__ __device__ constexpr uint32_t idesc_f16(uint32_t M, uint32_t N) {
     return (1u << 4) | ((N >> 3) << 17) | ((M >> 4) << 24);
 }
+// The same with B MN-major (bit 16, "transpose B"): B's N elements are contiguous.
+// Its no-swizzle smem descriptor takes LBO = the stride between 8-row K groups and
+// SBO = the stride between 8-element N groups of the 128-byte core matrices
+// (8 K rows of 16 bytes, each holding 8 consecutive N elements).
+__host__ __device__ constexpr uint32_t idesc_f16_bmn(uint32_t M, uint32_t N) { return idesc_f16(M, N) | (1u << 16); }
 
 // ---- TMEM allocation (one full warp executes these) ----
 __device__ __forceinline__ void tmem_alloc(uint32_t* smem_dst, uint32_t ncols) {

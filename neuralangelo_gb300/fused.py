@@ -111,7 +111,7 @@ def pack_sdf(sdf):
         b0 = sdf.mlp.linears[0].bias.detach().float()
         pk = dict(
             table=sdf.tcnn_encoding.params.detach().half(),
-            w0e=w0e, w0eT=w0e.t().contiguous(), w0b=w0_with_tail(w0e, w0x, b0),
+            w0e=w0e, w0b=w0_with_tail(w0e, w0x, b0),
             w0x=w0x, b0=b0,
             whead=sdf.mlp.linear_sdf.weight.detach()[0].contiguous().float(),
             bhead=sdf.mlp.linear_sdf.bias.detach().float())
@@ -143,7 +143,7 @@ def sdf_weight_args(sdf, pk, A, K0, err=None):
     fa = FieldArgs()
     fa.grid = sdf.tcnn_encoding.layout.struct
     fa.active, fa.K0 = A, K0
-    fa.table, fa.w0e, fa.w0eT, fa.w0b = _p(pk['table']), _p(pk['w0e']), _p(pk['w0eT']), _p(pk['w0b'])
+    fa.table, fa.w0e, fa.w0b = _p(pk['table']), _p(pk['w0e']), _p(pk['w0b'])
     fa.w0x, fa.b0, fa.whead, fa.bhead = _p(pk['w0x']), _p(pk['b0']), _p(pk['whead']), _p(pk['bhead'])
     fa.beta = float(sdf.cfg_sdf.mlp.activ_params.beta)
     fa.err = _p(err)
@@ -304,7 +304,7 @@ class FusedField:
         fa.app_idx = _p(app_idx)
         fa.grid = lay.struct
         fa.active, fa.K0 = self.A, self.K0
-        fa.table, fa.w0e, fa.w0eT, fa.w0b = _p(pk['table']), _p(pk['w0e']), _p(pk['w0eT']), _p(pk['w0b'])
+        fa.table, fa.w0e, fa.w0b = _p(pk['table']), _p(pk['w0e']), _p(pk['w0b'])
         fa.w0x, fa.b0, fa.whead, fa.bhead = _p(pk['w0x']), _p(pk['b0']), _p(pk['whead']), _p(pk['bhead'])
         fa.beta = float(m.cfg.sdf.mlp.activ_params.beta)
         fa.eps = eps

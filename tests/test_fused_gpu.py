@@ -26,7 +26,7 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def build(log2T=14, n_images=10, seed=0, table_range=0.05, rgb_layers=4, rgb_hidden=256, small=False):
+def build(log2T=14, n_images=10, seed=0, table_range=0.05, rgb_layers=4, rgb_hidden=256, small=False, active=8):
     cfg = field_config("small" if small else "full")
     cfg.sdf.encoding.hashgrid.dict_size = log2T
     if not small:
@@ -36,7 +36,7 @@ def build(log2T=14, n_images=10, seed=0, table_range=0.05, rgb_layers=4, rgb_hid
     torch.manual_seed(seed)
     model = FieldModel(cfg).to(DEV)
     init_field_params(model, seed)
-    model.schedule(full_field_iteration(8))
+    model.schedule(full_field_iteration(active))
     with torch.no_grad():
         model.neural_sdf.tcnn_encoding.params.uniform_(-table_range, table_range)
     return model
@@ -140,6 +140,30 @@ def test_fused_matches_oracle(small):
     # up to ~8e-3 (two builds of this step that differ only in FP32 rounding differ by as much).
     for k, e in storage.items():
         assert e < 1e-2, (k, e)
+
+
+@pytest.mark.parametrize("active", [10, 16])
+def test_fused_more_levels_matches_oracle(active):
+    """10 active levels (80 encoder columns: some warps store two d_enc chunks) and all 16
+    (128 columns: the largest shared-memory and TMEM footprint of the field kernels)."""
+    model = build(active=active)
+    assert model.neural_sdf.active_levels == active
+    R, S = 32, 32
+    batch = make_rays(R, S, seed=4, miss_frac=0.1, n_images=10, device=DEV)
+    ff = FusedField(model)
+    model.zero_grad(set_to_none=True)
+    res = ff.step(batch)
+    torch.cuda.synchronize()
+    assert ff.check_device_errors() == 0
+    assert ff.K0 == 16 * ((active * 8 + 15) // 16)       # packed at the step
+    mine = fused_grads(model)
+    out_q, g_q = oracle_run(model, batch, fp16=True)
+    inside = ~batch['outside'][:, 0].cpu()
+    e_sdf = rel(ff.ws['sdf'].reshape(R, S).cpu()[inside], out_q['sdf'].detach()[inside])
+    e_tab = rel(mine['table'], g_q['table'])
+    e_rgb = rel(res['rgb'].cpu(), out_q['rgb'].detach())
+    print(f"\n{active} levels: sdf {e_sdf:.2e} table {e_tab:.2e} rgb {e_rgb:.2e}")
+    assert e_sdf < 1e-4 and e_tab < 1e-3 and e_rgb < 1e-4
 
 
 def test_fused_matches_plain_full_table():
