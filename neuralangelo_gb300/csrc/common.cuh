@@ -100,24 +100,54 @@ __device__ __forceinline__ float softplus_grad(float x, float beta) {
 }
 __device__ __forceinline__ float sigmoidf_(float x) { return 1.0f / (1.0f + expf(-x)); }
 
-// Fast-path softplus(beta) and its derivative for the fused FP16 kernels, from
-// one exponential: e = exp(beta z); softplus = log(1 + e) / beta; d/dz = e / (1 + e).
-// (MUFU exp/log; relative error ~1e-7, well inside the FP16 path's tolerances.)
-__device__ __forceinline__ void softplus_fast(float z, float beta, float inv_beta, float& h, float& dh) {
-    const float bz = z * beta;
-    if (bz > 20.0f) {
-        h = z;
-        dh = 1.0f;
-    } else {
-        const float e = __expf(bz);
-        const float one_e = 1.0f + e;
-        h = __logf(one_e) * inv_beta;
-        dh = __fdividef(e, one_e);
-    }
+// MUFU approximations with subnormals flushed to zero (PTX ex2/lg2/rcp .approx.ftz):
+// the fused FP16 path's activations never need subnormal precision, and the flushing
+// forms take no range fix-ups around the MUFU op.
+__device__ __forceinline__ float ex2_ftz(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
-__device__ __forceinline__ float softplus_fast_h(float z, float beta, float inv_beta) {
-    const float bz = z * beta;
-    return bz > 20.0f ? z : __logf(1.0f + __expf(bz)) * inv_beta;
+__device__ __forceinline__ float lg2_ftz(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_ftz(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Fast-path softplus(beta) and its derivative for the fused FP16 kernels, from one
+// exponential: t = beta z log2(e), e = 2^t, softplus = log2(1 + e) ln(2) / beta,
+// d/dz = e / (1 + e).  Above torch's threshold (beta z > 20) softplus is z; t is capped
+// at 64 so that e stays finite there (and d/dz rounds to 1).  Relative error ~1e-7
+// away from the far negative tail, well inside the FP16 path's tolerances.
+struct SoftplusK {
+    float c1;      // beta log2(e)
+    float c2;      // ln(2) / beta
+    float tthr;    // 20 log2(e): the threshold in units of t
+};
+__device__ __forceinline__ SoftplusK softplus_k(float beta) {
+    SoftplusK k;
+    k.c1 = beta * 1.4426950408889634f;
+    k.c2 = 0.6931471805599453f / beta;
+    k.tthr = 20.0f * 1.4426950408889634f;
+    return k;
+}
+__device__ __forceinline__ void softplus_fast(float z, const SoftplusK& k, float& h, float& dh) {
+    const float t = fminf(z * k.c1, 64.0f);
+    const float e = ex2_ftz(t);
+    const float one_e = 1.0f + e;
+    dh = e * rcp_ftz(one_e);
+    const float hl = lg2_ftz(one_e) * k.c2;
+    h = t > k.tthr ? z : hl;
+}
+__device__ __forceinline__ float softplus_fast_h(float z, const SoftplusK& k) {
+    const float t = fminf(z * k.c1, 64.0f);
+    const float hl = lg2_ftz(1.0f + ex2_ftz(t)) * k.c2;
+    return t > k.tthr ? z : hl;
 }
 
 // Column sums of a 32 x 32 block held one row per lane (v[j] = element (lane, j)):

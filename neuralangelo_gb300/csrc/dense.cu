@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(DENSE_TPB, 1) k_dense(const __grid_constant__ 
         __syncwarp();
     } else {
         // ---------------- epilogue ----------------
-        const float inv_beta = 1.0f / p.beta;
+        const SoftplusK spk = softplus_k(p.beta);
         const int q = warp & 3;                 // TMEM lane quadrant of this warp
         const int part = warp >> 2;             // which quarter of the columns this warp reads
         const int row = q * 32 + lane;
@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(DENSE_TPB, 1) k_dense(const __grid_constant__ 
 #pragma unroll
                             for (int k = 0; k < 8; ++k) {
                                 if constexpr (EPI == EPI_DRELU) v[j + k] = g[k] > 0.0f ? v[j + k] : 0.0f;
-                                else v[j + k] *= 1.0f - __expf(-p.beta * g[k]);
+                                else v[j + k] *= 1.0f - ex2_ftz(-g[k] * spk.c1);
                             }
                         }
                     } else {
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(DENSE_TPB, 1) k_dense(const __grid_constant__ 
                         for (int j = 0; j < CHUNK; ++j) {
                             const float z = v[j] + bias_s[c0 + j];
                             if constexpr (EPI == EPI_RELU) v[j] = fmaxf(z, 0.0f);
-                            else if constexpr (EPI == EPI_SOFTPLUS) v[j] = softplus_fast_h(z, p.beta, inv_beta);
+                            else if constexpr (EPI == EPI_SOFTPLUS) v[j] = softplus_fast_h(z, spk);
                             else v[j] = z;
                         }
                     }

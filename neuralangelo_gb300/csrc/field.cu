@@ -404,14 +404,14 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
         const int64_t s = s0 + sl_row;
         const bool keep = row < SPT * EVALS && s < p.Ns && e_row == 0;
         float part4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        const float inv_beta = 1.0f / p.beta;
+        const SoftplusK spk = softplus_k(p.beta);
 #pragma unroll 1
         for (int c0 = half * 128; c0 < half * 128 + 128; c0 += 32) {
             float v[32];
             umma::tmem_ld32(umma::taddr(tmem, q * 32, c0), v);
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
-                const float h = softplus_fast_h(v[j], p.beta, inv_beta);
+                const float h = softplus_fast_h(v[j], spk);
                 v[j] = h;
                 part4[j & 3] = fmaf(wh_s[c0 + j], h, part4[j & 3]);
             }
@@ -460,9 +460,7 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
                     const float* dv = p.ray_unit + 3 * r;
                     const float dx = dv[0], dy = dv[1], dz = dv[2];
                     const float xx = dx * dx, yy = dy * dy, zz = dz * dz;
-                    float col[48];
-#pragma unroll
-                    for (int k = 0; k < 48; ++k) col[k] = 0.0f;
+                    float col[22];
                     col[0] = c[0]; col[1] = c[1]; col[2] = c[2];
                     // real spherical-harmonic basis, degree <= 3 (spherical_harmonics.py:47-84)
                     col[3] = 0.28209479177387814f;
@@ -483,17 +481,28 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
                     col[18] = -0.5900435899266435f * dx * (xx - 3.0f * yy);
                     const float nrm = fmaxf(sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]), 1e-12f);
                     col[19] = g[0] / nrm; col[20] = g[1] / nrm; col[21] = g[2] / nrm;
-                    if (p.app_table && p.app_dim > 0) {
-                        const float* a = p.app_table + (int64_t)p.app_idx[r] * p.app_dim;
-                        for (int k = 0; k < p.app_dim && k < 26; ++k) col[22 + k] = a[k];
-                    }
+                    // this thread's 8 columns k = 8 kc8 + i: the 22 computed ones picked with
+                    // compile-time indices (col[] stays in registers), the appearance code read
+                    // straight from the table, and the last (padding) column a constant 1: the
+                    // colour layer-0 weight gradient dZ^T xc then carries the bias gradient there
+                    const float* a = (p.app_table && p.app_dim > 0)
+                                         ? p.app_table + (int64_t)p.app_idx[r] * p.app_dim
+                                         : nullptr;
                     __half* dst = (__half*)p.xc + ss * (int64_t)p.ldxc + HID;
                     const int ncol = p.ldxc - HID;
-                    // the last (padding) column is a constant 1: the colour layer-0 weight
-                    // gradient dZ^T xc then carries the bias gradient in that column
-                    col[ncol - 1] = 1.0f;
-                    store_half8(dst + 8 * kc8, col + 8 * kc8);
-                    (void)ncol;
+                    float o8[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const int k = 8 * kc8 + i;
+                        float val = 0.0f;
+#pragma unroll
+                        for (int cc = 0; cc < 22; ++cc)
+                            if (cc == k) val = col[cc];
+                        if (a && k >= 22 && k - 22 < p.app_dim) val = a[k - 22];
+                        if (k == ncol - 1) val = 1.0f;
+                        o8[i] = val;
+                    }
+                    store_half8(dst + 8 * kc8, o8);
                 }
             }
         }
@@ -718,15 +727,24 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         if (lane == 0) umma::bulk_wait_read0();      // the previous tile's d_enc store has read the buffer
         __syncwarp();
         {
+            // dead rows (past Ns, and rows 126-127) get d f = 0 and no d_h0c: their
+            // pre-activations are finite, so their d_pre and head terms come out 0
             const int64_t s = s0 + sl_row;
             const bool live = row < SPT * EVALS && s < p.Ns;
             const float df = live ? df_s[(it & 1) * (EVALS * SPT) + row] : 0.0f;
             const bool centre = live && e_row == 0;
-            const float inv_beta = 1.0f / p.beta;
+            const SoftplusK spk = softplus_k(p.beta);
+            // the next chunk's TMEM load is in flight while this chunk is processed
+            uint32_t rn[16];
+            umma::tmem_ld16_nowait(umma::taddr(tmem, q * 32, part * 64), rn);
+            umma::tmem_ld_wait16(rn);
 #pragma unroll 1
             for (int c0 = part * 64; c0 < part * 64 + 64; c0 += 16) {
                 float v[16];
-                umma::tmem_ld16(umma::taddr(tmem, q * 32, c0), v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(rn[j]);
+                const bool more = c0 + 16 < part * 64 + 64;
+                if (more) umma::tmem_ld16_nowait(umma::taddr(tmem, q * 32, c0 + 16), rn);
                 float dh0[16];
                 if (centre) {
                     const float4* src = reinterpret_cast<const float4*>(dh0_s + sl_row * DH0_LD + c0);
@@ -743,9 +761,9 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     float hval, sg;
-                    softplus_fast(v[j], p.beta, inv_beta, hval, sg);
-                    v[j] = live ? (df * wh_s[c0 + j] + dh0[j]) * sg : 0.0f;
-                    hc[j] = live ? df * hval : 0.0f;
+                    softplus_fast(v[j], spk, hval, sg);
+                    v[j] = fmaf(df, wh_s[c0 + j], dh0[j]) * sg;
+                    hc[j] = df * hval;
                 }
                 {
                     const float colsum = warp_column_sum16(hc, lane);
@@ -760,6 +778,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
                     hi[i] = *reinterpret_cast<const uint32_t*>(&h2);
                     lo[i] = *reinterpret_cast<const uint32_t*>(&l2);
                 }
+                if (more) umma::tmem_ld_wait16(rn);
                 umma::tmem_st8(umma::taddr(t_hi, q * 32, c0 / 2), hi);
                 umma::tmem_st8(umma::taddr(t_lo, q * 32, c0 / 2), lo);
                 // d_pre0 (hi) into the staging rows; dead samples store zeros (their x0ext
@@ -901,7 +920,7 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_sdf_points(FieldParams p, 
     const uint32_t idesc = umma::idesc_f16(TILE_M, HID);
     const uint32_t a_addr = umma::smem_u32(a_s), a2_addr = umma::smem_u32(a2_s), w_addr = umma::smem_u32(w_s);
     const float bhead = p.bhead[0];
-    const float inv_beta = 1.0f / p.beta;
+    const SoftplusK spk = softplus_k(p.beta);
     const int64_t ntiles = (q.M + TILE_M - 1) / TILE_M;
     const int qd = warp & 3, half = warp >> 2;
     const int row = qd * 32 + lane;
@@ -959,7 +978,7 @@ __global__ void __launch_bounds__(FIELD_THREADS, 1) k_sdf_points(FieldParams p, 
             for (int j = 0; j < 32; ++j) {
                 const int n = c0 + j;
                 const float z = v[j] + w0x_s[3 * n] * x[0] + w0x_s[3 * n + 1] * x[1] + w0x_s[3 * n + 2] * x[2] + b0_s[n];
-                part4[j & 3] = fmaf(wh_s[n], softplus_fast_h(z, p.beta, inv_beta), part4[j & 3]);
+                part4[j & 3] = fmaf(wh_s[n], softplus_fast_h(z, spk), part4[j & 3]);
             }
         }
         part_s[half * TILE_M + row] = (part4[0] + part4[1]) + (part4[2] + part4[3]);
