@@ -62,7 +62,7 @@ def profiled_traffic(kernel):
 
 
 # kernels of this library launched by one call of each entry point (cuBLAS excluded)
-KERNELS_PER_CALL = {"gbsdf_field_fwd": 2, "gbsdf_field_bwd": 2, "gbsdf_gemm_wgrad": 0}
+KERNELS_PER_CALL = {"gbsdf_field_fwd": 2, "gbsdf_field_bwd": 2, "gbsdf_gemm_wgrad": 0}   # others: 1
 
 
 # --------------------------------------------------------------------------- extra workloads
@@ -367,33 +367,60 @@ def main():
     e2e_ms = max_over_ranks(e2e_ms)
 
     # per-kernel algorithmic work (bytes, flops) of one launch, for the roofline
+    # Bytes: what each launch must move per sample (table corners counted at every
+    # touch, as the encoder's algorithmic figure does; L2 serves many of them).
+    # FLOPs: the algorithmic MACs x 2 of the layer-0 GEMMs (no hi/lo doubling).
     F, A, H = 8, ACTIVE, 256
+    K0 = 16 * ((A * F + 15) // 16)
+    KX = 2 * K0 + 16                                     # x0ext row: features hi | tail | lo
     enc_read = A * 8 * F * (2 if mode == "fused" else 4)
     work = {
         "gbsdf_hashgrid_fwd": (n_samples * (A * 8 * F * 4 + 16 * F * 4 + 12), 0),
         "gbsdf_hashgrid_bwd": (n_samples * (A * 8 * F * 8 + 16 * F * 4), 0),
-        "gbsdf_field_fwd": (n_samples * (7 * enc_read + H * 2 + 48 * 2 + 28 + 12), n_samples * 7 * 2 * 64 * H),
-        "gbsdf_field_bwd": (n_samples * (7 * enc_read + 7 * A * 8 * F * 8 + 7 * H * 2 + 7 * 80 * 2 + H * 2 + 64 + 64),
-                            n_samples * 7 * 3 * 2 * 64 * H),
+        # table corners of 7 evaluations -> x0ext rows
+        "gbsdf_field_encode": (n_samples * (7 * enc_read + 7 * KX * 2 + 4), 0),
+        # x0ext rows -> SDF, gradient, Hessian, h0c row, colour-input tail
+        "gbsdf_field_mlp_fwd": (n_samples * (7 * KX * 2 + 4 + 12 + 12 + (H + 8) * 2 + 48 * 2),
+                                n_samples * 7 * 2 * H * (K0 + 4 + 1)),
+        # x0ext rows, d_h0c and the per-sample output gradients -> d_pre0 (fp16), d_enc (fp32)
+        "gbsdf_field_mlp_bwd": (n_samples * (7 * KX * 2 + H * 4 + 52 + 7 * H * 2 + 7 * K0 * 4),
+                                n_samples * 7 * 2 * H * (2 * K0 + 4 + 1)),
+        # d_enc -> FP32 read-modify-write of every corner touch
+        "gbsdf_field_scatter": (n_samples * (7 * K0 * 4 + 7 * A * 8 * F * 8 + 4), 0),
     }
-    dom = max(ksum.items(), key=lambda kv: kv[1][1]) if ksum else None
-    roof = None
-    if dom is not None:
-        name, (calls, tot_ms) = dom
+    tensor_peak = peaks.get("bf16_tflops_sustained", 1700.0)
+
+    def roofline_of(name, calls, tot_ms):
+        """The binding roofline of one call: HBM (algorithmic bytes / measured copy
+        bandwidth) or tensor (algorithmic FLOPs / measured sustained bf16 rate),
+        whichever floor is longer."""
         per_launch_ms = tot_ms / calls
-        if name in work:
-            by, fl = work[name]
-            ach = by / (per_launch_ms * 1e-3) / 1e9
-            tps, tsrc = profiled_traffic(name)
-            traffic = round(tps * n_samples) if tps is not None else None
-            roof = dict(kernel=name, bound="hbm", achieved=round(ach, 1), peak=hbm_peak, unit="GB/s",
-                        frac=round(ach / hbm_peak, 4), traffic=traffic, traffic_source=tsrc,
-                        dram_gbs=round(traffic / (per_launch_ms * 1e-3) / 1e9, 1) if traffic else None,
-                        per_launch_ms=round(per_launch_ms, 4),
-                        algorithmic_bytes_per_launch=by, flops_per_launch=fl,
-                        tensor_tflops=round(fl / (per_launch_ms * 1e-3) / 1e12, 2),
-                        launches_per_step=calls / args.steps,
-                        peak_source="MEASURED_PEAKS.json hbm_gbs (burst, of measured)")
+        by, fl = work[name]
+        t = per_launch_ms * 1e-3
+        hbm_floor, tensor_floor = by / (hbm_peak * 1e9), fl / (tensor_peak * 1e12)
+        if tensor_floor > hbm_floor:
+            r = dict(kernel=name, bound="tensor", achieved=round(fl / t / 1e12, 2), peak=tensor_peak,
+                     unit="TFLOP/s", frac=round(fl / t / 1e12 / tensor_peak, 4),
+                     peak_source="MEASURED_PEAKS.json bf16_tflops_sustained (of measured)")
+        else:
+            r = dict(kernel=name, bound="hbm", achieved=round(by / t / 1e9, 1), peak=hbm_peak, unit="GB/s",
+                     frac=round(by / t / 1e9 / hbm_peak, 4),
+                     peak_source="MEASURED_PEAKS.json hbm_gbs (burst, of measured)")
+        tps, tsrc = profiled_traffic(name)
+        traffic = round(tps * n_samples) if tps is not None else None
+        r.update(traffic=traffic, traffic_source=tsrc,
+                 dram_gbs=round(traffic / t / 1e9, 1) if traffic else None,
+                 per_launch_ms=round(per_launch_ms, 4), algorithmic_bytes_per_launch=by, flops_per_launch=fl,
+                 tensor_tflops=round(fl / t / 1e12, 2), launches_per_step=calls / args.steps)
+        return r
+
+    timed = [(k, v) for k, v in ksum.items() if k in work]
+    dom = max(timed, key=lambda kv: kv[1][1]) if timed else None
+    roof = roofline_of(dom[0], *dom[1]) if dom else None
+    # the same for every timed field kernel (the dominant one is `roofline`)
+    rooflines = {k: {x: y for x, y in roofline_of(k, *v).items()
+                     if x in ("bound", "achieved", "unit", "frac", "per_launch_ms", "dram_gbs")}
+                 for k, v in timed}
     launches = int(sum(c * KERNELS_PER_CALL.get(k, 1) for k, (c, _) in ksum.items()) / args.steps)
     extras = {}
     if not args.no_extras and fused is not None:
@@ -423,6 +450,7 @@ def main():
                     flops_per_sample=flops_per_sample(model.cfg, ACTIVE),
                     encoder_bytes_per_sample=encoder_bytes_per_sample(ACTIVE, 8, 4),
                     kernel_ms_per_step={k: round(v[1] / args.steps, 4) for k, v in ksum.items()},
+                    kernel_rooflines=rooflines,
                     **extras)
         print(json.dumps(line), flush=True)
     if world > 1:

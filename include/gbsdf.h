@@ -200,8 +200,18 @@ typedef struct gbsdf_field_args {
 } gbsdf_field_args;
 
 size_t gbsdf_field_args_size(void);
+/* Forward: hash-grid gather of the 7 evaluations into x0ext, then the MLP forward
+ * (NeuralSDF.forward + compute_gradients, modules.py:68-74,132-156). */
 int gbsdf_field_fwd(const gbsdf_field_args* args, void* stream);
+/* Backward: the MLP backward into d_enc / d_pre0 / d_whead / d_bhead, then the table-
+ * gradient scatter into d_table (the tcnn.Encoding backward behind modules.py:85). */
 int gbsdf_field_bwd(const gbsdf_field_args* args, void* stream);
+/* The same four kernels one at a time, in step order (gbsdf_field_fwd = encode +
+ * mlp_fwd, gbsdf_field_bwd = mlp_bwd + scatter), so each can be timed on its own. */
+int gbsdf_field_encode(const gbsdf_field_args* args, void* stream);
+int gbsdf_field_mlp_fwd(const gbsdf_field_args* args, void* stream);
+int gbsdf_field_mlp_bwd(const gbsdf_field_args* args, void* stream);
+int gbsdf_field_scatter(const gbsdf_field_args* args, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Fused per-ray rendering forward + backward: NeuS alpha (model.py:275-298),

@@ -156,8 +156,10 @@ __device__ void stage_encoding(const FieldParams& p, int64_t s0, uint8_t* a_s, u
 // columns [l F, l F + F) as fp16 hi and, at K0 + 16 + l F, the fp16 residual lo;
 // the level-0 thread also writes the 16-column tail after the hi features and
 // zeroes the padding columns.  Rows of samples past the end are zeros.
+// Six blocks per SM (at most 40 registers): the gather waits on L2 latency, and the
+// extra resident warps keep more corner loads in flight.
 template <int F>
-__global__ void __launch_bounds__(256) k_field_gather(FieldParams p, int64_t ntiles) {
+__global__ void __launch_bounds__(256, 6) k_field_gather(FieldParams p, int64_t ntiles) {
     const int A = p.active, K0 = p.K0, KX = 2 * K0 + 16;
     // 32-bit index arithmetic: the launcher checks rows * A < 2^32
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1010,16 +1012,13 @@ static size_t bwd_smem(int K0) {
     return need > BWD_SMEM_FLOOR ? need : BWD_SMEM_FLOOR;
 }
 
+// The field's four kernels, in step order.  `which`: bit 0 the hash-grid gather,
+// bit 1 the MLP forward, bit 2 the MLP backward, bit 3 the table-gradient scatter.
+enum FieldKernels : int { FK_GATHER = 1, FK_MLP_FWD = 2, FK_MLP_BWD = 4, FK_SCATTER = 8 };
+
 template <int F>
-static int launch_field(const FieldParams& p, bool backward, cudaStream_t s) {
-    const size_t smem = backward ? bwd_smem(p.K0) : fwd_smem(p.K0);
-    if (smem > 227 * 1024) {
-        set_error("field kernel needs %zu B of shared memory", smem);
-        return GBSDF_ERR_UNSUPPORTED;
-    }
+static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
     const int64_t ntiles = (p.Ns + SPT - 1) / SPT;
-    int64_t grid = num_sms() * (backward ? 1 : FWD_CTAS_PER_SM);
-    if (grid > ntiles) grid = ntiles;
     // largest thread index: gather ntiles * 126 * active, scatter Ns * active * 8
     const int64_t gather_items = ntiles * (SPT * EVALS) * (int64_t)p.active;
     const int64_t scatter_items = p.Ns * (int64_t)p.active * 8;
@@ -1028,7 +1027,29 @@ static int launch_field(const FieldParams& p, bool backward, cudaStream_t s) {
                   p.active);
         return GBSDF_ERR_UNSUPPORTED;
     }
-    if (backward) {
+    if (which & FK_GATHER) {
+        const int64_t items = ntiles * (SPT * EVALS) * p.active;
+        k_field_gather<F><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p, ntiles);
+        if (int st = launch_status("field gather")) return st;
+    }
+    if (which & FK_MLP_FWD) {
+        const size_t smem = fwd_smem(p.K0);
+        if (smem > 227 * 1024) {
+            set_error("field forward needs %zu B of shared memory", smem);
+            return GBSDF_ERR_UNSUPPORTED;
+        }
+        int64_t grid = num_sms() * FWD_CTAS_PER_SM;
+        if (grid > ntiles) grid = ntiles;
+        cudaFuncSetAttribute(k_field_fwd<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_field_fwd<F><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p);
+        if (int st = launch_status("field forward")) return st;
+    }
+    if (which & FK_MLP_BWD) {
+        const size_t smem = bwd_smem(p.K0);
+        if (smem > 227 * 1024) {
+            set_error("field backward needs %zu B of shared memory", smem);
+            return GBSDF_ERR_UNSUPPORTED;
+        }
         // d_pre0 [126 T, 256] fp16 and d_enc [126 T, K0] fp32 as TMA store targets
         const int64_t rows = ntiles * TILE_ROWS;
         if (rows >= ((int64_t)1 << 31)) {
@@ -1049,17 +1070,18 @@ static int launch_field(const FieldParams& p, bool backward, cudaStream_t s) {
         if (int st = tensor_map_2d(&tm_enc30, true, p.d_enc, rows, p.K0, p.K0, 16, 30, CU_TENSOR_MAP_SWIZZLE_64B, l2n,
                                    "d_enc"))
             return st;
+        int64_t grid = num_sms();
+        if (grid > ntiles) grid = ntiles;
         cudaFuncSetAttribute(k_field_bwd<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_field_bwd<F><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30);
+        if (int st = launch_status("field backward")) return st;
+    }
+    if (which & FK_SCATTER) {
         const int64_t items = p.Ns * p.active;
         k_field_scatter<F><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p);
-    } else {
-        const int64_t items = ntiles * (SPT * EVALS) * p.active;
-        k_field_gather<F><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p, ntiles);
-        cudaFuncSetAttribute(k_field_fwd<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_field_fwd<F><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p);
+        if (int st = launch_status("field scatter")) return st;
     }
-    return launch_status(backward ? "field_bwd" : "field_fwd");
+    return GBSDF_OK;
 }
 
 static int check_field_weights(const FieldParams& p) {
@@ -1086,42 +1108,69 @@ using namespace gbsdf;
 
 extern "C" size_t gbsdf_field_args_size(void) { return sizeof(gbsdf_field_args); }
 
-extern "C" int gbsdf_field_fwd(const gbsdf_field_args* params, void* stream) {
-    clear_error();
-    GBSDF_CHECK_ARG(params != nullptr, "params NULL");
-    const FieldParams& p = *params;
-    if (int st = check_field(p)) return st;
-    if (p.Ns == 0) return GBSDF_OK;
-    GBSDF_CHECK_ARG(p.sdf && p.grad && p.hess && p.h0c && p.x0ext, "NULL output");
-    GBSDF_CHECK_ARG(p.w0b && aligned(p.w0b, 16), "w0b (fp16 [256, K0 + 16]) missing or misaligned");
-    GBSDF_CHECK_ARG(p.ld_h0c == 0 || (p.ld_h0c >= HID && p.ld_h0c % 8 == 0), "ld_h0c %d", p.ld_h0c);
-    GBSDF_CHECK_ARG(!p.xc || (p.ldxc % 16 == 0 && p.ldxc - HID >= 23 + p.app_dim && p.ldxc - HID <= 48),
-                    "xc leading dimension %d (needs 256 + 23 + app_dim <= ldxc <= 304, multiple of 16)", p.ldxc);
-    GBSDF_CHECK_ARG(!p.xc || p.app_dim == 0 || (p.app_table && p.app_idx), "appearance table / index missing");
+static int field_dispatch(const FieldParams& p, int which, void* stream) {
     switch (p.grid.n_features) {
-        case 2: return launch_field<2>(p, false, as_stream(stream));
-        case 4: return launch_field<4>(p, false, as_stream(stream));
-        default: return launch_field<8>(p, false, as_stream(stream));
+        case 2: return launch_field<2>(p, which, as_stream(stream));
+        case 4: return launch_field<4>(p, which, as_stream(stream));
+        default: return launch_field<8>(p, which, as_stream(stream));
     }
 }
 
-extern "C" int gbsdf_field_bwd(const gbsdf_field_args* params, void* stream) {
+static int check_fwd(const FieldParams& p, int which) {
+    if (int st = check_field(p)) return st;
+    GBSDF_CHECK_ARG(p.x0ext, "NULL x0ext");
+    if (which & FK_MLP_FWD) {
+        GBSDF_CHECK_ARG(p.sdf && p.grad && p.hess && p.h0c, "NULL output");
+        GBSDF_CHECK_ARG(p.w0b && aligned(p.w0b, 16), "w0b (fp16 [256, K0 + 16]) missing or misaligned");
+        GBSDF_CHECK_ARG(p.ld_h0c == 0 || (p.ld_h0c >= HID && p.ld_h0c % 8 == 0), "ld_h0c %d", p.ld_h0c);
+        GBSDF_CHECK_ARG(!p.xc || (p.ldxc % 16 == 0 && p.ldxc - HID >= 23 + p.app_dim && p.ldxc - HID <= 48),
+                        "xc leading dimension %d (needs 256 + 23 + app_dim <= ldxc <= 304, multiple of 16)", p.ldxc);
+        GBSDF_CHECK_ARG(!p.xc || p.app_dim == 0 || (p.app_table && p.app_idx), "appearance table / index missing");
+    }
+    return GBSDF_OK;
+}
+
+static int check_bwd(const FieldParams& p, int which) {
+    if (int st = check_field(p)) return st;
+    GBSDF_CHECK_ARG(p.d_enc && aligned(p.d_enc, 16), "d_enc missing or misaligned");
+    if (which & FK_MLP_BWD) {
+        GBSDF_CHECK_ARG(p.w0b && aligned(p.w0b, 16), "w0b (fp16 [256, K0 + 16]) missing or misaligned");
+        GBSDF_CHECK_ARG(p.grad && p.d_sdf && p.d_grad && p.d_hess && p.d_xc && p.d_h0c && p.d_pre0 && p.x0ext &&
+                            p.d_whead && p.d_bhead,
+                        "NULL pointer");
+        GBSDF_CHECK_ARG(aligned(p.d_pre0, 16) && aligned(p.d_h0c, 16), "d_pre0 / d_h0c alignment");
+    }
+    if (which & FK_SCATTER) GBSDF_CHECK_ARG(p.d_table && aligned(p.d_table, 16), "d_table missing or misaligned");
+    return GBSDF_OK;
+}
+
+static int field_call(const gbsdf_field_args* params, int which, void* stream) {
     clear_error();
     GBSDF_CHECK_ARG(params != nullptr, "params NULL");
     const FieldParams& p = *params;
-    if (int st = check_field(p)) return st;
+    const bool fwd = (which & (FK_GATHER | FK_MLP_FWD)) != 0;
+    if (int st = fwd ? check_fwd(p, which) : check_bwd(p, which)) return st;
     if (p.Ns == 0) return GBSDF_OK;
-    GBSDF_CHECK_ARG(p.w0b && aligned(p.w0b, 16), "w0b (fp16 [256, K0 + 16]) missing or misaligned");
-    GBSDF_CHECK_ARG(p.grad && p.d_sdf && p.d_grad && p.d_hess && p.d_xc && p.d_h0c && p.d_table &&
-                        p.d_pre0 && p.x0ext && p.d_enc && p.d_whead && p.d_bhead,
-                    "NULL pointer");
-    GBSDF_CHECK_ARG(aligned(p.d_table, 16) && aligned(p.d_enc, 16) && aligned(p.d_pre0, 16),
-                    "d_table / d_enc / d_pre0 alignment");
-    switch (p.grid.n_features) {
-        case 2: return launch_field<2>(p, true, as_stream(stream));
-        case 4: return launch_field<4>(p, true, as_stream(stream));
-        default: return launch_field<8>(p, true, as_stream(stream));
-    }
+    return field_dispatch(p, which, stream);
+}
+
+extern "C" int gbsdf_field_fwd(const gbsdf_field_args* params, void* stream) {
+    return field_call(params, FK_GATHER | FK_MLP_FWD, stream);
+}
+extern "C" int gbsdf_field_bwd(const gbsdf_field_args* params, void* stream) {
+    return field_call(params, FK_MLP_BWD | FK_SCATTER, stream);
+}
+extern "C" int gbsdf_field_encode(const gbsdf_field_args* params, void* stream) {
+    return field_call(params, FK_GATHER, stream);
+}
+extern "C" int gbsdf_field_mlp_fwd(const gbsdf_field_args* params, void* stream) {
+    return field_call(params, FK_MLP_FWD, stream);
+}
+extern "C" int gbsdf_field_mlp_bwd(const gbsdf_field_args* params, void* stream) {
+    return field_call(params, FK_MLP_BWD, stream);
+}
+extern "C" int gbsdf_field_scatter(const gbsdf_field_args* params, void* stream) {
+    return field_call(params, FK_SCATTER, stream);
 }
 
 extern "C" int gbsdf_sdf_points(const gbsdf_field_args* params, int64_t M, const float* pts, const float* ax,

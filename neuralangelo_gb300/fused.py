@@ -56,8 +56,9 @@ class RenderArgs(ctypes.Structure):
 
 _lib.register("gbsdf_field_args_size", [])
 _lib.register("gbsdf_render_args_size", [])
-_lib.register("gbsdf_field_fwd", [c_vp, c_vp])
-_lib.register("gbsdf_field_bwd", [c_vp, c_vp])
+for _name in ("gbsdf_field_fwd", "gbsdf_field_bwd", "gbsdf_field_encode", "gbsdf_field_mlp_fwd",
+              "gbsdf_field_mlp_bwd", "gbsdf_field_scatter"):
+    _lib.register(_name, [c_vp, c_vp])
 _lib.register("gbsdf_render_fused", [c_vp, c_vp])
 _lib.register("gbsdf_rgb_head_fwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp])
 _lib.register("gbsdf_rgb_head_bwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp])
@@ -318,7 +319,8 @@ class FusedField:
         fa.x0ext = _p(ws['x0ext'])
         fa.err = _p(ws['err'])
         # ---------------- forward ----------------
-        _lib.call("gbsdf_field_fwd", ctypes.byref(fa), stream)
+        _lib.call("gbsdf_field_encode", ctypes.byref(fa), stream)     # = gbsdf_field_fwd in two calls
+        _lib.call("gbsdf_field_mlp_fwd", ctypes.byref(fa), stream)
         # SDF feature layer, written into the colour input's first 256 columns
         _dense(ws['h0c'], pk['w1'], 256, 256, ws['xc'], bias=pk['b1'], epi=EPI_SOFTPLUS, beta=fa.beta,
                err=ws['err'])
@@ -416,7 +418,8 @@ class FusedField:
         fa.d_h0c = _p(ws['d_h0c'])
         fa.d_table, fa.d_pre0, fa.d_enc = _p(d_table), _p(ws['d_pre0']), _p(ws['d_enc'])
         fa.d_whead, fa.d_bhead = _p(ws['d_whead']), _p(ws['d_bhead'])
-        _lib.call("gbsdf_field_bwd", ctypes.byref(fa), stream)
+        _lib.call("gbsdf_field_mlp_bwd", ctypes.byref(fa), stream)    # = gbsdf_field_bwd in two calls
+        _lib.call("gbsdf_field_scatter", ctypes.byref(fa), stream)
         gw0x = torch.empty(256, 2 * self.K0 + 16, **dev32)
         _wgrad(ws['d_pre0'], ws['x0ext'], 256, 2 * self.K0 + 16, gw0x)
         grads['w0ext'] = gw0x

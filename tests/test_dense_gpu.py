@@ -75,3 +75,44 @@ def test_dense_split_operand_and_output():
     e_hi = (hi.double() - R).norm() / R.norm()
     assert e_pair < 1e-5, float(e_pair)
     assert e_hi > 1e-4                       # a single fp16 output is much coarser
+
+
+@pytest.mark.parametrize("epi", [D.EPI_SOFTPLUS, D.EPI_DSOFTPLUS])
+def test_dense_fp32_softplus_epilogues_against_cuda_math(epi):
+    """The fused kernels' softplus(beta = 100) and its derivative (change of base to the
+    MUFU ex2 / lg2 / rcp approximations) against torch's softplus and exp (CUDA's
+    expf / log1pf) on the same FP32 pre-activations, with FP32 outputs so the FP16
+    storage of the fused path does not hide the function's own error.  The
+    pre-activations span the far tail (beta z ~ -40), the steep middle and torch's
+    identity threshold (beta z > 20)."""
+    M, K, N = 4096, 16, 128
+    g = torch.Generator(DEV).manual_seed(11 + epi)
+    X = (torch.randn(M, K, device=DEV, generator=g) * 0.5).half()
+    W = (torch.randn(N, K, device=DEV, generator=g) * 0.08).half()
+    b = torch.linspace(-0.4, 0.4, N, device=DEV)
+    beta = 100.0
+    G = None
+    if epi == D.EPI_DSOFTPLUS:   # a softplus output: positive, from ~1e-6 up to ~0.4
+        G = torch.nn.functional.softplus(torch.randn(M, N, device=DEV, generator=g) * 0.15, beta=beta).half()
+    out = torch.empty(M, N, device=DEV, dtype=torch.float32)
+    err = torch.zeros(1, dtype=torch.int32, device=DEV)
+    D.dense(X, W, b, epi=epi, beta=beta, G=G, out=out, err=err)
+    torch.cuda.synchronize()
+    assert int(err) == 0
+    z = X.float() @ W.float().t()
+    # the tensor core and torch sum the 16 products in different orders: an FP32
+    # difference of order 2^-24 sum |x w| that is absolute, not relative to |z|
+    zabs = X.float().abs() @ W.float().abs().t()
+    if epi == D.EPI_SOFTPLUS:
+        z = z + b
+        assert float((z * beta).min()) < -30 and float((z * beta).max()) > 25
+        R = torch.nn.functional.softplus(z, beta=beta)
+        # relative 1e-5, with an absolute floor for the lg2 approximation near 1 + e = 1
+        bound = 1e-5 * R.abs() + 2e-8 + 1e-6 * zabs
+    else:
+        R = z * (1 - torch.exp(-beta * G.float()))
+        # 1 - e^(-beta g) cancels for small g: the ex2 approximation's ~2^-22 error on e
+        # is then absolute, relative to |z|
+        bound = 1e-5 * R.abs() + 5e-7 * z.abs() + 1e-6 * zabs
+    excess = ((out - R).abs() - bound).max()
+    assert float(excess) <= 0.0, float(excess)

@@ -185,6 +185,37 @@ def test_fused_matches_plain_full_table():
         assert rel(mine[k], ref[k]) < 2e-2, k
 
 
+def test_combined_field_entry_points_match_split_calls(monkeypatch):
+    """gbsdf_field_fwd / gbsdf_field_bwd (two kernels each) give the step that the four
+    single-kernel calls give."""
+    from neuralangelo_gb300 import _lib
+    model = build()
+    batch = make_rays(32, 32, seed=2, n_images=10, device=DEV)
+    ff = FusedField(model)
+    model.zero_grad(set_to_none=True)
+    a = ff.step(batch)['loss']
+    g1 = {k: v.clone() for k, v in fused_grads(model).items()}
+    real = _lib.call
+    seen = []
+
+    def combined(name, *args):
+        if name in ("gbsdf_field_encode", "gbsdf_field_scatter"):
+            return None                                  # part of the combined call below
+        name = {"gbsdf_field_mlp_fwd": "gbsdf_field_fwd", "gbsdf_field_mlp_bwd": "gbsdf_field_bwd"}.get(name, name)
+        seen.append(name)
+        return real(name, *args)
+
+    monkeypatch.setattr(_lib, "call", combined)
+    model.zero_grad(set_to_none=True)
+    b = ff.step(batch)['loss']
+    torch.cuda.synchronize()
+    assert "gbsdf_field_fwd" in seen and "gbsdf_field_bwd" in seen
+    assert abs(a - b) < 1e-6 * abs(a)
+    g2 = fused_grads(model)
+    for k in ('table', 'sdf.l0.v', 'sdf.head.w', 'rgb.l0.v'):
+        assert rel(g2[k].cpu(), g1[k].cpu()) < 1e-5, k          # atomics reorder only
+
+
 def test_fused_second_step_reuses_workspace():
     model = build()
     batch = make_rays(32, 16, seed=1, n_images=10, device=DEV)
