@@ -41,6 +41,8 @@ def parse():
     p.add_argument("--samples", type=int, default=N_SAMPLES)
     p.add_argument("--no-extras", action="store_true",
                    help="skip the ragged-batching, sampler and mesh measurements")
+    p.add_argument("--split-colour-grads", action="store_true",
+                   help="carry the colour MLP's input gradients as fp16 hi+lo pairs")
     return p.parse_args()
 
 
@@ -323,7 +325,7 @@ def main():
     fused = None
     if args.mode in ("auto", "fused"):
         from neuralangelo_gb300.fused import FusedField
-        fused = FusedField(model)
+        fused = FusedField(model, split_colour_grads=args.split_colour_grads)
     mode = "fused" if fused is not None else "plain"
 
     def step_fused(b, compute_loss=False):
@@ -442,6 +444,7 @@ def main():
                     speedup_vs_plain=round(plain_ms / ms, 3) if plain_ms == plain_ms else None,
                     config=dict(workload=f"full field L16 F8 T2^22 (8 active), {R} rays x {N} samples, mode={mode}",
                                 rays=R, samples_per_ray=N, active_levels=ACTIVE, mode=mode,
+                                split_colour_grads=bool(args.split_colour_grads),
                                 l2="inputs larger than L2 (1.46 GB table)", parallelism="replicas"),
                     e2e=dict(value=round(world * n_samples / (e2e_ms * 1e-3), 1), unit="samples/s",
                              h2d_bytes_per_step=h2d, d2h_bytes_per_step=32 if fused is not None else 4,

@@ -215,12 +215,15 @@ __global__ void __launch_bounds__(256, 6) k_field_gather(FieldParams p, int64_t 
 }
 
 // Table gradient of one (sample, level) over the sample's 7 evaluations: each
-// evaluation's grid position is computed once and its 8 corners are accumulated in
+// evaluation's grid position is computed and its corners are accumulated in
 // registers, merging consecutive evaluations that hit the same entry of a corner
 // (the taps are eps apart: at coarse levels all 7 usually share the cell) before the
-// vector atomics.
-template <int F>
-__global__ void __launch_bounds__(256) k_field_scatter(FieldParams p) {
+// vector atomics.  The 8 corners go in passes of CPT (the positions and d_enc rows
+// are read again per pass, from L1): fewer accumulator registers, more resident warps.
+constexpr int SCATTER_CPT = 2;
+
+template <int F, int CPT>
+__global__ void __launch_bounds__(256, CPT >= 8 ? 2 : (CPT == 4 ? 3 : 4)) k_field_scatter(FieldParams p) {
     const int A = p.active, K0 = p.K0;
     // 32-bit index arithmetic: the launcher checks Ns * active * 8 < 2^32
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -235,83 +238,86 @@ __global__ void __launch_bounds__(256) k_field_scatter(FieldParams p) {
     const LevelDesc d = level_desc(p.grid, l);
     float* base = p.d_table + d.offset * F;
     const float gscale = p.d_table_scale != 0.0f ? p.d_table_scale : 1.0f;
-    uint32_t pidx[8];
-    float pacc[8][F];
-#pragma unroll
-    for (int cc = 0; cc < 8; ++cc) {
-        pidx[cc] = 0xffffffffu;
-#pragma unroll
-        for (int f = 0; f < F; ++f) pacc[cc][f] = 0.0f;
-    }
-#pragma unroll 1
-    for (int e = 0; e < EVALS; ++e) {
-        float x[3], xu[3];
-        eval_point(c, e, p.eps, x);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) xu[k] = to_unit(x[k]);
-        uint32_t bx, by, bz;
-        float fx, fy, fz;
-        grid_pos(d.scale, xu[0], bx, fx);
-        grid_pos(d.scale, xu[1], by, fy);
-        grid_pos(d.scale, xu[2], bz, fz);
-        const float* dv = p.d_enc + (t * (SPT * EVALS) + e * SPT + sl) * (int64_t)K0 + l * F;
-        float g[F];
-        if constexpr (F % 4 == 0) {
-#pragma unroll
-            for (int f = 0; f < F; f += 4) {
-                const float4 q4 = __ldg(reinterpret_cast<const float4*>(dv + f));
-                g[f] = q4.x; g[f + 1] = q4.y; g[f + 2] = q4.z; g[f + 3] = q4.w;
-            }
-        } else {
-#pragma unroll
-            for (int f = 0; f < F; ++f) g[f] = __ldg(dv + f);
-        }
-#pragma unroll
-        for (int f = 0; f < F; ++f) g[f] *= gscale;
-#pragma unroll
-        for (int cc = 0; cc < 8; ++cc) {
-            const uint32_t idx = grid_index(d, bx + (cc & 1), by + ((cc >> 1) & 1), bz + ((cc >> 2) & 1));
-            const float w = corner_weight(cc, fx, fy, fz);
-            if (idx != pidx[cc]) {
-                if (pidx[cc] != 0xffffffffu) scatter_add<F>(base + (uint64_t)pidx[cc] * F, pacc[cc]);
-                pidx[cc] = idx;
-#pragma unroll
-                for (int f = 0; f < F; ++f) pacc[cc][f] = 0.0f;
-            }
-#pragma unroll
-            for (int f = 0; f < F; ++f) pacc[cc][f] = fmaf(w, g[f], pacc[cc][f]);
-        }
-    }
+    const int lane = threadIdx.x & 31;
     // Final flush.  With 8 active levels the lanes l, l + 8, l + 16, l + 24 of a warp hold
     // level l of four consecutive samples, which at coarse levels often end in the same
     // cell.  Two xor-shuffle steps merge equal entries: two lanes merge only when both
     // still own their sums, the lower lane absorbing the upper one's, so every
     // contribution is written exactly once.  Only whole live warps take part (Ns * 8 a
     // multiple of 32), so no lane has left the kernel.
-    const int lane = threadIdx.x & 31;
     const bool grouped = A == 8 && (((uint32_t)p.Ns * 8u) & 31u) == 0u;
+#pragma unroll 1
+    for (int c0 = 0; c0 < 8; c0 += CPT) {
+        uint32_t pidx[CPT];
+        float pacc[CPT][F];
 #pragma unroll
-    for (int cc = 0; cc < 8; ++cc) {
-        bool mine = true;
-        if (grouped) {
+        for (int cc = 0; cc < CPT; ++cc) {
+            pidx[cc] = 0xffffffffu;
 #pragma unroll
-            for (int off = 8; off <= 16; off <<= 1) {
-                const uint32_t other_idx = __shfl_xor_sync(0xffffffffu, pidx[cc], off);
-                const bool other_mine = __shfl_xor_sync(0xffffffffu, mine ? 1 : 0, off) != 0;
-                float other[F];
+            for (int f = 0; f < F; ++f) pacc[cc][f] = 0.0f;
+        }
+#pragma unroll 1
+        for (int e = 0; e < EVALS; ++e) {
+            float x[3], xu[3];
+            eval_point(c, e, p.eps, x);
 #pragma unroll
-                for (int f = 0; f < F; ++f) other[f] = __shfl_xor_sync(0xffffffffu, pacc[cc][f], off);
-                if (mine && other_mine && other_idx == pidx[cc]) {
-                    if ((lane & off) == 0) {
+            for (int k = 0; k < 3; ++k) xu[k] = to_unit(x[k]);
+            uint32_t bx, by, bz;
+            float fx, fy, fz;
+            grid_pos(d.scale, xu[0], bx, fx);
+            grid_pos(d.scale, xu[1], by, fy);
+            grid_pos(d.scale, xu[2], bz, fz);
+            const float* dv = p.d_enc + (t * (SPT * EVALS) + e * SPT + sl) * (int64_t)K0 + l * F;
+            float g[F];
+            if constexpr (F % 4 == 0) {
 #pragma unroll
-                        for (int f = 0; f < F; ++f) pacc[cc][f] += other[f];
-                    } else {
-                        mine = false;
+                for (int f = 0; f < F; f += 4) {
+                    const float4 q4 = __ldg(reinterpret_cast<const float4*>(dv + f));
+                    g[f] = q4.x; g[f + 1] = q4.y; g[f + 2] = q4.z; g[f + 3] = q4.w;
+                }
+            } else {
+#pragma unroll
+                for (int f = 0; f < F; ++f) g[f] = __ldg(dv + f);
+            }
+#pragma unroll
+            for (int cc = 0; cc < CPT; ++cc) {
+                const int corner = c0 + cc;
+                const uint32_t idx =
+                    grid_index(d, bx + (corner & 1), by + ((corner >> 1) & 1), bz + ((corner >> 2) & 1));
+                const float w = corner_weight(corner, fx, fy, fz) * gscale;
+                if (idx != pidx[cc]) {
+                    if (pidx[cc] != 0xffffffffu) scatter_add<F>(base + (uint64_t)pidx[cc] * F, pacc[cc]);
+                    pidx[cc] = idx;
+#pragma unroll
+                    for (int f = 0; f < F; ++f) pacc[cc][f] = 0.0f;
+                }
+#pragma unroll
+                for (int f = 0; f < F; ++f) pacc[cc][f] = fmaf(w, g[f], pacc[cc][f]);
+            }
+        }
+#pragma unroll
+        for (int cc = 0; cc < CPT; ++cc) {
+            bool mine = true;
+            if (grouped) {
+#pragma unroll
+                for (int off = 8; off <= 16; off <<= 1) {
+                    const uint32_t other_idx = __shfl_xor_sync(0xffffffffu, pidx[cc], off);
+                    const bool other_mine = __shfl_xor_sync(0xffffffffu, mine ? 1 : 0, off) != 0;
+                    float other[F];
+#pragma unroll
+                    for (int f = 0; f < F; ++f) other[f] = __shfl_xor_sync(0xffffffffu, pacc[cc][f], off);
+                    if (mine && other_mine && other_idx == pidx[cc]) {
+                        if ((lane & off) == 0) {
+#pragma unroll
+                            for (int f = 0; f < F; ++f) pacc[cc][f] += other[f];
+                        } else {
+                            mine = false;
+                        }
                     }
                 }
             }
+            if (mine) scatter_add<F>(base + (uint64_t)pidx[cc] * F, pacc[cc]);
         }
-        if (mine) scatter_add<F>(base + (uint64_t)pidx[cc] * F, pacc[cc]);
     }
 }
 
@@ -1078,7 +1084,7 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
     }
     if (which & FK_SCATTER) {
         const int64_t items = p.Ns * p.active;
-        k_field_scatter<F><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p);
+        k_field_scatter<F, SCATTER_CPT><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p);
         if (int st = launch_status("field scatter")) return st;
     }
     return GBSDF_OK;

@@ -157,8 +157,9 @@ class FusedField:
     def __init__(self, model, loss_scale=2.0 ** 15, split_colour_grads=False):
         check_struct_sizes()
         self.model = model
-        # carry the colour MLP's input gradients as fp16 hi+lo pairs (costs ~10% of the step;
-        # the dominant colour-gradient error comes from fp16 activation storage instead)
+        # carry the colour MLP's input gradients as fp16 hi+lo pairs (costs ~9% of the step and
+        # leaves the weight-gradient error unchanged: that comes from fp16 storage of the
+        # forward activations, whose rounding moves ReLU gates near zero)
         self.split = bool(split_colour_grads)
         self.loss_scale = float(loss_scale)
         sdf = model.neural_sdf
