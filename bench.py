@@ -130,9 +130,26 @@ def bench_mesh(model, device, res=512, block_res=128):
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     pts = (res + (res // block_res - 1)) ** 3          # lattice points incl. the block overlaps
+    # output stage (extract_mesh.py:96-100): weld across blocks, transform, degenerate
+    # faces on the GPU; then the PLY file
+    import tempfile
+    from neuralangelo_gb300.mesh import finalize_mesh, write_ply
+    V = torch.from_numpy(mesh.vertices).to(device)
+    F = torch.from_numpy(mesh.faces).to(device)
+    finalize_mesh(V[:1000], F[:0], weld=True)                            # warm-up
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    Vo, Fo = finalize_mesh(V, F, weld=True, scale=1.0, offset=(0.0, 0.0, 0.0))
+    torch.cuda.synchronize()
+    t_fin = time.perf_counter() - t1
+    with tempfile.TemporaryDirectory() as d:
+        t2 = time.perf_counter()
+        write_ply(os.path.join(d, "mesh.ply"), Vo.cpu().numpy(), Fo.cpu().numpy())
+        t_ply = time.perf_counter() - t2
     return dict(resolution=res, block_res=block_res, seconds=round(dt, 4), lattice_points=pts,
                 points_per_s=round(pts / dt, 1), vertices=int(mesh.vertices.shape[0]),
-                faces=int(mesh.faces.shape[0]))
+                faces=int(mesh.faces.shape[0]), welded_vertices=int(Vo.shape[0]),
+                finalize_seconds=round(t_fin, 5), ply_write_seconds=round(t_ply, 4))
 
 
 # --------------------------------------------------------------------------- CPU baseline

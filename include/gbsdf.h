@@ -300,6 +300,23 @@ int gbsdf_mc_block(const float* vol, int nx, int ny, int nz, double iso, const d
                    void* workspace, size_t ws_bytes, double* V, int64_t V_cap, int64_t* F, int64_t F_cap,
                    int64_t* counts, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Mesh output stage (scripts/extract_mesh.py:96-97 after utils/mesh.py:121-129 and
+ * :43-46): optional vertex weld (coordinates equal after round-half-even of v *
+ * weld_mult, e.g. 1e8 for trimesh's 8-digit merge; first occurrence kept), then
+ * V * scale + offset, then faces re-indexed and those whose two heights
+ * 2A/|v1-v0|, 2A/|v2-v0| are not both > min_side dropped (min_side 0: only faces that
+ * repeat a vertex index; min_side < 0: none, as trimesh's per-block merge keeps them).  V [nv,3] float64 and F [nf,3] int64 are device
+ * inputs; V_out [>= nv,3], F_out [>= nf,3] device outputs; counts [2] (vertices,
+ * faces) device int64.  The caller owns a 256-byte aligned device workspace of
+ * gbsdf_mesh_finalize_workspace_size(nv, nf) bytes.  err (device int, optional) gets
+ * 3 if a hash probe ran past the table, 4 for a face index outside [0, nv). */
+size_t gbsdf_mesh_finalize_workspace_size(int64_t nv, int64_t nf);
+int gbsdf_mesh_finalize(const double* V, int64_t nv, const int64_t* F, int64_t nf, int weld, double weld_mult,
+                        double scale, const double* offset, double min_side, void* workspace,
+                        size_t workspace_bytes, double* V_out, int64_t* F_out, int64_t* counts, int* err,
+                        void* stream);
+
 /* Marching cubes of one block without any device allocation (no counterpart in
  * the reference).  For callers that cannot allocate device memory -- a host
  * application that owns the device budget and forbids allocations after

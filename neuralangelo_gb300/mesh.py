@@ -23,7 +23,12 @@ _lib.register("gbsdf_mc_table", [c_vp, c_vp])
 _lib.register("gbsdf_mc_block_noalloc", [c_vp, c_i32, c_i32, c_i32, c_dbl, c_vp, c_dbl, c_vp, c_i64, c_vp, c_i64,
                                          c_vp, c_vp])
 
+_lib.register("gbsdf_mesh_finalize", [c_vp, c_i64, c_vp, c_i64, c_i32, c_dbl, c_dbl, c_vp, c_dbl, c_vp, c_sz, c_vp,
+                                      c_vp, c_vp, c_vp, c_vp])
+
 NOALLOC_MAX_POINTS = 33
+MERGE_DIGITS = 8          # trimesh's merge tolerance, 1e-8
+MERGE_TOL = 1e-8
 
 
 def marching_cubes_noalloc(vol, origin, intv, V, F, counts, iso=0.0):
@@ -118,13 +123,109 @@ class Mesh:
         self.faces = faces
 
 
+def finalize_mesh(V, F, weld=False, digits=MERGE_DIGITS, scale=1.0, offset=(0.0, 0.0, 0.0), min_side=MERGE_TOL):
+    """gbsdf_mesh_finalize on device tensors V [nv,3] float64, F [nf,3] int64:
+    optional weld (coordinates equal at ``digits`` decimals, first occurrence kept)
+    -> V * scale + offset -> faces re-indexed, degenerate ones dropped (min_side > 0:
+    both heights 2A/|v1-v0|, 2A/|v2-v0| must exceed it; 0: only repeated indices;
+    < 0: none).  Returns (V', F') device tensors."""
+    _lib.require_cuda(V, F)
+    V = V.contiguous().to(torch.float64)
+    F = F.contiguous().to(torch.int64)
+    nv, nf = V.shape[0], F.shape[0]
+    lib = _lib.load()
+    lib.gbsdf_mesh_finalize_workspace_size.restype = c_sz
+    lib.gbsdf_mesh_finalize_workspace_size.argtypes = [c_i64, c_i64]
+    ws = torch.empty(int(lib.gbsdf_mesh_finalize_workspace_size(nv, nf)) + 256, dtype=torch.uint8, device=V.device)
+    pad = (-ws.data_ptr()) % 256
+    Vo = torch.empty(max(nv, 1), 3, dtype=torch.float64, device=V.device)
+    Fo = torch.empty(max(nf, 1), 3, dtype=torch.int64, device=V.device)
+    counts = torch.zeros(2, dtype=torch.int64, device=V.device)
+    err = torch.zeros(1, dtype=torch.int32, device=V.device)
+    off = (c_dbl * 3)(*[float(o) for o in offset])
+    _lib.call("gbsdf_mesh_finalize", c_vp(V.data_ptr()), nv, c_vp(F.data_ptr()), nf, 1 if weld else 0,
+              float(10 ** digits), float(scale), off, float(min_side), c_vp(ws.data_ptr() + pad), ws.numel() - pad,
+              c_vp(Vo.data_ptr()), c_vp(Fo.data_ptr()), c_vp(counts.data_ptr()), c_vp(err.data_ptr()),
+              _lib.stream_ptr(V.device))
+    if int(err.item()) != 0:
+        raise RuntimeError(f"gbsdf_mesh_finalize reported device error {int(err.item())}")
+    nv2, nf2 = counts.tolist()
+    return Vo[:nv2], Fo[:nf2]
+
+
+def write_ply(path, vertices, faces, colors=None):
+    """Binary little-endian PLY with the element layout of the reference's export
+    (trimesh, scripts/extract_mesh.py:100): float32 x y z [uchar red green blue alpha],
+    faces as a uchar count and three int32 indices."""
+    V = np.asarray(vertices, np.float64).reshape(-1, 3)
+    F = np.asarray(faces, np.int64).reshape(-1, 3)
+    vdt = [("xyz", "<f4", (3,))]
+    if colors is not None:
+        C = np.asarray(colors, np.uint8).reshape(len(V), -1)
+        if C.shape[1] == 3:
+            C = np.concatenate([C, np.full((len(V), 1), 255, np.uint8)], axis=1)
+        vdt.append(("rgba", "u1", (4,)))
+    vrec = np.empty(len(V), dtype=vdt)
+    vrec["xyz"] = V.astype(np.float32)
+    if colors is not None:
+        vrec["rgba"] = C
+    frec = np.empty(len(F), dtype=[("n", "u1"), ("idx", "<i4", (3,))])
+    frec["n"] = 3
+    frec["idx"] = F.astype(np.int32)
+    head = ["ply", "format binary_little_endian 1.0", "comment gbsdf mesh export", f"element vertex {len(V)}",
+            "property float x", "property float y", "property float z"]
+    if colors is not None:
+        head += ["property uchar red", "property uchar green", "property uchar blue", "property uchar alpha"]
+    head += [f"element face {len(F)}", "property list uchar int vertex_indices", "end_header"]
+    with open(path, "wb") as fh:
+        fh.write(("\n".join(head) + "\n").encode("ascii"))
+        fh.write(vrec.tobytes())
+        fh.write(frec.tobytes())
+
+
+def read_ply(path):
+    """The files write_ply makes: (vertices float32 [nv,3], faces int64 [nf,3], rgba or None)."""
+    with open(path, "rb") as fh:
+        data = fh.read()
+    end = data.index(b"end_header\n") + len(b"end_header\n")
+    lines = data[:end].decode("ascii").split("\n")
+    if lines[0] != "ply" or lines[1] != "format binary_little_endian 1.0":
+        raise ValueError("not a binary little-endian PLY")
+    nv = int(next(ln.split()[2] for ln in lines if ln.startswith("element vertex")))
+    nf = int(next(ln.split()[2] for ln in lines if ln.startswith("element face")))
+    has_rgba = "property uchar red" in lines
+    vdt = [("xyz", "<f4", (3,))] + ([("rgba", "u1", (4,))] if has_rgba else [])
+    vrec = np.frombuffer(data, dtype=vdt, count=nv, offset=end)
+    frec = np.frombuffer(data, dtype=[("n", "u1"), ("idx", "<i4", (3,))], count=nf,
+                         offset=end + vrec.nbytes)
+    if nf and not np.all(frec["n"] == 3):
+        raise ValueError("only triangle faces are supported")
+    return vrec["xyz"].copy(), frec["idx"].astype(np.int64), (vrec["rgba"].copy() if has_rgba else None)
+
+
+def export_mesh(mesh, path, sphere_radius=1.0, sphere_center=(0.0, 0.0, 0.0), device="cuda"):
+    """scripts/extract_mesh.py:96-100 on the GPU: vertices * sphere_radius +
+    sphere_center, drop the degenerate faces (trimesh's tolerance 1e-8), write the
+    PLY.  Returns the exported Mesh."""
+    V = torch.as_tensor(np.asarray(mesh.vertices, np.float64), device=device).reshape(-1, 3)
+    F = torch.as_tensor(np.asarray(mesh.faces, np.int64), device=device).reshape(-1, 3)
+    Vo, Fo = finalize_mesh(V, F, weld=False, scale=sphere_radius, offset=sphere_center, min_side=MERGE_TOL)
+    out = Mesh(Vo.cpu().numpy(), Fo.cpu().numpy())
+    write_ply(path, out.vertices, out.faces)
+    return out
+
+
 def lattice_axes(bounds, intv, device):
     """LatticeGrid axes: torch.arange(min, max, intv) in float32 (mesh.py:74-76)."""
     return [torch.arange(lo, hi, intv).to(device) for lo, hi in bounds]
 
 
-def extract_mesh(sdf_func, bounds, intv, block_res=64, texture_func=None, filter_lcc=False, device="cuda"):
-    """extract_mesh of the reference (mesh.py:25-49) on the GPU; returns a Mesh."""
+def extract_mesh(sdf_func, bounds, intv, block_res=64, texture_func=None, filter_lcc=False, device="cuda",
+                 merge_vertices=False):
+    """extract_mesh of the reference (mesh.py:25-49) on the GPU; returns a Mesh.
+    merge_vertices=True also runs the per-block vertex merge that the reference's
+    trimesh.Trimesh(V, F) applies (mesh.py:124-126: coordinates equal at 8 decimals),
+    keeping every face as trimesh does there."""
     if texture_func is not None or filter_lcc:
         raise NotImplementedError("texture and largest-component filtering are outside this path")
     axes = lattice_axes(bounds, intv, device)
@@ -147,6 +248,8 @@ def extract_mesh(sdf_func, bounds, intv, block_res=64, texture_func=None, filter
                 V, F = mc(vol, origin, intv)
                 if V.shape[0] == 0:
                     continue
+                if merge_vertices:
+                    V, F = finalize_mesh(V, F, weld=True, min_side=-1.0)
                 Vs.append(V.cpu().numpy())
                 Fs.append(F.cpu().numpy() + off)
                 off += V.shape[0]

@@ -20,6 +20,10 @@ field.py      float64 torch restatement of NeuralSDF / NeuralRGB / NeuS alpha /
 mc.c          C restatement of iso-surface marching cubes used by
               projects/neuralangelo/utils/mesh.py:119-133 (PyMCubes, third
               party, unpinned: requirements.txt:23).
+mesh_out.py   numpy restatement of the mesh output stage: trimesh's per-block
+              vertex merge (utils/mesh.py:121-129), the centre/scale transform
+              and degenerate-face removal (scripts/extract_mesh.py:96-97);
+              trimesh is third party and absent, so parity is unpinned.
 sampler.py    restatement of the hierarchical sampler
               (projects/neuralangelo/model.py:232-267,
               projects/nerf/utils/nerf_util.py:20-68).

@@ -65,9 +65,11 @@ def block_slices(n_points, block_res):
     return [(b * block_res, min(b * block_res + block_res + 1, n_points)) for b in range(nb)]
 
 
-def extract_mesh_blocks(sdf_volume_fn, bounds, intv, block_res, iso=0.0):
+def extract_mesh_blocks(sdf_volume_fn, bounds, intv, block_res, iso=0.0, merge_vertices=False):
     """sdf_volume_fn(xs, ys, zs) -> float32 [len(xs), len(ys), len(zs)] (already negated
-    as extract_mesh.py:85 does).  Returns the concatenated (V, F) over blocks in order."""
+    as extract_mesh.py:85 does).  Returns the concatenated (V, F) over blocks in order;
+    merge_vertices applies trimesh's per-block merge (mesh.py:124-126, see mesh_out.py)."""
+    from oracle import mesh_out
     ax = lattice_axes(bounds, intv)
     sx, sy, sz = (block_slices(len(a), block_res) for a in ax)
     Vs, Fs, off = [], [], 0
@@ -79,6 +81,8 @@ def extract_mesh_blocks(sdf_volume_fn, bounds, intv, block_res, iso=0.0):
                 V, F = marching_cubes_block(vol, np.array([xs[0], ys[0], zs[0]], np.float32), intv, iso)
                 if V.shape[0] == 0:
                     continue
+                if merge_vertices:
+                    V, F = mesh_out.merge_vertices(V, F)
                 Vs.append(V)
                 Fs.append(F + off)
                 off += V.shape[0]

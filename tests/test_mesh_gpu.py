@@ -108,3 +108,94 @@ def test_extract_mesh_with_callable_like_reference():
     Vr, Fr = om.extract_mesh_blocks(vol_fn, bounds, intv, 8)
     assert np.array_equal(mesh.faces, Fr)
     assert np.allclose(mesh.vertices, Vr, rtol=0, atol=1e-12)
+
+
+# ---------------------------------------------------------------------------- output stage
+
+def planted_mesh(nv, nf, seed):
+    """Random mesh with exact and near duplicate vertices (some within the 8-digit merge,
+    some just outside it) and degenerate faces of every kind."""
+    rng = np.random.default_rng(seed)
+    V = rng.uniform(-1, 1, size=(nv, 3))
+    dup = rng.choice(nv, size=nv // 5, replace=False)
+    src = rng.choice(nv, size=nv // 5)
+    V[dup] = V[src] + rng.choice([0.0, 2e-9, -3e-9, 2e-8], size=(nv // 5, 1)) * rng.integers(0, 2, (nv // 5, 3))
+    F = rng.integers(0, nv, size=(nf, 3))
+    k = nf // 10
+    F[:k, 1] = F[:k, 0]                                        # repeated index
+    a, b = F[k:2 * k, 0], F[k:2 * k, 1]
+    V[F[k:2 * k, 2]] = 0.5 * (V[a] + V[b])                     # (nearly) collinear
+    return V, F
+
+
+@pytest.mark.parametrize("weld", [False, True])
+@pytest.mark.parametrize("min_side", [-1.0, 0.0, 1e-8, 1e-3])
+def test_finalize_matches_oracle(weld, min_side):
+    from oracle import mesh_out as mo
+    V, F = planted_mesh(5000, 9000, seed=3)
+    scale, offset = 1.7, (0.25, -3.0, 1e-3)
+    Vg, Fg = gm.finalize_mesh(torch.from_numpy(V).to(DEV), torch.from_numpy(F).to(DEV), weld=weld, scale=scale,
+                              offset=offset, min_side=min_side)
+    Vr, Fr = mo.finalize(V, F, weld=weld, scale=scale, offset=offset, height=min_side)
+    assert np.array_equal(Vg.cpu().numpy(), Vr)                  # same float64 operations
+    assert np.array_equal(Fg.cpu().numpy(), Fr)
+    if weld:
+        assert len(Vr) < len(V)
+    if min_side >= 0:
+        assert len(Fr) < len(F)
+
+
+def test_finalize_weld_at_scale():
+    """A million vertices with 30 % duplicates: the hash-table weld against the oracle."""
+    from oracle import mesh_out as mo
+    rng = np.random.default_rng(5)
+    base = rng.integers(-4000, 4000, size=(700_000, 3)) * 1e-4
+    V = base[rng.integers(0, len(base), size=1_000_000)]
+    F = rng.integers(0, len(V), size=(1_500_000, 3))
+    Vg, Fg = gm.finalize_mesh(torch.from_numpy(V).to(DEV), torch.from_numpy(F).to(DEV), weld=True, min_side=0.0)
+    Vr, Fr = mo.finalize(V, F, weld=True, height=0.0)
+    assert np.array_equal(Vg.cpu().numpy(), Vr) and np.array_equal(Fg.cpu().numpy(), Fr)
+
+
+def test_finalize_empty_and_bad_index():
+    e = torch.zeros(0, 3, dtype=torch.float64, device=DEV)
+    Vg, Fg = gm.finalize_mesh(e, torch.zeros(0, 3, dtype=torch.int64, device=DEV), weld=True)
+    assert Vg.shape[0] == 0 and Fg.shape[0] == 0
+    V = torch.rand(4, 3, dtype=torch.float64, device=DEV)
+    F = torch.tensor([[0, 1, 4]], dtype=torch.int64, device=DEV)     # index 4 of 4 vertices
+    with pytest.raises(RuntimeError, match="device error 4"):
+        gm.finalize_mesh(V, F)
+
+
+def test_extract_mesh_block_merge_matches_oracle():
+    """A field that is exactly zero on lattice points (|x| - 0.5 on the 2/32 lattice, at
+    (+-0.5, 0, 0) and its permutations).  A corner counts as positive only when
+    v > 0, so each such corner has five positive neighbours and marching cubes emits
+    five vertices on it, which the reference's per-block trimesh merge joins."""
+    bounds, intv, block = [(-1, 1)] * 3, 2.0 / 32, 8
+
+    def sdf(x):
+        return torch.sqrt((x * x).sum(-1, keepdim=True)) - 0.5
+
+    def vol_fn(xs, ys, zs):
+        X, Y, Z = torch.meshgrid(*[torch.from_numpy(a).to(DEV) for a in (xs, ys, zs)], indexing='ij')
+        return sdf(torch.stack([X, Y, Z], -1))[..., 0].cpu().numpy()
+
+    plain = gm.extract_mesh(sdf, bounds, intv, block_res=block, device=DEV)
+    merged = gm.extract_mesh(sdf, bounds, intv, block_res=block, device=DEV, merge_vertices=True)
+    Vr, Fr = om.extract_mesh_blocks(vol_fn, bounds, intv, block, merge_vertices=True)
+    assert len(merged.vertices) < len(plain.vertices)
+    assert np.array_equal(merged.faces, Fr)
+    assert np.allclose(merged.vertices, Vr, rtol=0, atol=1e-12)
+
+
+def test_export_mesh_writes_the_oracle_mesh(tmp_path):
+    from oracle import mesh_out as mo
+    target = shapes_union(2)
+    mesh = gm.extract_mesh(lambda x: -target(x)[..., None], [(-1, 1)] * 3, 2.0 / 40, block_res=16, device=DEV)
+    radius, center = 2.5, (0.1, -0.2, 3.0)
+    out = gm.export_mesh(mesh, tmp_path / "mesh.ply", sphere_radius=radius, sphere_center=center, device=DEV)
+    Vr, Fr = mo.finalize(mesh.vertices, mesh.faces, scale=radius, offset=center)
+    assert np.array_equal(out.vertices, Vr) and np.array_equal(out.faces, Fr)
+    V, F, C = gm.read_ply(tmp_path / "mesh.ply")
+    assert C is None and np.array_equal(F, Fr) and np.array_equal(V, Vr.astype(np.float32))
