@@ -62,8 +62,21 @@ def rgb_config(layers=4, hidden=256):
         mode="idr", encoding_view=dict(type="spherical", levels=3)))
 
 
-def field_config(name):
-    """Return AttrDict(sdf=..., rgb=..., appear_embed=..., s_var=..., render=...)."""
+def background_config(enabled=True, layers=8, hidden=256, skip=(4,), layers_rgb=2, hidden_rgb=128, levels=10,
+                      view_levels=3, samples=32):
+    """cfg.model.background (base.yaml:84-104) and render.num_samples.background."""
+    return to_attr(dict(
+        enabled=enabled, white=False, view_dep=True, samples=samples,
+        mlp=dict(num_layers=layers, hidden_dim=hidden, skip=list(skip), num_layers_rgb=layers_rgb,
+                 hidden_dim_rgb=hidden_rgb, skip_rgb=[], activ="relu", activ_params={},
+                 activ_density="softplus", activ_density_params={}),
+        encoding=dict(type="fourier", levels=levels),
+        encoding_view=dict(type="spherical", levels=view_levels)))
+
+
+def field_config(name, background=False):
+    """Return AttrDict(sdf=..., rgb=..., appear_embed=..., s_var=..., background=...).
+    background=True enables the background NeRF of the reference's base config."""
     if name == "small":
         sdf = sdf_config(levels=8, dim=4, dict_size=16, min_logres=4, max_logres=None, per_level_scale=1.5,
                          hidden=256)
@@ -76,6 +89,7 @@ def field_config(name):
     else:
         raise ValueError(name)
     return to_attr(dict(sdf=sdf, rgb=rgb, appear_embed=app, s_var=dict(init_val=3.0, anneal_end=0.1),
+                        background=background_config(enabled=bool(background)),
                         loss_weight=dict(render=1.0, eikonal=0.1, curvature=5e-4), warm_up_end=5000,
                         max_iter=500000))
 

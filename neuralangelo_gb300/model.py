@@ -1,7 +1,8 @@
 """Field model and training forward with the reference's structure (plain FP32 drop-in).
 
 ``FieldModel.render_step`` follows Model.render_rays_object + render_rays
-(projects/neuralangelo/model.py:124-190, background disabled) and
+(projects/neuralangelo/model.py:124-190; with the background NeRF of
+render_rays_background, :192-205, when ``cfg.background.enabled``) and
 Trainer._compute_loss (projects/neuralangelo/trainer.py:40-52).  Hash grid,
 NeuS alpha and compositing weights run on libgbsdf; the MLPs are torch linears
 exactly as in the reference.  ``schedule`` restates the per-iteration
@@ -11,7 +12,7 @@ import torch
 import torch.nn.functional as torch_F
 
 from . import render
-from .modules import NeuralRGB, NeuralSDF
+from .modules import BackgroundNeRF, NeuralRGB, NeuralSDF
 
 
 class FieldModel(torch.nn.Module):
@@ -24,6 +25,13 @@ class FieldModel(torch.nn.Module):
         self.appear_embed = None
         if cfg.appear_embed.enabled:
             self.appear_embed = torch.nn.Embedding(cfg.appear_embed.num_images, cfg.appear_embed.dim)
+        bg = cfg.get("background")
+        self.with_background = bool(bg and bg.enabled)
+        self.background_nerf = self.appear_embed_outside = None
+        if self.with_background:
+            self.background_nerf = BackgroundNeRF(bg, cfg.appear_embed)                 # model.py:60-61
+            if cfg.appear_embed.enabled:                                             # model.py:51-54
+                self.appear_embed_outside = torch.nn.Embedding(cfg.appear_embed.num_images, cfg.appear_embed.dim)
         self.outside_val = 1000.0 * (-1 if cfg.sdf.mlp.inside_out else 1)
         self.anneal_end = cfg.s_var.anneal_end
         self.progress = 0.0
@@ -46,7 +54,8 @@ class FieldModel(torch.nn.Module):
         """One training forward on a batch of rays; returns outputs and the total loss.
 
         batch: center [R,3], ray_unit [R,3], dists [R,N], far [R,1], outside [R,1] (bool),
-               target [R,3], app_idx [R] (long, when the appearance embedding is on).
+               target [R,3], app_idx [R] (long, when the appearance embedding is on),
+               dists_bg [R,Nb] (background sample distances, with the background NeRF).
         """
         c, d, dists = batch["center"], batch["ray_unit"], batch["dists"]
         R, N = dists.shape
@@ -63,8 +72,19 @@ class FieldModel(torch.nn.Module):
         rgbs = self.neural_rgb(points, normals, rays_unit, feats, app)
         alphas = render.compute_neus_alphas(d, sdfs[..., 0], gradients, dists, self.s_var, dist_far=batch["far"],
                                             progress=self.progress, anneal_end=self.anneal_end)
-        weights = render.alpha_compositing_weights(alphas)
-        rgb = render.composite(rgbs, weights)
+        rgbs_all, alphas_all = rgbs, alphas
+        if self.with_background:                                                      # model.py:129-134, 192-205
+            dists_bg = batch["dists_bg"]
+            pts_bg = c[:, None, :] + d[:, None, :] * dists_bg[..., None]
+            app_out = None
+            if self.appear_embed_outside is not None:
+                app_out = self.appear_embed_outside(batch["app_idx"])[:, None, :].expand(R, dists_bg.shape[1], -1)
+            rgbs_bg, dens_bg = self.background_nerf(pts_bg, d[:, None, :].expand_as(pts_bg), app_out)
+            alphas_bg = render.volume_rendering_alphas_dist(dens_bg, dists_bg)
+            rgbs_all = torch.cat([rgbs, rgbs_bg], dim=1)
+            alphas_all = torch.cat([alphas, alphas_bg], dim=1)
+        weights = render.alpha_compositing_weights(alphas_all)
+        rgb = render.composite(rgbs_all, weights)
         lw = self.cfg.loss_weight
         l_render = torch_F.l1_loss(rgb, batch["target"]) * 3                   # trainer.py:43
         inside = (~outside.expand(R, N)).float()

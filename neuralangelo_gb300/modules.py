@@ -269,3 +269,50 @@ class NeuralRGB(torch.nn.Module):
         if self.cfg_rgb.mode == "no_normal":
             parts.remove(normals)
         return self.mlp(torch.cat(parts, dim=-1)).sigmoid_()
+
+
+def positional_encoding(x, num_freq_bases):
+    """nerf_util.py:134-147: [sin(2^k pi x), cos(2^k pi x)] per input channel, k < L,
+    laid out [..., N, 2, L] -> [..., 2 N L]."""
+    freq = 2 ** torch.arange(num_freq_bases, dtype=torch.float32, device=x.device) * np.pi
+    spectrum = x[..., None] * freq
+    enc = torch.stack([spectrum.sin(), spectrum.cos()], dim=-2)
+    return enc.view(*x.shape[:-1], -1)
+
+
+class BackgroundNeRF(torch.nn.Module):
+    """modules.py:232-311: points reparametrised onto the unit sphere plus inverse
+    distance [x / |x|, 1 / |x|], Fourier-encoded (levels L: 4 + 8 L inputs); an
+    8-layer ReLU MLP with the input concatenated again at layer 4 gives the softplus
+    density (output 0) and 256 ReLU features; the view-dependent colour MLP takes
+    [features, SH(d), app] -> sigmoid RGB.  No weight norm (build_mlp passes none)."""
+
+    def __init__(self, cfg_bg, appear_embed):
+        super().__init__()
+        self.cfg = cfg_bg
+        assert cfg_bg.encoding.type == "fourier" and cfg_bg.encoding_view.type == "spherical"
+        self.levels = cfg_bg.encoding.levels
+        self.sh_levels = cfg_bg.encoding_view.levels
+        m = cfg_bg.mlp
+        in_dim = 4 + 8 * self.levels
+        view_dim = m.hidden_dim + (self.sh_levels + 1) ** 2 + (appear_embed.dim if appear_embed.enabled else 0)
+        self.mlp_feat = MLPwithSkipConnection([in_dim] + [m.hidden_dim] * (m.num_layers - 1) + [m.hidden_dim + 1],
+                                              skip_connection=m.skip, activ=get_activation(m.activ, **m.activ_params))
+        self.activ_density = get_activation(m.activ_density, **m.activ_density_params)
+        self.mlp_rgb = MLPwithSkipConnection([view_dim] + [m.hidden_dim_rgb] * (m.num_layers_rgb - 1) + [3],
+                                             skip_connection=m.skip_rgb,
+                                             activ=get_activation(m.activ, **m.activ_params))
+
+    def encode(self, points_3D):
+        norm = points_3D.norm(dim=-1, keepdim=True)
+        pts = torch.cat([points_3D / norm, 1.0 / norm], dim=-1)
+        return torch.cat([pts, positional_encoding(pts, self.levels)], dim=-1)
+
+    def forward(self, points_3D, rays_unit, app_outside):
+        out = self.mlp_feat(self.encode(points_3D))
+        density, feat = self.activ_density(out[..., 0]), self.mlp_feat.activ(out[..., 1:])
+        parts = [feat, get_spherical_harmonics(rays_unit, self.sh_levels)]
+        if app_outside is not None:
+            parts.append(app_outside)
+        rgb = self.mlp_rgb(torch.cat(parts, dim=-1)).sigmoid_()
+        return rgb, density

@@ -4,6 +4,7 @@ Mirrors the reference call surface:
   compute_neus_alphas(...)          Model.compute_neus_alphas, projects/neuralangelo/model.py:275-292
   alpha_compositing_weights(alphas) projects/nerf/utils/render.py:87-99
   composite(quantities, weights)    projects/nerf/utils/render.py:102-112
+  volume_rendering_alphas_dist(...) projects/nerf/utils/render.py:68-84 (background samples; torch)
 Shapes follow the reference ([B,R,N] with B folded into R).
 """
 import torch
@@ -71,6 +72,16 @@ class _WeightsFn(torch.autograd.Function):
         _lib.call("gbsdf_composite_weights_bwd", R, N, _lib.ptr(a), _lib.ptr(d_w.contiguous().float()),
                   _lib.ptr(d_a), _lib.stream_ptr(a.device))
         return d_a
+
+
+def volume_rendering_alphas_dist(densities, dists, dist_far=None):
+    """render.py:68-84: alpha = 1 - exp(-density * interval), the last interval running to
+    dist_far (1e10 by default); densities [R,N], dists [R,N] -> alphas [R,N]."""
+    if dist_far is None:
+        dist_far = torch.empty_like(dists[..., :1]).fill_(1e10)
+    d = torch.cat([dists, dist_far], dim=-1)
+    sigma_delta = densities * (d[..., 1:] - d[..., :-1])
+    return 1 - (-sigma_delta).exp()
 
 
 def alpha_compositing_weights(alphas):

@@ -24,7 +24,7 @@ def sphere_bounds(center, ray_unit):
     return near, far, outside
 
 
-def make_rays(R, N, seed=0, miss_frac=0.0, n_images=0, device="cpu"):
+def make_rays(R, N, seed=0, miss_frac=0.0, n_images=0, device="cpu", n_bg=0):
     g = torch.Generator().manual_seed(seed)
     c = torch.randn(R, 3, generator=g)
     c = 3.0 * c / c.norm(dim=-1, keepdim=True)
@@ -39,7 +39,20 @@ def make_rays(R, N, seed=0, miss_frac=0.0, n_images=0, device="cpu"):
     target = torch.rand(R, 3, generator=g)
     app_idx = torch.randint(0, max(n_images, 1), (R,), generator=g)
     b = dict(center=c, ray_unit=d, dists=dists, far=far, outside=outside, target=target, app_idx=app_idx)
+    if n_bg:
+        b["dists_bg"] = background_dists(far, n_bg, torch.rand(R, n_bg, generator=g))
     return {k: v.to(device) for k, v in b.items()}
+
+
+def background_dists(far, n, u=None):
+    """Model.sample_dists_background (model.py:269-273): inverse distances stratified
+    from 1 down to 0 (nerf_util.py:20-38 with dist_range (1, 0)), dists = far / (inv +
+    1e-5); u [R, n] in [0, 1), or 0.5 when not stratified.  far [R, 1] -> [R, n]."""
+    R = far.shape[0]
+    if u is None:
+        u = torch.full((R, n), 0.5)
+    inv = (u + torch.arange(n, dtype=torch.float32)[None]) / n * (0.0 - 1.0) + 1.0
+    return far / (inv + 1e-5)
 
 
 def make_ragged_rays(R, seed=0, zero_frac=0.3, lo=16, hi=256, n_images=0, device="cpu"):

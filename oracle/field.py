@@ -23,7 +23,9 @@ def make_config(n_levels=16, n_features=8, log2_hashmap_size=22, base_resolution
                 per_level_scale=None, max_resolution=2048, active_levels=None,
                 sdf_hidden=256, rgb_hidden=256, rgb_layers=4, app_dim=0, n_images=0,
                 softplus_beta=100.0, out_bias=0.5, inside_out=False, s_var_init=3.0,
-                anneal_end=0.1, taps=6, vol_range=(-2.0, 2.0), sh_levels=3, f32_positions=False):
+                anneal_end=0.1, taps=6, vol_range=(-2.0, 2.0), sh_levels=3, f32_positions=False,
+                bg_enabled=False, bg_layers=8, bg_hidden=256, bg_skip=(4,), bg_layers_rgb=2, bg_hidden_rgb=128,
+                bg_levels=10, bg_view_levels=3):
     if per_level_scale is None:
         # modules.py:39-41
         per_level_scale = float(np.exp((np.log(max_resolution) - np.log(base_resolution)) / (n_levels - 1)))
@@ -33,7 +35,9 @@ def make_config(n_levels=16, n_features=8, log2_hashmap_size=22, base_resolution
                 sdf_hidden=sdf_hidden, rgb_hidden=rgb_hidden, rgb_layers=rgb_layers, app_dim=app_dim,
                 n_images=n_images, softplus_beta=softplus_beta, out_bias=out_bias, inside_out=inside_out,
                 s_var_init=s_var_init, anneal_end=anneal_end, taps=taps, vol_range=vol_range,
-                sh_levels=sh_levels, f32_positions=f32_positions)
+                sh_levels=sh_levels, f32_positions=f32_positions, bg_enabled=bg_enabled, bg_layers=bg_layers,
+                bg_hidden=bg_hidden, bg_skip=tuple(bg_skip), bg_layers_rgb=bg_layers_rgb,
+                bg_hidden_rgb=bg_hidden_rgb, bg_levels=bg_levels, bg_view_levels=bg_view_levels)
 
 
 def eps_resolutions(cfg):
@@ -136,7 +140,87 @@ def init_params(cfg, seed=0, enc_perturb=1e-2, table_scale=1e-4, dtype=torch.flo
     p['s_var'] = torch.tensor(cfg['s_var_init'], dtype=torch.float64)
     if cfg['app_dim'] > 0:
         p['app'] = torch.randn(cfg['n_images'], cfg['app_dim'], generator=gen, dtype=torch.float64)
+    if cfg.get('bg_enabled'):
+        # BackgroundNeRF (modules.py:232-266): torch.nn.Linear default init, no weight
+        # norm, last-layer biases zero (nerf_util.py:182-183)
+        for pre, dims, skip in (('bg', bg_feat_dims(cfg), cfg['bg_skip']), ('bg.rgb', bg_rgb_dims(cfg), ())):
+            for i, (k_in, k_out) in enumerate(zip(dims[:-1], dims[1:])):
+                k_in = k_in + (dims[0] if i in skip else 0)
+                bound = 1.0 / math.sqrt(k_in)
+                p[f'{pre}.l{i}.w'] = (torch.rand(k_out, k_in, generator=gen, dtype=torch.float64) * 2 - 1) * bound
+                b = (torch.rand(k_out, generator=gen, dtype=torch.float64) * 2 - 1) * bound
+                p[f'{pre}.l{i}.b'] = torch.zeros_like(b) if i == len(dims) - 2 else b
+        if cfg['app_dim'] > 0:
+            p['app_bg'] = torch.randn(cfg['n_images'], cfg['app_dim'], generator=gen, dtype=torch.float64)
     return {k: v.to(dtype) for k, v in p.items()}, layout
+
+
+def bg_feat_dims(cfg):
+    """BackgroundNeRF.build_mlp (modules.py:258-261): [4 + 8 L] + [H] * (layers - 1) + [H + 1]."""
+    return [4 + 8 * cfg['bg_levels']] + [cfg['bg_hidden']] * (cfg['bg_layers'] - 1) + [cfg['bg_hidden'] + 1]
+
+
+def bg_rgb_dims(cfg):
+    """modules.py:238-240, 263-264: [H + SH + app] + [H_rgb] * (layers_rgb - 1) + [3]."""
+    d_in = cfg['bg_hidden'] + (cfg['bg_view_levels'] + 1) ** 2 + cfg['app_dim']
+    return [d_in] + [cfg['bg_hidden_rgb']] * (cfg['bg_layers_rgb'] - 1) + [3]
+
+
+def positional_encoding(x, num_freq_bases):
+    """nerf_util.py:134-147; the frequencies 2^k pi are float32 as the reference builds them."""
+    freq = (2 ** torch.arange(num_freq_bases, dtype=torch.float32) * np.pi).to(x.dtype)
+    spectrum = x[..., None] * freq
+    enc = torch.stack([spectrum.sin(), spectrum.cos()], dim=-2)
+    return enc.reshape(*x.shape[:-1], -1)
+
+
+def bg_encode(cfg, pts):
+    """BackgroundNeRF.encode (modules.py:286-301): [x/|x|, 1/|x|] and its Fourier code."""
+    norm = pts.norm(dim=-1, keepdim=True)
+    q = torch.cat([pts / norm, 1.0 / norm], dim=-1)
+    return torch.cat([q, positional_encoding(q, cfg['bg_levels'])], dim=-1)
+
+
+def background(p, cfg, pts, rays_unit, app_out=None):
+    """BackgroundNeRF.forward (modules.py:268-284) -> (rgb [...,3], density [...])."""
+    x = bg_encode(cfg, pts)
+    h = x
+    n = cfg['bg_layers']
+    for i in range(n):                                        # MLPwithSkipConnection (nerf_util.py:187-196)
+        if i in cfg['bg_skip']:
+            h = torch.cat([h, x], dim=-1)
+        h = h @ p[f'bg.l{i}.w'].t() + p[f'bg.l{i}.b']
+        if i != n - 1:
+            h = torch.relu(h)
+    density, feat = F.softplus(h[..., 0]), torch.relu(h[..., 1:])
+    parts = [feat, spherical_harmonics(rays_unit)]
+    if app_out is not None:
+        parts.append(app_out)
+    g = torch.cat(parts, dim=-1)
+    m = cfg['bg_layers_rgb']
+    for i in range(m):
+        g = g @ p[f'bg.rgb.l{i}.w'].t() + p[f'bg.rgb.l{i}.b']
+        if i != m - 1:
+            g = torch.relu(g)
+    return torch.sigmoid(g), density
+
+
+def volume_alphas(density, dists, dist_far=1e10):
+    """render.py:68-84: 1 - exp(-density * interval), the last interval to dist_far."""
+    d = torch.cat([dists, torch.full_like(dists[..., :1], dist_far)], dim=-1)
+    return 1 - torch.exp(-(density * (d[..., 1:] - d[..., :-1])))
+
+
+def background_branch(p, cfg, center, ray_unit, dists_bg, app_idx=None):
+    """Model.render_rays_background (model.py:192-205) on precomputed distances
+    (sample_dists_background, model.py:269-273): (rgbs [R,Nb,3], alphas [R,Nb])."""
+    pts = center[:, None, :] + ray_unit[:, None, :] * dists_bg[..., None]
+    rays = ray_unit[:, None, :].expand_as(pts)
+    app_out = None
+    if cfg['app_dim'] > 0 and 'app_bg' in p:
+        app_out = p['app_bg'][app_idx][:, None, :].expand(pts.shape[0], pts.shape[1], cfg['app_dim'])
+    rgbs, dens = background(p, cfg, pts, rays, app_out)
+    return rgbs, volume_alphas(dens, dists_bg)
 
 
 # ---------------------------------------------------------------------------
@@ -331,7 +415,8 @@ def curvature_loss(hess, outside):
 
 def render_step(p, cfg, layout, batch, eps, progress, w_eik, w_curv, training=True, retain=False):
     """One training forward of Model.render_rays_object + render_rays + Trainer._compute_loss
-    (model.py:124-190, trainer.py:40-52), background disabled.
+    (model.py:124-190, trainer.py:40-52), with the background NeRF's samples composited
+    after the object's (model.py:129-134) when cfg['bg_enabled'] and batch['dists_bg'].
 
     batch: center [R,3], ray_unit [R,3], dists [R,N], far [R,1], outside [R,1] (bool),
            target [R,3], app_idx [R] (or None).  Returns a dict of outputs incl. 'loss'.
@@ -356,8 +441,14 @@ def render_step(p, cfg, layout, batch, eps, progress, w_eik, w_curv, training=Tr
         app = p['app'][batch['app_idx']][:, None, :].expand(R, N, cfg['app_dim'])
     rgbs = neural_rgb(p, cfg, pts, normals, rays, feat, app)
     alphas = neus_alphas(d, sdf[..., 0], grads, dists, batch['far'], p['s_var'], progress, cfg['anneal_end'])
-    weights = compositing_weights(alphas)
-    rgb = (rgbs * weights[..., None]).sum(dim=1)
+    rgbs_all, alphas_all = rgbs, alphas
+    if cfg.get('bg_enabled') and batch.get('dists_bg') is not None:     # model.py:129-134
+        rgbs_bg, alphas_bg = background_branch(p, cfg, c, d, batch['dists_bg'], batch.get('app_idx'))
+        rgbs_all = torch.cat([rgbs, rgbs_bg], dim=1)
+        alphas_all = torch.cat([alphas, alphas_bg], dim=1)
+    weights = compositing_weights(alphas_all)
+    rgb = (rgbs_all * weights[..., None]).sum(dim=1)
+    weights = weights[:, :N]
     l_render = (rgb - batch['target']).abs().mean() * 3.0                  # trainer.py:43
     out_mask = outside.expand(R, N)
     l_eik = eikonal_loss(grads, out_mask)
@@ -397,12 +488,21 @@ def render_step_ragged(p, cfg, layout, batch, eps, progress, w_eik, w_curv, mean
             for r in rays:
                 rgb_rows[r] = torch.zeros(3, dtype=dt)
                 sdf_flat[r] = torch.zeros(0, dtype=dt)
+            if cfg.get('bg_enabled') and batch.get('dists_bg') is not None:
+                idx = torch.tensor(rays)
+                rgbs_bg, alphas_bg = background_branch(
+                    p, cfg, batch['center'][idx], batch['ray_unit'][idx], batch['dists_bg'][idx],
+                    batch['app_idx'][idx] if batch.get('app_idx') is not None else None)
+                rgb0 = (rgbs_bg * compositing_weights(alphas_bg)[..., None]).sum(dim=1)
+                for j, r in enumerate(rays):
+                    rgb_rows[r] = rgb0[j]
             continue
         idx = torch.tensor(rays)
         d = torch.stack([batch['dists'][offs[r]:offs[r + 1]] for r in rays])
         sub = dict(center=batch['center'][idx], ray_unit=batch['ray_unit'][idx], dists=d,
                    far=batch['far'][idx], outside=batch['outside'][idx], target=batch['target'][idx],
-                   app_idx=batch['app_idx'][idx] if batch.get('app_idx') is not None else None)
+                   app_idx=batch['app_idx'][idx] if batch.get('app_idx') is not None else None,
+                   dists_bg=batch['dists_bg'][idx] if batch.get('dists_bg') is not None else None)
         out = render_step(p, cfg, layout, sub, eps, progress, w_eik, w_curv)
         ins = (~sub['outside']).to(dt).expand(len(rays), n)
         eik = ((out['grads'].norm(dim=-1) - 1.0) ** 2).nan_to_num(nan=0.0, posinf=0.0, neginf=0.0)

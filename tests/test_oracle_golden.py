@@ -43,3 +43,34 @@ def test_oracle_matches_reference_modules(name):
     if 'g_app' in z:
         assert rel(params['app'].grad, z['g_app']) < 1e-10
     assert np.linalg.norm(z['g_table']) > 0   # the perturbed encoding columns make the table gradient live
+
+
+def test_background_oracle_matches_reference_golden():
+    """Background NeRF (modules.py:232-311), its alphas (render.py:68-84) and the
+    compositing behind object samples (model.py:129-141), forward and the L1 loss
+    gradients, against the reference's own modules run in float64
+    (tests/golden/make_golden_background.py)."""
+    z = np.load(golden_io.GOLDEN + "/background.npz")
+    R, NO, NB, H, HRGB, APP, NIMG = [int(v) for v in z['meta']]
+    cfg = of.make_config(app_dim=APP, n_images=NIMG, bg_enabled=True, bg_hidden=H, bg_hidden_rgb=HRGB)
+    p = {k: torch.from_numpy(z[k]).requires_grad_(True) for k in z.files
+         if k.startswith('bg.') or k == 'app_bg'}
+    t = {k: torch.from_numpy(z[k]) for k in ('center', 'ray_unit', 'far', 'app_idx', 'target', 'dists_bg')}
+    obj_a = torch.from_numpy(z['obj_alpha']).requires_grad_(True)
+    obj_c = torch.from_numpy(z['obj_rgbs']).requires_grad_(True)
+    rgbs_bg, alphas_bg = of.background_branch(p, cfg, t['center'], t['ray_unit'], t['dists_bg'], t['app_idx'])
+    w = of.compositing_weights(torch.cat([obj_a, alphas_bg], dim=1))
+    rgb = (torch.cat([obj_c, rgbs_bg], dim=1) * w[..., None]).sum(dim=1)
+    loss = (rgb - t['target']).abs().mean() * 3
+    loss.backward()
+    close = dict(rtol=1e-10, atol=1e-12)
+    assert np.allclose(rgbs_bg.detach().numpy(), z['rgbs_bg'], **close)
+    assert np.allclose(alphas_bg.detach().numpy(), z['alphas_bg'], **close)
+    assert np.allclose(rgb.detach().numpy(), z['rgb'], **close)
+    assert np.allclose(float(loss), float(z['loss']), **close)
+    assert np.allclose(obj_a.grad.numpy(), z['d_obj_alpha'], **close)
+    assert np.allclose(obj_c.grad.numpy(), z['d_obj_rgbs'], **close)
+    assert np.allclose(p['app_bg'].grad.numpy(), z['d_app_bg'], **close)
+    for k, v in p.items():
+        if k.startswith('bg.'):
+            assert np.allclose(v.grad.numpy(), z['d_' + k], **close), k
