@@ -97,6 +97,39 @@ def bench_ragged(model, device, steps, warmup, rays=65536, seed=0):
     return out
 
 
+def bench_background(device, steps, warmup, rays=R_RAYS, samples=N_SAMPLES, n_bg=32, seed=0):
+    """The same full-field step with the background NeRF of the reference's base config
+    (8 x 256 ReLU with a skip at 4, 32 background samples per ray composited behind the
+    object's: model.py:129-141), fused, against the plain FP32 path on the same rays."""
+    import torch
+    from neuralangelo_gb300.config import field_config
+    from neuralangelo_gb300.fused import CapturedStep, FusedField
+    from neuralangelo_gb300.model import FieldModel
+    from neuralangelo_gb300.workloads import full_field_iteration, init_field_params, make_rays
+    cfg = field_config("full", background=True)
+    torch.manual_seed(seed)
+    m = FieldModel(cfg).to(device)
+    init_field_params(m, seed)
+    m.schedule(full_field_iteration(ACTIVE))
+    b = make_rays(rays, samples, seed=seed, n_images=100, device=device, n_bg=n_bg)
+    ff = FusedField(m)
+    cap = CapturedStep(ff, b)
+    ms = time_steps(cap.replay, steps, warmup, lambda: None)
+    assert ff.check_device_errors() == 0
+    del cap
+    ff.release()
+
+    def plain():
+        m.zero_grad(set_to_none=True)
+        m.render_step(b)["loss"].backward()
+    ms_plain = time_steps(plain, max(2, steps // 2), 1, lambda: None)
+    torch.cuda.empty_cache()
+    ns = rays * samples
+    return dict(rays=rays, object_samples=ns, background_samples=rays * n_bg, ms_per_step=round(ms, 3),
+                samples_per_s=round(ns / (ms * 1e-3), 1), plain_fp32_ms_per_step=round(ms_plain, 3),
+                speedup_vs_plain=round(ms_plain / ms, 3))
+
+
 def bench_sampler(model, device, steps=5, warmup=2, rays=R_RAYS, seed=0):
     """The no-grad hierarchical pre-pass (64 coarse + 4 x 16 importance samples per ray,
     SDF of the fused field kernel), timed separately from the training step."""
@@ -446,6 +479,7 @@ def main():
         fused.release()
         torch.cuda.empty_cache()
         extras["ragged"] = bench_ragged(model, device, max(3, args.steps // 2), args.warmup)
+        extras["background"] = bench_background(device, max(3, args.steps // 2), args.warmup)
         extras["sampler"] = bench_sampler(model, device)
         extras["mesh"] = bench_mesh(model, device)
     cb = None

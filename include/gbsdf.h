@@ -130,7 +130,7 @@ int gbsdf_composite_weights_bwd(int64_t R, int64_t N, const float* alpha, const 
  *         previous layer's activation; G = its stored output; bias ignored)
  * X [M, ldx] fp16, W [N, K] fp16 row-major, bias [N] fp32 (may be NULL),
  * G [M, ldg] fp16, Y [M, ldy] fp16 (fp32 when y_f32 != 0).  K % 16 == 0,
- * K <= 320, N % 64 == 0, ldx/ldg/ldy % 8 == 0, 16-byte aligned bases.
+ * K <= 512 (and the weight slice within shared memory), N % 64 == 0, ldx/ldg/ldy % 8 == 0, 16-byte aligned bases.
  * Xlo (optional): low fp16 half of X (X = Xhi + Xlo), multiplied as well;
  * Ylo (optional): receives the fp16 rounding residual of Y (Y = Yhi + Ylo).
  * The split pair carries a gradient through the colour MLP's input-gradient
@@ -249,6 +249,17 @@ typedef struct gbsdf_render_args {
     float* d_s_var;              /* [1] accumulated */
     double* loss_sums;           /* [4] accumulated: l1 sum, eikonal sum, curvature sum, (unused) */
     int32_t* err;                /* device flag: 2 = a ray longer than 512 samples was skipped */
+    /* Background NeRF samples composited after each ray's object samples (model.py:129-141):
+     * n_bg per ray (0: none), alpha = 1 - exp(-sigma dt) with the last interval to 1e10
+     * (render.py:68-84).  Object + background samples of a ray must number <= 512. */
+    int32_t n_bg;
+    int32_t ld_d_bg_pre;         /* row stride (elements) of d_bg_pre */
+    const float* bg_dists;       /* [R, n_bg] */
+    const float* bg_sigma;       /* [R, n_bg] density (softplus output) */
+    const float* bg_rgbs;        /* [R, n_bg, 3] */
+    float* bg_weights;           /* [R, n_bg] out (may be NULL) */
+    float* d_bg_rgbs;            /* [R, n_bg, 3] out */
+    void* d_bg_pre;              /* fp16 out, row s at s * ld_d_bg_pre: d loss / d density pre-activation */
 } gbsdf_render_args;
 
 size_t gbsdf_render_args_size(void);
@@ -299,6 +310,20 @@ size_t gbsdf_mc_workspace_size(int nx, int ny, int nz);
 int gbsdf_mc_block(const float* vol, int nx, int ny, int nz, double iso, const double* origin, double intv,
                    void* workspace, size_t ws_bytes, double* V, int64_t V_cap, int64_t* F, int64_t F_cap,
                    int64_t* counts, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Background NeRF pieces of the fused step (projects/neuralangelo/utils/modules.py:232-311).
+ * gbsdf_bg_encode: for the NB background samples of each of R rays (points c + d t at
+ * dists [R, NB]) writes the first layer's fp16 input row X [R NB, ldx] -- x/|x|, 1/|x|,
+ * their 10-level Fourier code (nerf_util.py:134-147), a constant 1 at column 84, zeros up
+ * to x_cols -- and the colour MLP's input tail T [R NB, ldt] -- SH(d) (16), the appearance
+ * code app_table[app_idx[r]] (app_dim, may be 0), a constant 1, zeros up to t_cols.
+ * gbsdf_bg_density: sigma [M] = softplus(H [M, ldh] . w [H] + b[0]) (beta 1, threshold 20). */
+int gbsdf_bg_encode(int64_t R, int32_t NB, const float* center, const float* ray_unit, const float* dists,
+                    const float* app_table, const int32_t* app_idx, int32_t app_dim, void* X, int32_t ldx,
+                    int32_t x_cols, void* T, int32_t ldt, int32_t t_cols, void* stream);
+int gbsdf_bg_density(int64_t M, const void* H, int32_t ldh, int32_t Hdim, const float* w, const float* b,
+                     float* sigma, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Mesh output stage (scripts/extract_mesh.py:96-97 after utils/mesh.py:121-129 and

@@ -396,7 +396,7 @@ extern "C" int gbsdf_dense(int64_t M, int K, int N, const void* X, const void* X
     GBSDF_CHECK_ARG(M >= 0 && K > 0 && N > 0, "bad sizes");
     if (M == 0) return GBSDF_OK;
     GBSDF_CHECK_ARG(X && W && Y, "NULL pointer");
-    GBSDF_CHECK_ARG(K % 16 == 0 && K <= 320, "K=%d must be a multiple of 16 and <= 320", K);
+    GBSDF_CHECK_ARG(K % 16 == 0 && K <= 512, "K=%d must be a multiple of 16 and <= 512", K);
     GBSDF_CHECK_ARG(N % 64 == 0 && N <= 512, "N=%d must be a multiple of 64 and <= 512", N);
     GBSDF_CHECK_ARG(ldx % 8 == 0 && ldy % 8 == 0 && ldx >= K && ldy >= N, "leading dimensions");
     GBSDF_CHECK_ARG(aligned(X, 16) && aligned(W, 16) && aligned(Y, 16), "X, W, Y must be 16-byte aligned");

@@ -3,7 +3,8 @@
 //
 // gbsdf_render_fused : NeuS alpha (projects/neuralangelo/model.py:275-298),
 //   front-to-back compositing with FP32 log-space transmittance
-//   (projects/nerf/utils/render.py:87-112), L1 colour x3, eikonal and curvature
+//   (projects/nerf/utils/render.py:87-112) of the object samples followed by the
+//   background NeRF's (model.py:129-141, render.py:68-84), L1 colour x3, eikonal and curvature
 //   losses (projects/neuralangelo/trainer.py:40-52, utils/misc.py:74-89) and the
 //   analytic backward of all of it, one warp per ray.
 // gbsdf_rgb_head_*   : last colour layer 256 -> 3 + sigmoid (modules.py:215,
@@ -34,7 +35,9 @@ __global__ void __launch_bounds__(RENDER_WARPS * 32) k_render_fused(gbsdf_render
     const int64_t beg = p.S > 0 ? r * p.S : p.ray_offsets[r];
     const int64_t end = p.S > 0 ? beg + p.S : p.ray_offsets[r + 1];
     const int n = (int)(end - beg);
-    if (n > MAX_RAY_SAMPLES) {   // longer rays do not fit the per-warp buffers: report, skip
+    const int nb = p.n_bg;                     // background samples follow the object samples
+    const int ntot = n + nb;
+    if (ntot > MAX_RAY_SAMPLES) {   // longer rays do not fit the per-warp buffers: report, skip
         if (lane == 0 && p.err) atomicCAS(p.err, 0, 2);
         return;
     }
@@ -49,9 +52,16 @@ __global__ void __launch_bounds__(RENDER_WARPS * 32) k_render_fused(gbsdf_render
     float carry = 0.0f;   // sum of log(1 - alpha) over earlier chunks
     float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
     float eik_sum = 0.0f, curv_sum = 0.0f;
-    for (int base = 0; base < n; base += 32) {
+    for (int base = 0; base < ntot; base += 32) {
         const int k = base + lane;
         float a = 0.0f, la = 0.0f;
+        if (k >= n && k < ntot) {
+            // background sample: alpha = 1 - exp(-sigma dt), log(1 - alpha) = -sigma dt
+            const int64_t q = r * nb + (k - n);
+            const float dnext = (k + 1 < ntot) ? p.bg_dists[q + 1] : 1e10f;
+            la = -(p.bg_sigma[q] * (dnext - p.bg_dists[q]));
+            a = -expm1f(la);
+        }
         if (k < n) {
             const int64_t s = beg + k;
             const float gx = p.grad[3 * s], gy = p.grad[3 * s + 1], gz = p.grad[3 * s + 2];
@@ -82,15 +92,23 @@ __global__ void __launch_bounds__(RENDER_WARPS * 32) k_render_fused(gbsdf_render
         float excl = __shfl_up_sync(0xffffffffu, incl, 1);
         if (lane == 0) excl = 0.0f;
         const float T = expf(carry + excl);   // prod_{j<k} (1 - a_j)
-        if (k < n) {
-            const int64_t s = beg + k;
+        if (k < ntot) {
             sa[k] = a;
             sT[k] = T;
             const float w = a * T;
-            if (p.weights) p.weights[s] = w;
-            c0 = fmaf(w, p.rgbs[3 * s], c0);
-            c1 = fmaf(w, p.rgbs[3 * s + 1], c1);
-            c2 = fmaf(w, p.rgbs[3 * s + 2], c2);
+            const float* cp;
+            if (k < n) {
+                const int64_t s = beg + k;
+                if (p.weights) p.weights[s] = w;
+                cp = p.rgbs + 3 * s;
+            } else {
+                const int64_t q = r * nb + (k - n);
+                if (p.bg_weights) p.bg_weights[q] = w;
+                cp = p.bg_rgbs + 3 * q;
+            }
+            c0 = fmaf(w, cp[0], c0);
+            c1 = fmaf(w, cp[1], c1);
+            c2 = fmaf(w, cp[2], c2);
         }
         carry += __shfl_sync(0xffffffffu, incl, 31);
     }
@@ -119,22 +137,23 @@ __global__ void __launch_bounds__(RENDER_WARPS * 32) k_render_fused(gbsdf_render
     // ---------------- backward (reverse chunks) ----------------
     float Snext = 0.0f;    // S of the first sample after the current chunk
     float ds_acc = 0.0f;
-    const int last = ((n + 31) / 32 - 1) * 32;
+    const int last = ((ntot + 31) / 32 - 1) * 32;
     for (int base = last; base >= 0; base -= 32) {
         const int k = base + lane;
-        const bool live = k < n;
+        const bool live = k < ntot;
         float a = 0.0f, T = 0.0f, dw = 0.0f;
-        float rc0 = 0.f, rc1 = 0.f, rc2 = 0.f;
         int64_t s = beg + k;
+        const int64_t q = r * nb + (k - n);      // background index when k >= n
         if (live) {
             a = sa[k];
             T = sT[k];
-            rc0 = p.rgbs[3 * s]; rc1 = p.rgbs[3 * s + 1]; rc2 = p.rgbs[3 * s + 2];
-            dw = dr0 * rc0 + dr1 * rc1 + dr2 * rc2;
+            const float* cp = k < n ? p.rgbs + 3 * s : p.bg_rgbs + 3 * q;
+            float* dcp = k < n ? p.d_rgbs + 3 * s : p.d_bg_rgbs + 3 * q;
+            dw = dr0 * cp[0] + dr1 * cp[1] + dr2 * cp[2];
             const float w = a * T;
-            p.d_rgbs[3 * s] = dr0 * w;
-            p.d_rgbs[3 * s + 1] = dr1 * w;
-            p.d_rgbs[3 * s + 2] = dr2 * w;
+            dcp[0] = dr0 * w;
+            dcp[1] = dr1 * w;
+            dcp[2] = dr2 * w;
         }
         // S_k = dw_k a_k + (1 - a_k) S_{k+1}: suffix scan of affine maps
         float A = live ? dw * a : 0.0f, B = live ? 1.0f - a : 1.0f;
@@ -150,7 +169,16 @@ __global__ void __launch_bounds__(RENDER_WARPS * 32) k_render_fused(gbsdf_render
         const float Sk = A + B * Snext;
         float Sk1 = __shfl_down_sync(0xffffffffu, Sk, 1);
         if (lane == 31) Sk1 = Snext;
-        if (live) {
+        if (live && k >= n) {
+            // background: d sigma = d alpha dt (1 - alpha); softplus' = 1 - exp(-sigma)
+            const float d_alpha = T * (dw - Sk1);
+            const float dnext = (k + 1 < ntot) ? p.bg_dists[q + 1] : 1e10f;
+            const float dt = dnext - p.bg_dists[q];
+            const float sig = p.bg_sigma[q];
+            const float d_sig = d_alpha * dt * expf(-sig * dt);
+            const float d_pre = d_sig * -expm1f(-sig);
+            reinterpret_cast<__half*>(p.d_bg_pre)[q * (int64_t)p.ld_d_bg_pre] = __float2half_rn(d_pre);
+        } else if (live) {
             float d_alpha = T * (dw - Sk1);
             // NeuS alpha backward (recomputed terms)
             const float gx = p.grad[3 * s], gy = p.grad[3 * s + 1], gz = p.grad[3 * s + 2];
@@ -327,6 +355,13 @@ extern "C" int gbsdf_render_fused(const gbsdf_render_args* a, void* stream) {
     GBSDF_CHECK_ARG(p.ray_unit && p.dists && p.far && p.target && p.s_var && p.sdf && p.grad && p.hess && p.rgbs &&
                         p.rgb && p.d_rgbs && p.d_sdf && p.d_grad && p.d_hess && p.d_s_var && p.loss_sums,
                     "NULL pointer");
+    GBSDF_CHECK_ARG(p.n_bg >= 0 && p.n_bg <= MAX_RAY_SAMPLES, "n_bg %d", p.n_bg);
+    GBSDF_CHECK_ARG(p.S == 0 || p.S + p.n_bg <= MAX_RAY_SAMPLES, "S + n_bg = %d exceeds %d samples per ray",
+                    p.S + p.n_bg, MAX_RAY_SAMPLES);
+    if (p.n_bg > 0) {
+        GBSDF_CHECK_ARG(p.bg_dists && p.bg_sigma && p.bg_rgbs && p.d_bg_rgbs && p.d_bg_pre && p.ld_d_bg_pre >= 1,
+                        "background sample pointers");
+    }
     const unsigned blocks = (unsigned)((p.R + RENDER_WARPS - 1) / RENDER_WARPS);
     k_render_fused<<<blocks, RENDER_WARPS * 32, 0, as_stream(stream)>>>(p);
     return launch_status("render_fused");

@@ -51,7 +51,8 @@ class RenderArgs(ctypes.Structure):
                 ("w_render", c_f32), ("w_eik", c_f32), ("w_curv", c_f32), ("l1_scale", c_f32),
                 ("mean_scale", c_f32), ("loss_scale", c_f32), ("pad1", c_i32), ("rgb", c_vp), ("weights", c_vp),
                 ("d_rgbs", c_vp), ("d_sdf", c_vp), ("d_grad", c_vp), ("d_hess", c_vp), ("d_s_var", c_vp),
-                ("loss_sums", c_vp), ("err", c_vp)]
+                ("loss_sums", c_vp), ("err", c_vp), ("n_bg", c_i32), ("ld_d_bg_pre", c_i32), ("bg_dists", c_vp),
+                ("bg_sigma", c_vp), ("bg_rgbs", c_vp), ("bg_weights", c_vp), ("d_bg_rgbs", c_vp), ("d_bg_pre", c_vp)]
 
 
 _lib.register("gbsdf_field_args_size", [])
@@ -65,6 +66,12 @@ _lib.register("gbsdf_rgb_head_bwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp
 _lib.register("gbsdf_app_grad", [c_i64, c_i32, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_vp])
 _lib.register("gbsdf_sdf_points", [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_f32, c_vp, c_vp])
 _lib.register("gbsdf_gemm_wgrad", [c_i64, c_i32, c_i32, c_vp, c_i32, c_vp, c_i32, c_vp, c_i32, c_f32, c_f32, c_vp])
+_lib.register("gbsdf_bg_encode", [c_i64, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i32,
+                                  c_i32, c_vp])
+_lib.register("gbsdf_bg_density", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp])
+
+BG_X_COLS = 96        # background input: 84 encoding columns, the ones column at 84, zeros
+BG_S_COLS = 256 + BG_X_COLS    # [h4 | background input]: the skip layer's input (modules.py:258-261)
 
 
 def check_struct_sizes():
@@ -183,6 +190,21 @@ class FusedField:
         self.Kc0 = 256 + _round16(self.tail + 1)       # + a padding column of ones (bias gradient)
         self.F = sdf.tcnn_encoding.layout.n_features
         self.L = sdf.tcnn_encoding.layout.n_levels
+        self.bg = bool(getattr(model, "with_background", False))
+        if self.bg:
+            cb = cfg.background
+            mb = cb.mlp
+            ok = (mb.num_layers == 8 and list(mb.skip) == [4] and mb.hidden_dim == 256 and mb.num_layers_rgb == 2
+                  and mb.hidden_dim_rgb in (64, 128, 256) and mb.activ == "relu" and not mb.activ_params
+                  and mb.activ_density == "softplus" and not mb.activ_density_params and cb.view_dep
+                  and cb.encoding.type == "fourier" and cb.encoding.levels == 10
+                  and cb.encoding_view.type == "spherical" and cb.encoding_view.levels == 3 and not cb.white)
+            if not ok:
+                raise ValueError("the fused background NeRF implements the reference's base configuration "
+                                 "(8 x 256 ReLU with a skip at 4, softplus density, 10 Fourier levels, SH 3)")
+            self.n_bg = int(cb.samples)
+            self.Hbr = int(mb.hidden_dim_rgb)
+            self.Kr0 = 256 + _round16(16 + self.app_dim + 1)   # [feat | SH 16, app, 1 | 0]
         self.ws = None
         self.err = None
 
@@ -222,11 +244,59 @@ class FusedField:
             pk['bl'] = lins[-1].bias.detach().float().contiguous()
             pk['s_var'] = m.s_var.detach().reshape(1).float().contiguous()
             pk['app'] = m.appear_embed.weight.detach().float().contiguous() if self.app_dim else None
+            if self.bg:
+                self._pack_background(pk)
         self.pk = pk
+
+    def _pack_background(self, pk):
+        """FP16 working copies of the background NeRF (no weight norm), laid out for the
+        dense kernel: layer 0 padded to the 96-column input, the skip layer over
+        [h4 | input], the last layer split into its 256 feature rows and the density row
+        (modules.py:258-264)."""
+        bgm = self.model.background_nerf
+        L, Lr = bgm.mlp_feat.linears, bgm.mlp_rgb.linears
+        dev = L[0].weight.device
+        f16 = torch.float16
+        h = lambda x: x.detach().to(f16).contiguous()                      # noqa: E731
+        b = [None] * 8
+        w = [None] * 8
+        w[0] = torch.zeros(256, BG_X_COLS, device=dev, dtype=f16)
+        w[0][:, :84] = L[0].weight.detach()
+        for i in (1, 2, 3, 5, 6):
+            w[i] = h(L[i].weight)
+        w[4] = torch.zeros(256, BG_S_COLS, device=dev, dtype=f16)
+        w[4][:, :340] = L[4].weight.detach()
+        W7 = L[7].weight.detach()
+        w[7] = h(W7[1:])
+        for i in range(7):
+            b[i] = L[i].bias.detach().float().contiguous()
+        b[7] = L[7].bias.detach()[1:].float().contiguous()
+        pk['bw'], pk['bb'] = w, b
+        pk['bw7d'] = W7[0].float().contiguous()
+        pk['bb7d'] = L[7].bias.detach()[:1].float().contiguous()
+        # input-gradient operands (the dense kernel takes W^T)
+        pk['bwT'] = [None] + [w[i].t().contiguous() if i != 4 else w[4][:, :256].t().contiguous()
+                              for i in range(1, 7)]
+        w7ext = torch.zeros(272, 256, device=dev, dtype=f16)
+        w7ext[:256] = W7[1:]
+        w7ext[256] = W7[0]
+        pk['bw7extT'] = w7ext.t().contiguous()                              # [256, 272]
+        Hbr, Kr0 = self.Hbr, self.Kr0
+        wr0 = torch.zeros(Hbr, Kr0, device=dev, dtype=f16)
+        wr0[:, :256 + 16 + self.app_dim] = Lr[0].weight.detach()            # [feat | SH | app]: same order
+        pk['bwr0'], pk['bbr0'] = wr0, Lr[0].bias.detach().float().contiguous()
+        pk['bwr0T_feat'] = wr0[:, :256].t().contiguous()                    # [256, Hbr]
+        t = torch.zeros(64, Hbr, device=dev, dtype=f16)
+        t[:Kr0 - 256] = wr0[:, 256:].t()
+        pk['bwr0T_tail'] = t                                                # [64, Hbr]
+        pk['bwr1'] = Lr[1].weight.detach().float().contiguous()            # [3, Hbr]
+        pk['bbr1'] = Lr[1].bias.detach().float().contiguous()
+        ae = self.model.appear_embed_outside
+        pk['app_bg'] = ae.weight.detach().float().contiguous() if ae is not None else None
 
     # ------------------------------------------------------------------ workspace
     def _workspace(self, R, S, Ns, device):
-        key = (R, S, Ns, self.K0)
+        key = (R, S, Ns, self.K0, self.bg)
         if self.ws is not None and self.ws['key'] == key:
             return self.ws
         self.ws = None                      # release the previous shape's buffers first
@@ -249,6 +319,17 @@ class FusedField:
                   d_whead=torch.zeros(256, device=device),
                   d_bhead=torch.zeros(1, device=device), d_bl=torch.zeros(3, device=device),
                   err=torch.zeros(1, device=device, dtype=torch.int32))
+        if self.bg:
+            Nb = R * self.n_bg
+            Hbr = self.Hbr
+            ws.update(bg_S=e(Nb, BG_S_COLS, dt=f16),
+                      bg_h={i: self._with_ones(e(Nb, 264, dt=f16), 256) for i in (1, 2, 3, 5, 6, 7)},
+                      bg_G=e(Nb, self.Kr0, dt=f16), bg_hr=self._with_ones(e(Nb, Hbr + 8, dt=f16), Hbr),
+                      bg_sigma=e(Nb), bg_rgbs=e(Nb, 3), bg_weights=e(Nb), bg_d_rgbs=e(Nb, 3),
+                      bg_dZ7=torch.zeros(Nb, 272, device=device, dtype=f16),
+                      bg_d_pre_last=e(Nb, 8, dt=f16), bg_dz_r=e(Nb, Hbr, dt=f16),
+                      bg_dz=[e(Nb, 256, dt=f16) for _ in range(2)],
+                      bg_d_tail=e(Nb, 64) if self.app_dim else None, bg_d_bl=torch.zeros(3, device=device))
         self.ws = ws
         return ws
 
@@ -332,6 +413,12 @@ class FusedField:
         ylast = ws['ys'][-1]
         _lib.call("gbsdf_rgb_head_fwd", Ns, c_vp(ylast.data_ptr()), ylast.stride(0), Hc, c_vp(pk['wl'].data_ptr()),
                   c_vp(pk['bl'].data_ptr()), c_vp(ws['rgbs'].data_ptr()), stream)
+        dists_bg = None
+        if self.bg:
+            dists_bg = batch['dists_bg'].reshape(-1).contiguous().float()
+            if dists_bg.numel() != R * self.n_bg:
+                raise ValueError(f"dists_bg must hold {self.n_bg} background samples per ray")
+            self._background_forward(R, center, ray_unit, dists_bg, app_idx, stream)
         # ---------------- render + losses, fwd + bwd ----------------
         lw = m.cfg.loss_weight
         n_mean = batch.get('mean_count', Ns)
@@ -354,6 +441,11 @@ class FusedField:
         ws['loss_sums'].zero_()
         ra.d_s_var, ra.loss_sums = _p(ws['d_s_var']), _p(ws['loss_sums'])
         ra.err = _p(ws['err'])
+        if self.bg:
+            ra.n_bg, ra.ld_d_bg_pre = self.n_bg, ws['bg_dZ7'].stride(0)
+            ra.bg_dists, ra.bg_sigma, ra.bg_rgbs = _p(dists_bg), _p(ws['bg_sigma']), _p(ws['bg_rgbs'])
+            ra.bg_weights, ra.d_bg_rgbs = _p(ws['bg_weights']), _p(ws['bg_d_rgbs'])
+            ra.d_bg_pre = ws['bg_dZ7'][:, 256:].data_ptr()             # column 256: the density row of layer 7
         _lib.call("gbsdf_render_fused", ctypes.byref(ra), stream)
         # ---------------- colour MLP backward ----------------
         ws['d_bl'].zero_()
@@ -425,11 +517,84 @@ class FusedField:
         _wgrad(ws['d_pre0'], ws['x0ext'], 256, 2 * self.K0 + 16, gw0x)
         grads['w0ext'] = gw0x
         grads['table'] = d_table
+        if self.bg:
+            grads['bg'] = self._background_backward(R, app_idx, stream)
         self._scatter_grads(grads)
         self._loss_norm = (R, n_mean, float(lw.render), float(lw.eikonal), float(m.w_curv or 0.0))
         out = self.losses() if compute_loss else {}
         out['rgb'] = ws['rgb']
         return out
+
+    # ------------------------------------------------------------------ background NeRF
+    def _background_forward(self, R, center, ray_unit, dists_bg, app_idx, stream):
+        """BackgroundNeRF.forward (modules.py:268-284) of the R x n_bg background samples:
+        encode -> 8 ReLU layers with the input concatenated at layer 4 -> density head and
+        256 features -> [features, SH(d), app] -> ReLU -> sigmoid colour."""
+        ws, pk = self.ws, self.pk
+        NB, Nb, Hbr, Kr0 = self.n_bg, R * self.n_bg, self.Hbr, self.Kr0
+        S, G, h = ws['bg_S'], ws['bg_G'], ws['bg_h']
+        X = S[:, 256:]
+        Gt = G[:, 256:]
+        _lib.call("gbsdf_bg_encode", R, NB, c_vp(center.data_ptr()), c_vp(ray_unit.data_ptr()),
+                  c_vp(dists_bg.data_ptr()), c_vp(_p(pk['app_bg'])), c_vp(_p(app_idx)), self.app_dim,
+                  c_vp(X.data_ptr()), S.stride(0), BG_X_COLS, c_vp(Gt.data_ptr()), G.stride(0), Kr0 - 256, stream)
+        err = ws['err']
+        w, b = pk['bw'], pk['bb']
+        _dense(X, w[0], 256, BG_X_COLS, h[1], bias=b[0], epi=EPI_RELU, err=err)
+        _dense(h[1], w[1], 256, 256, h[2], bias=b[1], epi=EPI_RELU, err=err)
+        _dense(h[2], w[2], 256, 256, h[3], bias=b[2], epi=EPI_RELU, err=err)
+        _dense(h[3], w[3], 256, 256, S, bias=b[3], epi=EPI_RELU, err=err)            # h4 into S[:, :256]
+        _dense(S, w[4], 256, BG_S_COLS, h[5], bias=b[4], epi=EPI_RELU, err=err)      # skip: [h4 | input]
+        _dense(h[5], w[5], 256, 256, h[6], bias=b[5], epi=EPI_RELU, err=err)
+        _dense(h[6], w[6], 256, 256, h[7], bias=b[6], epi=EPI_RELU, err=err)
+        _dense(h[7], w[7], 256, 256, G, bias=b[7], epi=EPI_RELU, err=err)            # features into G[:, :256]
+        _lib.call("gbsdf_bg_density", Nb, c_vp(h[7].data_ptr()), h[7].stride(0), 256, c_vp(pk['bw7d'].data_ptr()),
+                  c_vp(pk['bb7d'].data_ptr()), c_vp(ws['bg_sigma'].data_ptr()), stream)
+        hr = ws['bg_hr']
+        _dense(G, pk['bwr0'], Hbr, Kr0, hr, bias=pk['bbr0'], epi=EPI_RELU, err=err)
+        _lib.call("gbsdf_rgb_head_fwd", Nb, c_vp(hr.data_ptr()), hr.stride(0), Hbr, c_vp(pk['bwr1'].data_ptr()),
+                  c_vp(pk['bbr1'].data_ptr()), c_vp(ws['bg_rgbs'].data_ptr()), stream)
+
+    def _background_backward(self, R, app_idx, stream):
+        """Gradients of the background NeRF from the render kernel's d colour and d density
+        pre-activation (column 256 of the layer-7 gradient buffer); weight gradients
+        dZ^T [X | 1] (loss-scaled, FP32)."""
+        ws, pk = self.ws, self.pk
+        dev = ws['bg_S'].device
+        dev32 = dict(device=dev, dtype=torch.float32)
+        Nb, Hbr, Kr0 = R * self.n_bg, self.Hbr, self.Kr0
+        S, G, h, hr = ws['bg_S'], ws['bg_G'], ws['bg_h'], ws['bg_hr']
+        dZ7, dz = ws['bg_dZ7'], ws['bg_dz']
+        err = ws['err']
+        g = {}
+        ws['bg_d_bl'].zero_()
+        _lib.call("gbsdf_rgb_head_bwd", Nb, c_vp(hr.data_ptr()), hr.stride(0), Hbr, c_vp(pk['bwr1'].data_ptr()),
+                  c_vp(ws['bg_rgbs'].data_ptr()), c_vp(ws['bg_d_rgbs'].data_ptr()),
+                  c_vp(ws['bg_d_pre_last'].data_ptr()), c_vp(ws['bg_dz_r'].data_ptr()), None,
+                  c_vp(ws['bg_d_bl'].data_ptr()), stream)
+        g['r1'] = torch.empty(3, Hbr, **dev32)
+        _wgrad(ws['bg_d_pre_last'], hr, 3, Hbr, g['r1'])
+        g['r0'] = torch.empty(Hbr, Kr0, **dev32)
+        _wgrad(ws['bg_dz_r'], G, Hbr, Kr0, g['r0'])                                 # bias column 256 + 16 + app
+        _dense(ws['bg_dz_r'], pk['bwr0T_feat'], 256, Hbr, dZ7, epi=EPI_DRELU, G=G, err=err)   # d feature pre-act
+        if self.app_dim:
+            _dense(ws['bg_dz_r'], pk['bwr0T_tail'], 64, Hbr, ws['bg_d_tail'], epi=EPI_IDENTITY, err=err)
+            g['app'] = torch.zeros_like(pk['app_bg'])
+            _lib.call("gbsdf_app_grad", R, self.n_bg, None, c_vp(app_idx.data_ptr()),
+                      c_vp(ws['bg_d_tail'].data_ptr()), 64, 16, self.app_dim, c_vp(g['app'].data_ptr()), stream)
+        g[7] = torch.empty(272, 264, **dev32)
+        _wgrad(dZ7, h[7], 272, 264, g[7])
+        _dense(dZ7, pk['bw7extT'], 256, 272, dz[0], epi=EPI_DRELU, G=h[7], err=err)       # dZ6
+        cur = 0
+        for i, gate in ((6, h[6]), (5, h[5]), (4, S), (3, h[3]), (2, h[2]), (1, h[1])):
+            X = S if i == 4 else h[i]
+            g[i] = torch.empty(256, X.shape[1], **dev32)
+            _wgrad(dz[cur], X, 256, X.shape[1], g[i])
+            _dense(dz[cur], pk['bwT'][i], 256, 256, dz[1 - cur], epi=EPI_DRELU, G=gate, err=err)
+            cur = 1 - cur
+        g[0] = torch.empty(256, BG_X_COLS, **dev32)
+        _wgrad(dz[cur], S[:, 256:], 256, BG_X_COLS, g[0])
+        return g
 
     def losses(self):
         """Loss terms of the last step (reads the FP64 device sums: synchronises)."""
@@ -498,6 +663,32 @@ class FusedField:
         _acc(m.s_var, (self.ws['d_s_var'] * inv).reshape(()))
         if self.app_dim:
             _acc(m.appear_embed.weight, g['app'] * inv)
+        if self.bg:
+            self._scatter_background(g['bg'], inv)
+
+    def _scatter_background(self, g, inv):
+        """Background NeRF gradients (plain linears) from the packed layouts into .grad."""
+        bgm = self.model.background_nerf
+        L, Lr = bgm.mlp_feat.linears, bgm.mlp_rgb.linears
+        eff = {}
+        eff['bg.l0'] = (g[0][:, :84], g[0][:, 84])
+        for i in (1, 2, 3, 5, 6):
+            eff[f'bg.l{i}'] = (g[i][:, :256], g[i][:, 256])
+        eff['bg.l4'] = (g[4][:, :340], g[4][:, 340])
+        g7 = g[7]
+        eff['bg.l7'] = (torch.cat([g7[256:257, :256], g7[:256, :256]], dim=0),
+                        torch.cat([g7[256:257, 256], g7[:256, 256]], dim=0))
+        nin = 256 + 16 + self.app_dim
+        eff['bg.rgb.l0'] = (g['r0'][:, :nin], g['r0'][:, nin])
+        eff['bg.rgb.l1'] = (g['r1'], self.ws['bg_d_bl'])
+        lins = {f'bg.l{i}': L[i] for i in range(8)}
+        lins.update({'bg.rgb.l0': Lr[0], 'bg.rgb.l1': Lr[1]})
+        self.bg_grads = {k: (dW * inv, db * inv) for k, (dW, db) in eff.items()}
+        for k, (dW, db) in self.bg_grads.items():
+            _acc(lins[k].weight, dW)
+            _acc(lins[k].bias, db)
+        if self.app_dim:
+            _acc(self.model.appear_embed_outside.weight, g['app'] * inv)
 
     def found_inf(self):
         """True when any master gradient is non-finite (skip the step, halve the scale)."""

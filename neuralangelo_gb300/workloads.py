@@ -24,14 +24,21 @@ def sphere_bounds(center, ray_unit):
     return near, far, outside
 
 
-def make_rays(R, N, seed=0, miss_frac=0.0, n_images=0, device="cpu", n_bg=0):
+def make_rays(R, N, seed=0, miss_frac=0.0, n_images=0, device="cpu", n_bg=0, miss_perpendicular=False):
+    """Dense batch.  The first miss_frac of the rays miss the unit sphere: aimed straight
+    away from it (the reference's bounds then give far < 0, its quirk), or, with
+    miss_perpendicular, across it (outside: near 1, far 1.2, as a background needs)."""
     g = torch.Generator().manual_seed(seed)
     c = torch.randn(R, 3, generator=g)
     c = 3.0 * c / c.norm(dim=-1, keepdim=True)
     d = -c + 0.3 * torch.randn(R, 3, generator=g)
     n_miss = int(round(miss_frac * R))
     if n_miss:
-        d[:n_miss] = c[:n_miss]
+        if miss_perpendicular:
+            side = torch.linalg.cross(c[:n_miss], torch.tensor([[0.3, -0.5, 0.8]]).expand(n_miss, 3), dim=-1)
+            d[:n_miss] = side
+        else:
+            d[:n_miss] = c[:n_miss]
     d = d / d.norm(dim=-1, keepdim=True)
     near, far, outside = sphere_bounds(c, d)
     u = torch.rand(R, N, generator=g)
@@ -55,7 +62,7 @@ def background_dists(far, n, u=None):
     return far / (inv + 1e-5)
 
 
-def make_ragged_rays(R, seed=0, zero_frac=0.3, lo=16, hi=256, n_images=0, device="cpu"):
+def make_ragged_rays(R, seed=0, zero_frac=0.3, lo=16, hi=256, n_images=0, device="cpu", n_bg=0):
     """Ragged batch after sphere culling and importance sampling: a ``zero_frac`` share of
     the rays miss the unit sphere and keep no samples; every other ray gets a count
     uniform in [lo, hi] of stratified samples in its [near, far].  Ray r owns the flat
@@ -83,6 +90,8 @@ def make_ragged_rays(R, seed=0, zero_frac=0.3, lo=16, hi=256, n_images=0, device
     app_idx = torch.randint(0, max(n_images, 1), (R,), generator=g)
     b = dict(center=c, ray_unit=d, dists=dists, far=far, outside=outside, target=target, app_idx=app_idx,
              ray_offsets=offs, sample_ray=sample_ray.to(torch.int32), near=near)
+    if n_bg:
+        b["dists_bg"] = background_dists(far, n_bg, torch.rand(R, n_bg, generator=g))
     return {k_: v.to(device) for k_, v in b.items()}
 
 

@@ -63,6 +63,13 @@ def model_grads(model):
         g[f'rgb.l{i}.v'], g[f'rgb.l{i}.g'], g[f'rgb.l{i}.b'] = lin.weight_v.grad, lin.weight_g.grad, lin.bias.grad
     if model.appear_embed is not None:
         g['app'] = model.appear_embed.weight.grad
+    if getattr(model, 'with_background', False):
+        bgm = model.background_nerf
+        for pre, lins in (('bg', bgm.mlp_feat.linears), ('bg.rgb', bgm.mlp_rgb.linears)):
+            for i, lin in enumerate(lins):
+                g[f'{pre}.l{i}.w'], g[f'{pre}.l{i}.b'] = lin.weight.grad, lin.bias.grad
+        if model.appear_embed_outside is not None:
+            g['app_bg'] = model.appear_embed_outside.weight.grad
     return {k: (v.detach().double().cpu() if v is not None else None) for k, v in g.items()}
 
 
@@ -116,4 +123,20 @@ def model_to_oracle(model, fp16_weights=False, effective=False):
     p['s_var'] = model.s_var.detach().double().cpu()
     if model.appear_embed is not None:
         p['app'] = model.appear_embed.weight.detach().double().cpu()
+    if getattr(model, 'with_background', False):
+        # the fused step rounds every background matrix to fp16 except the density row of
+        # layer 7 and the colour head, which stay FP32
+        bgm = model.background_nerf
+        for pre, lins in (('bg', bgm.mlp_feat.linears), ('bg.rgb', bgm.mlp_rgb.linears)):
+            for i, lin in enumerate(lins):
+                W = lin.weight.detach()
+                if fp16_weights:
+                    if pre == 'bg' and i == len(lins) - 1:
+                        W = torch.cat([W[:1], W[1:].half().float()], dim=0)
+                    elif not (pre == 'bg.rgb' and i == len(lins) - 1):
+                        W = W.half().float()
+                p[f'{pre}.l{i}.w'] = W.double().cpu()
+                p[f'{pre}.l{i}.b'] = lin.bias.detach().double().cpu()
+        if model.appear_embed_outside is not None:
+            p['app_bg'] = model.appear_embed_outside.weight.detach().double().cpu()
     return p

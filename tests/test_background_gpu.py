@@ -1,0 +1,146 @@
+"""Fused step with the background NeRF (modules.py:232-311, composited after the object
+samples as model.py:129-141 does) against the float64 oracle on the same fp16-rounded
+parameters, and against the plain FP32 path."""
+import numpy as np
+import pytest
+import torch
+
+from neuralangelo_gb300.config import field_config
+from neuralangelo_gb300.fused import FusedField
+from neuralangelo_gb300.model import FieldModel
+from neuralangelo_gb300.workloads import full_field_iteration, init_field_params, make_ragged_rays, make_rays
+from oracle import field as of
+from oracle import hashgrid as hgo
+from tests import params_io
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def build(log2T=14, n_images=10, seed=0):
+    cfg = field_config("full", background=True)
+    cfg.sdf.encoding.hashgrid.dict_size = log2T
+    cfg.appear_embed.num_images = n_images
+    torch.manual_seed(seed)
+    model = FieldModel(cfg).to(DEV)
+    init_field_params(model, seed)
+    model.schedule(full_field_iteration(8))
+    with torch.no_grad():
+        model.neural_sdf.tcnn_encoding.params.uniform_(-0.05, 0.05)
+        g = torch.Generator().manual_seed(seed + 1)
+        model.appear_embed_outside.weight.copy_(torch.randn(model.appear_embed_outside.weight.shape, generator=g))
+    return model
+
+
+def oracle_run(model, batch, effective=True):
+    c = model.cfg
+    hg = c.sdf.encoding.hashgrid
+    b = c.background.mlp
+    ocfg = of.make_config(n_levels=c.sdf.encoding.levels, n_features=hg.dim, log2_hashmap_size=hg.dict_size,
+                          base_resolution=2 ** hg.min_logres, per_level_scale=model.neural_sdf.growth_rate,
+                          active_levels=model.neural_sdf.active_levels, sdf_hidden=256,
+                          rgb_hidden=c.rgb.mlp.hidden_dim, rgb_layers=c.rgb.mlp.num_layers,
+                          app_dim=c.appear_embed.dim, n_images=c.appear_embed.num_images, bg_enabled=True,
+                          bg_hidden=b.hidden_dim, bg_hidden_rgb=b.hidden_dim_rgb)
+    layout = hgo.level_layout(ocfg['n_levels'], ocfg['n_features'], ocfg['log2_hashmap_size'],
+                              ocfg['base_resolution'], ocfg['per_level_scale'])
+    p = {k: (v.double().clone().requires_grad_(True) if v is not None else None)
+         for k, v in params_io.model_to_oracle(model, True, effective).items()}
+    bt = {k: (v.double().cpu() if v.is_floating_point() else v.cpu()) for k, v in batch.items()}
+    if 'ray_offsets' in bt:
+        out = of.render_step_ragged(p, ocfg, layout, bt, model.neural_sdf.normal_eps, model.progress, 0.1,
+                                    model.w_curv)
+    else:
+        out = of.render_step(p, ocfg, layout, bt, model.neural_sdf.normal_eps, model.progress, 0.1, model.w_curv)
+    out['loss'].backward()
+    return out, {k: (v.grad if v is not None else None) for k, v in p.items()}
+
+
+def bg_weight_errors(ff, g):
+    e = {k: rel(dW.double().cpu(), g[k + '.w']) for k, (dW, db) in ff.bg_grads.items()}
+    allw = rel(np.concatenate([ff.bg_grads[k][0].double().cpu().reshape(-1) for k in ff.bg_grads]),
+               np.concatenate([g[k + '.w'].reshape(-1) for k in ff.bg_grads]))
+    return e, allw
+
+
+def test_fused_background_matches_oracle():
+    model = build()
+    R, S = 24, 32
+    batch = make_rays(R, S, seed=6, miss_frac=0.25, n_images=10, device=DEV, n_bg=32, miss_perpendicular=True)
+    ff = FusedField(model)
+    model.zero_grad(set_to_none=True)
+    res = ff.step(batch)
+    torch.cuda.synchronize()
+    assert ff.check_device_errors() == 0
+    out, g = oracle_run(model, batch)
+    mine = params_io.model_grads(model)
+    e_rgb = rel(res['rgb'].cpu(), out['rgb'].detach())
+    e_loss = abs(res['loss'] - float(out['loss'])) / abs(float(out['loss']))
+    e_tab = rel(mine['table'], g['table'])
+    e_w, e_all = bg_weight_errors(ff, g)
+    e_app = rel(mine['app_bg'], g['app_bg'])
+    print(f"\nbackground: rgb {e_rgb:.2e} loss {e_loss:.2e} table {e_tab:.2e} bg weights {e_all:.2e} "
+          f"app_bg {e_app:.2e}")
+    print({k: f"{v:.1e}" for k, v in e_w.items()})
+    assert e_rgb < 1e-4 and e_loss < 1e-5
+    assert e_tab < 1e-3
+    assert e_all < 1e-2 and e_app < 1e-2
+
+
+def test_fused_background_matches_plain():
+    model = build(seed=3)
+    batch = make_rays(64, 64, seed=8, miss_frac=0.1, n_images=10, device=DEV, n_bg=32, miss_perpendicular=True)
+    model.zero_grad(set_to_none=True)
+    out = model.render_step(batch)
+    out['loss'].backward()
+    ref = {k: v.clone() for k, v in params_io.model_grads(model).items() if v is not None}
+    ref_loss = float(out['loss'])
+    model.zero_grad(set_to_none=True)
+    ff = FusedField(model)
+    res = ff.step(batch)
+    torch.cuda.synchronize()
+    mine = params_io.model_grads(model)
+    print(f"\nplain vs fused: loss {abs(res['loss'] - ref_loss) / abs(ref_loss):.2e}",
+          {k: f"{rel(mine[k], ref[k]):.1e}" for k in ('table', 'bg.l0.w', 'bg.l4.w', 'bg.l7.w', 'bg.rgb.l0.w',
+                                                        'bg.rgb.l1.w', 'app_bg')})
+    assert abs(res['loss'] - ref_loss) < 2e-3 * abs(ref_loss)
+    # single background layers carry fp16 activations through up to 8 layers of backward
+    assert rel(mine['table'], ref['table']) < 3e-3
+    for k in ('bg.l0.w', 'bg.l4.w', 'bg.l7.w', 'bg.rgb.l0.w', 'bg.rgb.l1.w', 'app_bg'):
+        assert rel(mine[k], ref[k]) < 6e-2, k
+
+
+def test_fused_background_ragged_matches_oracle():
+    """Ragged object samples (2..40 per ray), zero-sample rays included: those composite
+    the background only.  The table gradient is also checked with the curvature weight
+    at 0, which leaves out the curvature term's FP32-conditioned second difference."""
+    model = build()
+    batch = make_ragged_rays(40, seed=4, zero_frac=0.3, lo=2, hi=40, n_images=10, device=DEV, n_bg=32)
+    ff = FusedField(model)
+    model.zero_grad(set_to_none=True)
+    res = ff.step(batch)
+    torch.cuda.synchronize()
+    assert ff.check_device_errors() == 0
+    out, g = oracle_run(model, batch)
+    mine = params_io.model_grads(model)
+    e_rgb = rel(res['rgb'].cpu(), out['rgb'].detach())
+    e_tab = rel(mine['table'], g['table'])
+    _, e_all = bg_weight_errors(ff, g)
+    e_s = rel(mine['s_var'], g['s_var'])
+    model.w_curv = 0.0
+    model.zero_grad(set_to_none=True)
+    ff.step(batch)
+    torch.cuda.synchronize()
+    mine0 = params_io.model_grads(model)
+    _, g0 = oracle_run(model, batch)
+    e_tab0 = rel(mine0['table'], g0['table'])
+    print(f"\nragged background: rgb {e_rgb:.2e} table {e_tab:.2e} (without curvature {e_tab0:.2e}) "
+          f"bg weights {e_all:.2e} s_var {e_s:.2e}")
+    assert e_rgb < 1e-3 and e_all < 2e-2 and e_s < 1e-3
+    assert e_tab0 < 1e-3 and e_tab < 5e-3
