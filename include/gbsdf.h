@@ -260,6 +260,14 @@ typedef struct gbsdf_render_args {
     float* bg_weights;           /* [R, n_bg] out (may be NULL) */
     float* d_bg_rgbs;            /* [R, n_bg, 3] out */
     void* d_bg_pre;              /* fp16 out, row s at s * ld_d_bg_pre: d loss / d density pre-activation */
+    /* Evaluation outputs (Model.render_image / render_rays_object, model.py:90-114, 175-178),
+     * each may be NULL.  forward_only = 1 skips the losses and the backward (every d_* output
+     * and target may then be NULL). */
+    int32_t forward_only;
+    int32_t pad2;
+    float* out_opacity;          /* [R]    sum of the object samples' weights */
+    float* out_gradient;         /* [R, 3] sum of the object samples' weights x (unnormalised) gradient */
+    float* out_dist;             /* [R]    sum of weights x distance over object and background samples */
 } gbsdf_render_args;
 
 size_t gbsdf_render_args_size(void);

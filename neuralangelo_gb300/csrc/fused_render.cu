@@ -51,6 +51,7 @@ __global__ void __launch_bounds__(RENDER_WARPS * 32) k_render_fused(gbsdf_render
     // ---------------- forward: alpha, log-space transmittance, colour ----------------
     float carry = 0.0f;   // sum of log(1 - alpha) over earlier chunks
     float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
+    float op = 0.0f, gc0 = 0.0f, gc1 = 0.0f, gc2 = 0.0f, dc = 0.0f;   // evaluation composites
     float eik_sum = 0.0f, curv_sum = 0.0f;
     for (int base = 0; base < ntot; base += 32) {
         const int k = base + lane;
@@ -74,7 +75,7 @@ __global__ void __launch_bounds__(RENDER_WARPS * 32) k_render_fused(gbsdf_render
             const float Q = 1.0f / (1.0f + expf(-(sdf + ic * intv * 0.5f) * inv_s));
             a = fminf(fmaxf((P - Q) / (P + 1e-5f), 0.0f), 1.0f);
             la = log1pf(-a);
-            if (inside) {
+            if (inside && !p.forward_only) {       // losses: training only (hess may be NULL otherwise)
                 const float e = sqrtf(gx * gx + gy * gy + gz * gz) - 1.0f;
                 const float ev = e * e;
                 if (isfinite(ev)) eik_sum += ev;
@@ -101,10 +102,16 @@ __global__ void __launch_bounds__(RENDER_WARPS * 32) k_render_fused(gbsdf_render
                 const int64_t s = beg + k;
                 if (p.weights) p.weights[s] = w;
                 cp = p.rgbs + 3 * s;
+                op += w;
+                gc0 = fmaf(w, p.grad[3 * s], gc0);
+                gc1 = fmaf(w, p.grad[3 * s + 1], gc1);
+                gc2 = fmaf(w, p.grad[3 * s + 2], gc2);
+                dc = fmaf(w, p.dists[s], dc);
             } else {
                 const int64_t q = r * nb + (k - n);
                 if (p.bg_weights) p.bg_weights[q] = w;
                 cp = p.bg_rgbs + 3 * q;
+                dc = fmaf(w, p.bg_dists[q], dc);
             }
             c0 = fmaf(w, cp[0], c0);
             c1 = fmaf(w, cp[1], c1);
@@ -117,6 +124,30 @@ __global__ void __launch_bounds__(RENDER_WARPS * 32) k_render_fused(gbsdf_render
     c2 = warp_sum(c2);
     eik_sum = warp_sum(eik_sum);
     curv_sum = warp_sum(curv_sum);
+    if (p.out_opacity || p.out_gradient || p.out_dist) {
+        op = warp_sum(op);
+        gc0 = warp_sum(gc0);
+        gc1 = warp_sum(gc1);
+        gc2 = warp_sum(gc2);
+        dc = warp_sum(dc);
+        if (lane == 0) {
+            if (p.out_opacity) p.out_opacity[r] = op;
+            if (p.out_gradient) {
+                p.out_gradient[3 * r] = gc0;
+                p.out_gradient[3 * r + 1] = gc1;
+                p.out_gradient[3 * r + 2] = gc2;
+            }
+            if (p.out_dist) p.out_dist[r] = dc;
+        }
+    }
+    if (p.forward_only) {
+        if (lane == 0) {
+            p.rgb[3 * r] = c0;
+            p.rgb[3 * r + 1] = c1;
+            p.rgb[3 * r + 2] = c2;
+        }
+        return;
+    }
     const float t0 = p.target[3 * r], t1 = p.target[3 * r + 1], t2 = p.target[3 * r + 2];
     if (lane == 0) {
         p.rgb[3 * r] = c0;
@@ -352,15 +383,17 @@ extern "C" int gbsdf_render_fused(const gbsdf_render_args* a, void* stream) {
     if (p.R == 0) return GBSDF_OK;
     GBSDF_CHECK_ARG(p.S > 0 || p.ray_offsets, "need S > 0 or ray_offsets");
     GBSDF_CHECK_ARG(p.S <= MAX_RAY_SAMPLES, "S=%d exceeds %d samples per ray", p.S, MAX_RAY_SAMPLES);
-    GBSDF_CHECK_ARG(p.ray_unit && p.dists && p.far && p.target && p.s_var && p.sdf && p.grad && p.hess && p.rgbs &&
-                        p.rgb && p.d_rgbs && p.d_sdf && p.d_grad && p.d_hess && p.d_s_var && p.loss_sums,
-                    "NULL pointer");
+    GBSDF_CHECK_ARG(p.ray_unit && p.dists && p.far && p.s_var && p.sdf && p.grad && p.rgbs && p.rgb, "NULL pointer");
+    GBSDF_CHECK_ARG(p.forward_only || (p.target && p.hess && p.d_rgbs && p.d_sdf && p.d_grad && p.d_hess &&
+                                       p.d_s_var && p.loss_sums),
+                    "NULL pointer (training outputs)");
     GBSDF_CHECK_ARG(p.n_bg >= 0 && p.n_bg <= MAX_RAY_SAMPLES, "n_bg %d", p.n_bg);
     GBSDF_CHECK_ARG(p.S == 0 || p.S + p.n_bg <= MAX_RAY_SAMPLES, "S + n_bg = %d exceeds %d samples per ray",
                     p.S + p.n_bg, MAX_RAY_SAMPLES);
     if (p.n_bg > 0) {
-        GBSDF_CHECK_ARG(p.bg_dists && p.bg_sigma && p.bg_rgbs && p.d_bg_rgbs && p.d_bg_pre && p.ld_d_bg_pre >= 1,
-                        "background sample pointers");
+        GBSDF_CHECK_ARG(p.bg_dists && p.bg_sigma && p.bg_rgbs, "background sample pointers");
+        GBSDF_CHECK_ARG(p.forward_only || (p.d_bg_rgbs && p.d_bg_pre && p.ld_d_bg_pre >= 1),
+                        "background gradient pointers");
     }
     const unsigned blocks = (unsigned)((p.R + RENDER_WARPS - 1) / RENDER_WARPS);
     k_render_fused<<<blocks, RENDER_WARPS * 32, 0, as_stream(stream)>>>(p);

@@ -52,7 +52,9 @@ class RenderArgs(ctypes.Structure):
                 ("mean_scale", c_f32), ("loss_scale", c_f32), ("pad1", c_i32), ("rgb", c_vp), ("weights", c_vp),
                 ("d_rgbs", c_vp), ("d_sdf", c_vp), ("d_grad", c_vp), ("d_hess", c_vp), ("d_s_var", c_vp),
                 ("loss_sums", c_vp), ("err", c_vp), ("n_bg", c_i32), ("ld_d_bg_pre", c_i32), ("bg_dists", c_vp),
-                ("bg_sigma", c_vp), ("bg_rgbs", c_vp), ("bg_weights", c_vp), ("d_bg_rgbs", c_vp), ("d_bg_pre", c_vp)]
+                ("bg_sigma", c_vp), ("bg_rgbs", c_vp), ("bg_weights", c_vp), ("d_bg_rgbs", c_vp), ("d_bg_pre", c_vp),
+                ("forward_only", c_i32), ("pad2", c_i32), ("out_opacity", c_vp), ("out_gradient", c_vp),
+                ("out_dist", c_vp)]
 
 
 _lib.register("gbsdf_field_args_size", [])
@@ -342,7 +344,15 @@ class FusedField:
         return t
 
     # ------------------------------------------------------------------ step
-    def step(self, batch, compute_loss=True):
+    def render(self, batch):
+        """Forward only (evaluation, Model.render_rays with training off, model.py:124-190):
+        the same kernels with the render kernel's losses and backward switched off.
+        Returns per-ray rgb [R,3], opacity [R,1] (object samples), gradient [R,3] (the
+        weights' composite of the unnormalised object gradients) and dist [R,1] (composite
+        of the distances over object and background samples).  ``target`` may be absent."""
+        return self.step(batch, compute_loss=False, _evaluate=True)
+
+    def step(self, batch, compute_loss=True, _evaluate=False):
         """Forward + backward on a batch (same keys as FieldModel.render_step).
 
         Ragged batches pass ``ray_offsets`` [R+1] (int64) and flat ``dists`` [Ns];
@@ -372,7 +382,7 @@ class FusedField:
         ray_unit = batch['ray_unit'].contiguous().float()
         far = batch['far'].reshape(-1).contiguous().float()
         outside = batch['outside'].reshape(-1).to(torch.uint8).contiguous()
-        target = batch['target'].contiguous().float()
+        target = batch['target'].contiguous().float() if 'target' in batch else None
         app_idx = batch['app_idx'].to(torch.int32).contiguous() if self.app_dim else None
         stream = _lib.stream_ptr(dev)
         eps = float(sdfm.normal_eps)
@@ -446,6 +456,14 @@ class FusedField:
             ra.bg_dists, ra.bg_sigma, ra.bg_rgbs = _p(dists_bg), _p(ws['bg_sigma']), _p(ws['bg_rgbs'])
             ra.bg_weights, ra.d_bg_rgbs = _p(ws['bg_weights']), _p(ws['bg_d_rgbs'])
             ra.d_bg_pre = ws['bg_dZ7'][:, 256:].data_ptr()             # column 256: the density row of layer 7
+        if _evaluate:
+            ev = dict(opacity=torch.empty(R, 1, device=dev), gradient=torch.empty(R, 3, device=dev),
+                      dist=torch.empty(R, 1, device=dev))
+            ra.forward_only = 1
+            ra.out_opacity, ra.out_gradient, ra.out_dist = _p(ev['opacity']), _p(ev['gradient']), _p(ev['dist'])
+            _lib.call("gbsdf_render_fused", ctypes.byref(ra), stream)
+            ev['rgb'] = ws['rgb'].clone()
+            return ev
         _lib.call("gbsdf_render_fused", ctypes.byref(ra), stream)
         # ---------------- colour MLP backward ----------------
         ws['d_bl'].zero_()

@@ -118,9 +118,10 @@ class Mesh:
     """Minimal stand-in for the trimesh.Trimesh the reference returns: vertices
     [nv,3] float64 and faces [nf,3] int64 (numpy)."""
 
-    def __init__(self, vertices, faces):
+    def __init__(self, vertices, faces, colors=None):
         self.vertices = vertices
         self.faces = faces
+        self.colors = colors            # uint8 [nv, 3] for a textured mesh
 
 
 def finalize_mesh(V, F, weld=False, digits=MERGE_DIGITS, scale=1.0, offset=(0.0, 0.0, 0.0), min_side=MERGE_TOL):
@@ -210,8 +211,8 @@ def export_mesh(mesh, path, sphere_radius=1.0, sphere_center=(0.0, 0.0, 0.0), de
     V = torch.as_tensor(np.asarray(mesh.vertices, np.float64), device=device).reshape(-1, 3)
     F = torch.as_tensor(np.asarray(mesh.faces, np.int64), device=device).reshape(-1, 3)
     Vo, Fo = finalize_mesh(V, F, weld=False, scale=sphere_radius, offset=sphere_center, min_side=MERGE_TOL)
-    out = Mesh(Vo.cpu().numpy(), Fo.cpu().numpy())
-    write_ply(path, out.vertices, out.faces)
+    out = Mesh(Vo.cpu().numpy(), Fo.cpu().numpy(), getattr(mesh, "colors", None))
+    write_ply(path, out.vertices, out.faces, colors=out.colors)
     return out
 
 
@@ -225,13 +226,15 @@ def extract_mesh(sdf_func, bounds, intv, block_res=64, texture_func=None, filter
     """extract_mesh of the reference (mesh.py:25-49) on the GPU; returns a Mesh.
     merge_vertices=True also runs the per-block vertex merge that the reference's
     trimesh.Trimesh(V, F) applies (mesh.py:124-126: coordinates equal at 8 decimals),
-    keeping every face as trimesh does there."""
-    if texture_func is not None or filter_lcc:
-        raise NotImplementedError("texture and largest-component filtering are outside this path")
+    keeping every face as trimesh does there.  texture_func (points [n,3] numpy -> uint8
+    colours [n,3], e.g. ``inference.extract_texture`` bound to a model) colours each
+    block's vertices, as marching_cubes does before its sphere filter (mesh.py:121-128)."""
+    if filter_lcc:
+        raise NotImplementedError("largest-component filtering is outside this path")
     axes = lattice_axes(bounds, intv, device)
     nblk = [int(np.ceil(len(a) / block_res)) for a in axes]
     mc = MarchingCubes(block_res + 1, device)
-    Vs, Fs, off = [], [], 0
+    Vs, Fs, Cs, off = [], [], [], 0
     for bx in range(nblk[0]):
         for by in range(nblk[1]):
             for bz in range(nblk[2]):
@@ -252,7 +255,10 @@ def extract_mesh(sdf_func, bounds, intv, block_res=64, texture_func=None, filter
                     V, F = finalize_mesh(V, F, weld=True, min_side=-1.0)
                 Vs.append(V.cpu().numpy())
                 Fs.append(F.cpu().numpy() + off)
+                if texture_func is not None:
+                    Cs.append(np.asarray(texture_func(Vs[-1]), np.uint8).reshape(-1, 3))
                 off += V.shape[0]
     if not Vs:
-        return Mesh(np.zeros((0, 3)), np.zeros((0, 3), np.int64))
-    return Mesh(np.concatenate(Vs), np.concatenate(Fs))
+        return Mesh(np.zeros((0, 3)), np.zeros((0, 3), np.int64),
+                    np.zeros((0, 3), np.uint8) if texture_func is not None else None)
+    return Mesh(np.concatenate(Vs), np.concatenate(Fs), np.concatenate(Cs) if Cs else None)

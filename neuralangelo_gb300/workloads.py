@@ -57,8 +57,8 @@ def background_dists(far, n, u=None):
     1e-5); u [R, n] in [0, 1), or 0.5 when not stratified.  far [R, 1] -> [R, n]."""
     R = far.shape[0]
     if u is None:
-        u = torch.full((R, n), 0.5)
-    inv = (u + torch.arange(n, dtype=torch.float32)[None]) / n * (0.0 - 1.0) + 1.0
+        u = torch.full((R, n), 0.5, device=far.device)
+    inv = (u + torch.arange(n, dtype=torch.float32, device=far.device)[None]) / n * (0.0 - 1.0) + 1.0
     return far / (inv + 1e-5)
 
 

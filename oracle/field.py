@@ -521,3 +521,34 @@ def render_step_ragged(p, cfg, layout, batch, eps, progress, w_eik, w_curv, mean
     if w_curv:
         loss = loss + w_curv * l_curv
     return dict(loss=loss, l_render=l_render, l_eik=l_eik, l_curv=l_curv, rgb=rgb, sdf=torch.cat(sdf_flat))
+
+
+def render_eval(p, cfg, layout, batch, eps, progress):
+    """Model.render_rays + render_image with training off (model.py:90-114, 158-190):
+    rgb over object and background samples, opacity and the gradient composite over the
+    object samples' own weights, and the distance composite over all samples."""
+    c, d, dists = batch['center'], batch['ray_unit'], batch['dists']
+    R, N = dists.shape
+    pts = c[:, None, :] + d[:, None, :] * dists[..., None]
+    sdf, feat = neural_sdf(p, cfg, layout, pts, with_feat=True)
+    out_val = 1000.0 * (-1 if cfg['inside_out'] else 1)
+    sdf = torch.where(batch['outside'][:, None, :].expand_as(sdf), torch.full_like(sdf, out_val), sdf)
+    grads, _ = compute_gradients(p, cfg, layout, pts, eps, sdf, training=False)
+    normals = F.normalize(grads, dim=-1)
+    app = None
+    if cfg['app_dim'] > 0:
+        app = p['app'][batch['app_idx']][:, None, :].expand(R, N, cfg['app_dim'])
+    rgbs = neural_rgb(p, cfg, pts, normals, d[:, None, :].expand_as(pts), feat, app)
+    alphas = neus_alphas(d, sdf[..., 0], grads, dists, batch['far'], p['s_var'], progress, cfg['anneal_end'])
+    w_obj = compositing_weights(alphas)
+    opacity = w_obj.sum(dim=1, keepdim=True)
+    gradient = (grads * w_obj[..., None]).sum(dim=1)
+    rgbs_all, alphas_all, dists_all = rgbs, alphas, dists
+    if cfg.get('bg_enabled') and batch.get('dists_bg') is not None:
+        rgbs_bg, alphas_bg = background_branch(p, cfg, c, d, batch['dists_bg'], batch.get('app_idx'))
+        rgbs_all = torch.cat([rgbs, rgbs_bg], dim=1)
+        alphas_all = torch.cat([alphas, alphas_bg], dim=1)
+        dists_all = torch.cat([dists, batch['dists_bg']], dim=1)
+    w = compositing_weights(alphas_all)
+    return dict(rgb=(rgbs_all * w[..., None]).sum(dim=1), opacity=opacity, gradient=gradient,
+                dist=(dists_all * w).sum(dim=1, keepdim=True), normals=normals, feat=feat)
