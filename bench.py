@@ -333,25 +333,13 @@ def main():
         run_reference(args)
         return
     import torch
-    import torch.distributed as dist
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     device = f"cuda:{local}"
     torch.cuda.set_device(device)
-
-    def barrier():
-        if world > 1:
-            dist.barrier()
-
-    def max_over_ranks(v):
-        if world == 1:
-            return v
-        t = torch.tensor([v], device=device, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t)
+    from neuralangelo_gb300.replicas import ReplicaGroup
+    group = ReplicaGroup()            # replicas: one independent field per rank, shared timing only
+    world, rank = group.world, group.rank
+    barrier, max_over_ranks = group.barrier, group.max
 
     import __graft_entry__
     __graft_entry__.build()
@@ -507,8 +495,7 @@ def main():
                     kernel_rooflines=rooflines,
                     **extras)
         print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.destroy_process_group()
+    group.close()
 
 
 if __name__ == "__main__":
