@@ -386,21 +386,32 @@ def main():
     if not args.no_plain or fused is None:
         plain_ms, plain_k = measure(lambda: step_plain(model, batch), max(2, args.steps // 2), args.warmup)
         plain_ms = max_over_ranks(plain_ms)
+    cap = None
+    if fused is not None:
+        # per-call device times (CUDA events around every C-ABI call) from eager steps;
+        # the headline then times the same step launched as one CUDA graph (CapturedStep)
+        ksteps = max(3, args.steps // 2)
+        _, ksum = measure(lambda: step_fused(batch), ksteps, args.warmup)
+        from neuralangelo_gb300.fused import CapturedStep
+        cap = CapturedStep(fused, batch)
     clocks = ClockSampler(local)
     clocks.start()
-    if fused is not None:
-        ms, ksum = measure(lambda: step_fused(batch), args.steps, args.warmup)
+    if cap is not None:
+        ms = time_steps(cap.replay, args.steps, args.warmup, barrier)
     else:
         ms, ksum = measure(lambda: step_plain(model, batch), args.steps, args.warmup)
+        ksteps = args.steps
     clock = clocks.stop()
     ms = max_over_ranks(ms)
     value = world * n_samples / (ms * 1e-3)
 
-    # end to end through the public API: H2D of the batch, step, D2H of the loss
+    # end to end through the public API: H2D of the batch (from pinned memory) into the
+    # graph's inputs, the step, D2H of the loss
     def e2e_step():
+        if cap is not None:
+            cap.replay(pinned)
+            return cap.losses()["loss"]
         b = {k: v.to(device, non_blocking=True) for k, v in pinned.items()}
-        if fused is not None:
-            return step_fused(b, compute_loss=True)["loss"]
         return float(step_plain(model, b).detach().cpu())
 
     e2e_ms = time_steps(e2e_step, max(1, args.steps // 2), 1, barrier)
@@ -451,7 +462,7 @@ def main():
         r.update(traffic=traffic, traffic_source=tsrc,
                  dram_gbs=round(traffic / t / 1e9, 1) if traffic else None,
                  per_launch_ms=round(per_launch_ms, 4), algorithmic_bytes_per_launch=by, flops_per_launch=fl,
-                 tensor_tflops=round(fl / t / 1e12, 2), launches_per_step=calls / args.steps)
+                 tensor_tflops=round(fl / t / 1e12, 2), launches_per_step=calls / ksteps)
         return r
 
     timed = [(k, v) for k, v in ksum.items() if k in work]
@@ -461,10 +472,12 @@ def main():
     rooflines = {k: {x: y for x, y in roofline_of(k, *v).items()
                      if x in ("bound", "achieved", "unit", "frac", "per_launch_ms", "dram_gbs")}
                  for k, v in timed}
-    launches = int(sum(c * KERNELS_PER_CALL.get(k, 1) for k, (c, _) in ksum.items()) / args.steps)
+    launches = int(sum(c * KERNELS_PER_CALL.get(k, 1) for k, (c, _) in ksum.items()) / ksteps)
     extras = {}
     if not args.no_extras and fused is not None:
+        cap = None                     # the graph holds the workspace; drop both before the extras
         fused.release()
+        torch.cuda.empty_cache()
         torch.cuda.empty_cache()
         extras["ragged"] = bench_ragged(model, device, max(3, args.steps // 2), args.warmup)
         extras["background"] = bench_background(device, max(3, args.steps // 2), args.warmup)
@@ -491,7 +504,7 @@ def main():
                     roofline=roof, cpu_baseline=cb, gpu_launches=launches, clocks=clock,
                     flops_per_sample=flops_per_sample(model.cfg, ACTIVE),
                     encoder_bytes_per_sample=encoder_bytes_per_sample(ACTIVE, 8, 4),
-                    kernel_ms_per_step={k: round(v[1] / args.steps, 4) for k, v in ksum.items()},
+                    kernel_ms_per_step={k: round(v[1] / ksteps, 4) for k, v in ksum.items()},
                     kernel_rooflines=rooflines,
                     **extras)
         print(json.dumps(line), flush=True)
