@@ -433,9 +433,10 @@ def main():
         # x0ext rows -> SDF, gradient, Hessian, h0c row, colour-input tail
         "gbsdf_field_mlp_fwd": (n_samples * (7 * KX * 2 + 4 + 12 + 12 + (H + 8) * 2 + 48 * 2),
                                 n_samples * 7 * 2 * H * (K0 + 4 + 1)),
-        # x0ext rows, d_h0c and the per-sample output gradients -> d_pre0 (fp16), d_enc (fp32)
-        "gbsdf_field_mlp_bwd": (n_samples * (7 * KX * 2 + H * 4 + 52 + 7 * H * 2 + 7 * K0 * 4),
-                                n_samples * 7 * 2 * H * (2 * K0 + 4 + 1)),
+        # x0ext rows, d_h0c and the per-sample output gradients -> d_enc (fp32) and, K0 <= 64,
+        # the layer-0 weight gradient in-kernel (extra MACs, no traffic), else d_pre0 (fp16)
+        "gbsdf_field_mlp_bwd": (n_samples * (7 * KX * 2 + H * 4 + 52 + (0 if K0 <= 64 else 7 * H * 2) + 7 * K0 * 4),
+                                n_samples * 7 * 2 * H * (2 * K0 + 4 + 1 + (K0 + 4 if K0 <= 64 else 0))),
         # d_enc -> FP32 read-modify-write of every corner touch
         "gbsdf_field_scatter": (n_samples * (7 * K0 * 4 + 7 * A * 8 * F * 8 + 4), 0),
     }

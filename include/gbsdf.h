@@ -197,6 +197,10 @@ typedef struct gbsdf_field_args {
     float* d_whead;          /* [256] accumulated */
     float* d_bhead;          /* [1] accumulated */
     int32_t* err;            /* device flag for timed-out waits */
+    float* d_w0;             /* [256, K0 + 16] accumulated layer-0 weight gradient: columns
+                                [0, K0) the features (hi + lo), [K0, K0 + 16) the x0ext tail.
+                                Non-NULL (K0 <= 64): the backward accumulates it itself and
+                                leaves d_pre0 unused (may be NULL); NULL: it writes d_pre0 */
 } gbsdf_field_args;
 
 size_t gbsdf_field_args_size(void);

@@ -550,7 +550,17 @@ constexpr int BWD_STAGE_BYTES = 4096;            // per warp: 32 rows x 128 byte
 constexpr int TILE_ROWS = SPT * EVALS;           // 126
 constexpr int DH0_LD = HID + 4;                  // d_h0c rows in shared memory, padded against bank conflicts
 
-template <int F>
+// DW (K0 <= 64, the caller passes d_w0): the layer-0 weight gradient dW0 = d_pre^T [x hi |
+// tail] + d_pre^T x lo is accumulated here instead of through d_pre0 and a separate GEMM.
+//   * d_pre's hi/lo pair is written over MMA1's accumulator in place (chunk c: hi in
+//     columns [16c, 16c + 8), lo in [16c + 8, 16c + 16)), which frees TMEM for MMA2's
+//     result at 256 and two dW0 accumulators (hidden halves, K0 + 16 columns each) after it.
+//   * The dW0 MMAs read both operands MN-major: A = the d_pre hi rows of the staging
+//     buffers (128-byte swizzle atoms of 64 hidden units x 8 rows), B = the tile's x0ext rows.
+//   * The feature tile is double-buffered: the next tile's load may not overwrite what
+//     dW0 reads.  dW0 goes before MMA2, so MMA2's completion also frees the staging rows.
+//   * Each CTA adds its dW0 into d_w0 with atomics at the end.
+template <int F, bool DW>
 __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
                                                              const __grid_constant__ CUtensorMap tm_pre32,
                                                              const __grid_constant__ CUtensorMap tm_pre30,
@@ -562,9 +572,11 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     const int KX = 2 * K0 + 16;                                 // x0ext row width
     uint8_t* stage_s = smem;                                    // [16 warps][4 KB] TMA store staging
     uint8_t* w_s = stage_s + (BWD_THREADS / 32) * BWD_STAGE_BYTES;   // [256 x KB]  w0b: B of MMA1
-    uint8_t* a_s = w_s + HID * KB * 2;                          // [128 x KB]  features hi | tail
-    uint8_t* a3_s = a_s + TILE_M * KB * 2;                      // [128 x K0]  features lo
-    float* wh_s = reinterpret_cast<float*>(a3_s + TILE_M * K0 * 2);   // [256] head weights
+    uint8_t* a_s0 = w_s + HID * KB * 2;                         // [128 x KB]  features hi | tail
+    uint8_t* a3_s0 = a_s0 + TILE_M * KB * 2;                    // [128 x K0]  features lo
+    uint8_t* a_s1 = DW ? a3_s0 + TILE_M * K0 * 2 : a_s0;        // the second buffer (DW)
+    uint8_t* a3_s1 = DW ? a_s1 + TILE_M * KB * 2 : a3_s0;
+    float* wh_s = reinterpret_cast<float*>(a3_s1 + TILE_M * K0 * 2);   // [256] head weights
     float* dwh_s = wh_s + HID;                                  // [256] d_whead accumulator
     float* df_s = dwh_s + HID;                                  // [2][7][18] d f per evaluation, double-buffered
     float* dh0_s = df_s + 2 * EVALS * SPT + 4;                  // [18][DH0_LD] d_h0c of the tile's samples
@@ -589,11 +601,20 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     __syncthreads();
     umma::fence_after_sync();
     const uint32_t tmem = *tslot;
-    const uint32_t t_hi = tmem + HID, t_lo = tmem + HID + HID / 2;
+    // d_pre hi/lo of hidden units [16c, 16c + 16): separate TMEM regions, or in place (DW)
+    auto t_hi = [&](int c) { return DW ? tmem + 16u * c : tmem + HID + 8u * c; };
+    auto t_lo = [&](int c) { return DW ? tmem + 16u * c + 8u : tmem + HID + HID / 2 + 8u * c; };
+    const uint32_t t_enc = DW ? tmem + HID : tmem;              // MMA2's result
+    const uint32_t t_dw = tmem + HID + K0;                      // DW: dW0 of hidden half h at + h KB
     const uint32_t idesc1 = umma::idesc_f16(TILE_M, HID);
     const uint32_t idesc2 = umma::idesc_f16_bmn(TILE_M, K0);
-    const uint32_t a_addr = umma::smem_u32(a_s), w_addr = umma::smem_u32(w_s);
-    const uint32_t a3_addr = umma::smem_u32(a3_s);
+    const uint32_t w_addr = umma::smem_u32(w_s);
+    // feature buffer b (0, or 1 with DW): selects, not arrays, which would go to local memory
+    auto a_buf = [&](int b) { return b ? a_s1 : a_s0; };
+    auto a3_buf = [&](int b) { return b ? a3_s1 : a3_s0; };
+    auto a_addr = [&](int b) { return umma::smem_u32(a_buf(b)); };
+    auto a3_addr = [&](int b) { return umma::smem_u32(a3_buf(b)); };
+    bool dw_first = true;                                       // the CTA's first dW0 MMA initialises
     const int64_t ntiles = (p.Ns + SPT - 1) / SPT;
     const int q = warp & 3, part = warp >> 2;                   // lane quadrant, quarter of the hidden units
     const int row = q * 32 + lane;
@@ -674,10 +695,10 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     // are never used), and the d_h0c rows of its 18 samples; the next tile's load
     // overlaps this tile's epilogue
     const int64_t xrows = ntiles * (int64_t)(SPT * EVALS);
-    auto stage_a = [&](int64_t tt) {               // one cp.async group
+    auto stage_a = [&](int64_t tt, int buf) {      // one cp.async group
         const __half* xb = (const __half*)p.x0ext;
-        stage_rows_kmajor(a_s, xb, tt * (SPT * EVALS), xrows, KX, KB, tid, BWD_THREADS);
-        stage_rows_kmajor(a3_s, xb + K0 + 16, tt * (SPT * EVALS), xrows, KX, K0, tid, BWD_THREADS);
+        stage_rows_kmajor(a_buf(buf), xb, tt * (SPT * EVALS), xrows, KX, KB, tid, BWD_THREADS);
+        stage_rows_kmajor(a3_buf(buf), xb + K0 + 16, tt * (SPT * EVALS), xrows, KX, K0, tid, BWD_THREADS);
         cp_async_commit();
     };
     auto stage_dh0 = [&](int64_t tt) {             // one cp.async group
@@ -690,11 +711,11 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         }
         cp_async_commit();
     };
-    auto issue1 = [&]() {
+    auto issue1 = [&](int buf) {
         if (tid == 0) {
             umma::fence_after_sync();
-            issue_tile_mma_strided(tmem, a3_addr, K0, w_addr, KB, K0, idesc1);   // residuals first
-            issue_tile_mma(tmem, a_addr, w_addr, KB, idesc1, true);
+            issue_tile_mma_strided(tmem, a3_addr(buf), K0, w_addr, KB, K0, idesc1);   // residuals first
+            issue_tile_mma(tmem, a_addr(buf), w_addr, KB, idesc1, true);
             umma::mma_commit(mbar);
         }
     };
@@ -704,13 +725,13 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         prologue_load(t, pin);
         prologue_ray(t, pin);
         prologue_finish(t, pin, 0);
-        stage_a(t);
+        stage_a(t, 0);
         stage_dh0(t);
         cp_async_wait_all();
         umma::fence_proxy_async_smem();
     }
     __syncthreads();
-    if (t < ntiles) issue1();
+    if (t < ntiles) issue1(0);
     int it = 0;
     for (; t < ntiles && ok; t += gridDim.x, ++it) {
         const int64_t s0 = t * SPT;
@@ -722,9 +743,10 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
             break;
         }
         const int64_t tn = t + gridDim.x;
+        const int cb = DW ? (it & 1) : 0, nb = DW ? ((it + 1) & 1) : 0;   // this tile's / the next tile's A
         umma::fence_after_sync();
         if (tn < ntiles) {
-            stage_a(tn);                             // A is free: MMA1 of tile t completed
+            stage_a(tn, nb);                         // free: MMA1 of tile t completed (DW: the other buffer)
             prologue_load(tn, pin);                  // consumed at the end of the tile
         }
         // (2) d_pre = (d f * w_head + [centre] d_h0c) * softplus'(pre) -> TMEM (hi, lo) and d_pre0
@@ -787,8 +809,8 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
                     lo[i] = *reinterpret_cast<const uint32_t*>(&l2);
                 }
                 if (more) umma::tmem_ld_wait16(rn);
-                umma::tmem_st8(umma::taddr(t_hi, q * 32, c0 / 2), hi);
-                umma::tmem_st8(umma::taddr(t_lo, q * 32, c0 / 2), lo);
+                umma::tmem_st8(umma::taddr(t_hi(c0 >> 4), q * 32, 0), hi);
+                umma::tmem_st8(umma::taddr(t_lo(c0 >> 4), q * 32, 0), lo);
                 // d_pre0 (hi) into the staging rows; dead samples store zeros (their x0ext
                 // rows are zero too).  128-byte swizzle: 16-byte unit u of row r sits at u ^ (r & 7)
                 const int u = (c0 - part * 64) >> 3;
@@ -800,7 +822,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         }
         umma::fence_proxy_async_smem();
         __syncwarp();
-        if (lane == 0) {
+        if (!DW && lane == 0) {
             umma::tma_store_2d(tm_pre, part * 64, y0, stg);
             umma::bulk_commit();
         }
@@ -812,17 +834,39 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         // feature columns 8c..8c+7 sits at g * KB * 16 + c * 128 bytes)
         if (tid == 0) {
             umma::fence_after_sync();
+            if constexpr (DW) {
+                // dW0[h] += d_pre^T [x hi | tail], then += d_pre^T x lo on the first K0 columns.
+                // A (hidden half h = staging parts 2h, 2h + 1): atoms of 64 units x 8 rows, next
+                // 64 units 16 KB on, next 8 rows 1 KB on; B (the tile's rows, MN-major): next 8
+                // rows KB*16 (K0*16) bytes on, next 8 features 128 bytes on.
+                const uint32_t st = umma::smem_u32(stage_s);
+                const uint32_t id_b = umma::idesc_f16_mn(TILE_M, KB), id_l = umma::idesc_f16_mn(TILE_M, K0);
+                for (int h = 0; h < 2; ++h) {
+                    const uint32_t d = t_dw + (uint32_t)(h * KB);
+                    for (int ks = 0; ks < TILE_M / 16; ++ks) {
+                        const uint64_t ad = umma::make_desc_sw128_mn(st + h * 32768u + ks * 2048u, 16384u, 1024u);
+                        const uint64_t bd = umma::make_desc(a_addr(cb) + ks * 2u * KB * 16u, KB * 16u, 128u);
+                        umma::mma_f16(d, ad, bd, id_b, (dw_first && ks == 0) ? 0u : 1u);
+                    }
+                    for (int ks = 0; ks < TILE_M / 16; ++ks) {
+                        const uint64_t ad = umma::make_desc_sw128_mn(st + h * 32768u + ks * 2048u, 16384u, 1024u);
+                        const uint64_t bd = umma::make_desc(a3_addr(cb) + ks * 2u * K0 * 16u, K0 * 16u, 128u);
+                        umma::mma_f16(d, ad, bd, id_l, 1u);
+                    }
+                }
+            }
             const uint32_t lbo = (uint32_t)KB * 16u;          // next 8 hidden units (K)
             for (int ks = 0; ks < HID / 16; ++ks) {          // the lo half first (smaller addends)
                 const uint64_t bd = umma::make_desc(w_addr + ks * 2u * lbo, lbo, 128u);
-                umma::mma_f16_ta(tmem, t_lo + ks * 8, bd, idesc2, ks > 0 ? 1u : 0u);
+                umma::mma_f16_ta(t_enc, t_lo(ks), bd, idesc2, ks > 0 ? 1u : 0u);
             }
             for (int ks = 0; ks < HID / 16; ++ks) {
                 const uint64_t bd = umma::make_desc(w_addr + ks * 2u * lbo, lbo, 128u);
-                umma::mma_f16_ta(tmem, t_hi + ks * 8, bd, idesc2, 1u);
+                umma::mma_f16_ta(t_enc, t_hi(ks), bd, idesc2, 1u);
             }
             umma::mma_commit(mbar);
         }
+        if constexpr (DW) dw_first = false;
         if (tn < ntiles) {
             stage_dh0(tn);                           // every warp has read this tile's d_h0c rows
             prologue_ray(tn, pin);
@@ -837,11 +881,11 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         // (4) d_enc rows to global for k_field_scatter: 16-column chunks dealt in turn
         // to the four warps of a lane quadrant (K0 <= 128: at most two per warp, one
         // 2 KB half of the staging buffer each; 64-byte swizzle: unit j of row r at j ^ ((r >> 1) & 3))
-        if (lane == 0) umma::bulk_wait_read0();      // the d_pre0 store has read the buffer
+        if (lane == 0) umma::bulk_wait_read0();      // the d_pre0 store (or, DW, dW0's MMAs) has read it
         __syncwarp();
         for (int c0 = part * 16, i = 0; c0 < K0; c0 += 64, ++i) {
             float v[16];
-            umma::tmem_ld16(umma::taddr(tmem, q * 32, c0), v);
+            umma::tmem_ld16(umma::taddr(t_enc, q * 32, c0), v);
             uint8_t* eb = stg + i * 2048;
 #pragma unroll
             for (int j = 0; j < 4; ++j)
@@ -861,12 +905,30 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
             umma::fence_proxy_async_smem();
         }
         __syncthreads();   // the TMEM accumulator of tile t read; tile tn's A tile and d f in place
-        if (tn < ntiles) issue1();
+        if (tn < ntiles) issue1(nb);
     }
     cp_async_wait_all();
     if (lane == 0) umma::bulk_wait0();               // this warp's TMA stores have completed
     umma::fence_before_sync();
     __syncthreads();
+    if constexpr (DW) {
+        // the CTA's dW0 (complete: the last MMA2 completion covered it): warps with part 2h, 2h + 1
+        // read hidden half h, one half of its KB columns each
+        if (!dw_first && ok) {
+            umma::fence_after_sync();
+            const int h = part >> 1, half_cols = KB / 2, cbeg = (part & 1) * half_cols;
+            float* dst = p.d_w0 + (int64_t)(h * 128 + q * 32 + lane) * KB;
+            for (int c = cbeg; c < cbeg + half_cols; c += 8) {
+                float v[8];
+                umma::tmem_ld8(umma::taddr(t_dw + (uint32_t)(h * KB), q * 32, c), v);
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    if (v[j] != 0.0f) atomicAdd(dst + c + j, v[j]);
+            }
+        }
+        umma::fence_before_sync();
+        __syncthreads();
+    }
     for (int i = tid; i < HID; i += BWD_THREADS)
         if (dwh_s[i] != 0.0f) atomicAdd(&p.d_whead[i], dwh_s[i]);
     dbh = warp_sum(dbh);
@@ -1011,10 +1073,11 @@ static size_t fwd_smem(int K0) {
     const size_t KB = (size_t)K0 + 16;
     return (size_t)HID * KB * 2 + (size_t)TILE_M * (KB + K0) * 2 + (HID + 2 * TILE_M + EVALS * SPT + 2) * 4 + 16;
 }
-static size_t bwd_smem(int K0) {
+static size_t bwd_smem(int K0, bool dw) {
     const size_t KB = (size_t)K0 + 16;
     const size_t need = (size_t)(BWD_THREADS / 32) * BWD_STAGE_BYTES + (size_t)HID * KB * 2 +
-                        (size_t)TILE_M * (KB + K0) * 2 + (2 * HID + 2 * EVALS * SPT + 4 + SPT * DH0_LD) * 4 + 16;
+                        (size_t)TILE_M * (KB + K0) * 2 * (dw ? 2 : 1) +
+                        (2 * HID + 2 * EVALS * SPT + 4 + SPT * DH0_LD) * 4 + 16;
     return need > BWD_SMEM_FLOOR ? need : BWD_SMEM_FLOOR;
 }
 
@@ -1051,12 +1114,14 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
         if (int st = launch_status("field forward")) return st;
     }
     if (which & FK_MLP_BWD) {
-        const size_t smem = bwd_smem(p.K0);
+        const bool dw = p.d_w0 != nullptr;
+        const size_t smem = bwd_smem(p.K0, dw);
         if (smem > 227 * 1024) {
             set_error("field backward needs %zu B of shared memory", smem);
             return GBSDF_ERR_UNSUPPORTED;
         }
-        // d_pre0 [126 T, 256] fp16 and d_enc [126 T, K0] fp32 as TMA store targets
+        // d_pre0 [126 T, 256] fp16 (without d_w0) and d_enc [126 T, K0] fp32 as TMA store
+        // targets; with d_w0 the d_pre0 maps are never used and describe d_enc's memory
         const int64_t rows = ntiles * TILE_ROWS;
         if (rows >= ((int64_t)1 << 31)) {
             set_error("%lld backward rows exceed the TMA coordinate range", (long long)rows);
@@ -1064,22 +1129,30 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
         }
         CUtensorMap tm_pre32, tm_pre30, tm_enc32, tm_enc30;
         const CUtensorMapL2promotion l2n = CU_TENSOR_MAP_L2_PROMOTION_NONE;
-        if (int st = tensor_map_2d(&tm_pre32, false, p.d_pre0, rows, HID, HID, 64, 32, CU_TENSOR_MAP_SWIZZLE_128B,
-                                   l2n, "d_pre0"))
-            return st;
-        if (int st = tensor_map_2d(&tm_pre30, false, p.d_pre0, rows, HID, HID, 64, 30, CU_TENSOR_MAP_SWIZZLE_128B,
-                                   l2n, "d_pre0"))
-            return st;
+        if (!dw) {
+            if (int st = tensor_map_2d(&tm_pre32, false, p.d_pre0, rows, HID, HID, 64, 32,
+                                       CU_TENSOR_MAP_SWIZZLE_128B, l2n, "d_pre0"))
+                return st;
+            if (int st = tensor_map_2d(&tm_pre30, false, p.d_pre0, rows, HID, HID, 64, 30,
+                                       CU_TENSOR_MAP_SWIZZLE_128B, l2n, "d_pre0"))
+                return st;
+        }
         if (int st = tensor_map_2d(&tm_enc32, true, p.d_enc, rows, p.K0, p.K0, 16, 32, CU_TENSOR_MAP_SWIZZLE_64B, l2n,
                                    "d_enc"))
             return st;
         if (int st = tensor_map_2d(&tm_enc30, true, p.d_enc, rows, p.K0, p.K0, 16, 30, CU_TENSOR_MAP_SWIZZLE_64B, l2n,
                                    "d_enc"))
             return st;
+        if (dw) tm_pre32 = tm_pre30 = tm_enc32;
         int64_t grid = num_sms();
         if (grid > ntiles) grid = ntiles;
-        cudaFuncSetAttribute(k_field_bwd<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_field_bwd<F><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30);
+        if (dw) {
+            cudaFuncSetAttribute(k_field_bwd<F, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_field_bwd<F, true><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30);
+        } else {
+            cudaFuncSetAttribute(k_field_bwd<F, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_field_bwd<F, false><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30);
+        }
         if (int st = launch_status("field backward")) return st;
     }
     if (which & FK_SCATTER) {
@@ -1141,10 +1214,12 @@ static int check_bwd(const FieldParams& p, int which) {
     GBSDF_CHECK_ARG(p.d_enc && aligned(p.d_enc, 16), "d_enc missing or misaligned");
     if (which & FK_MLP_BWD) {
         GBSDF_CHECK_ARG(p.w0b && aligned(p.w0b, 16), "w0b (fp16 [256, K0 + 16]) missing or misaligned");
-        GBSDF_CHECK_ARG(p.grad && p.d_sdf && p.d_grad && p.d_hess && p.d_xc && p.d_h0c && p.d_pre0 && p.x0ext &&
-                            p.d_whead && p.d_bhead,
+        GBSDF_CHECK_ARG(p.grad && p.d_sdf && p.d_grad && p.d_hess && p.d_xc && p.d_h0c && p.x0ext && p.d_whead &&
+                            p.d_bhead,
                         "NULL pointer");
-        GBSDF_CHECK_ARG(aligned(p.d_pre0, 16) && aligned(p.d_h0c, 16), "d_pre0 / d_h0c alignment");
+        GBSDF_CHECK_ARG(p.d_w0 || (p.d_pre0 && aligned(p.d_pre0, 16)), "d_pre0 missing or misaligned (no d_w0)");
+        GBSDF_CHECK_ARG(!p.d_w0 || p.K0 <= 64, "d_w0 needs K0 <= 64 (K0 %d): pass d_pre0 instead", p.K0);
+        GBSDF_CHECK_ARG(aligned(p.d_h0c, 16), "d_h0c alignment");
     }
     if (which & FK_SCATTER) GBSDF_CHECK_ARG(p.d_table && aligned(p.d_table, 16), "d_table missing or misaligned");
     return GBSDF_OK;

@@ -50,6 +50,20 @@ __device__ __forceinline__ uint64_t make_desc_sw128(uint32_t saddr) {
     return d;
 }
 
+// An MN-major operand in the 128-byte swizzle: atoms of 64 consecutive MN elements
+// (128 B) x 8 K rows, 1024 B, swizzled as TMA writes them; LBO = the stride between
+// atoms along MN, SBO = the stride between atoms along K, layout type 2 (SWIZZLE_128B).
+// Atom bases must be 1024-byte aligned; a K = 16 step advances the start by 2 atoms.
+__device__ __forceinline__ uint64_t make_desc_sw128_mn(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
 // Instruction descriptor for kind::f16: D = f32 (bits 4-5 = 1), A = B = f16
 // (bits 7-9 = 0, 10-12 = 0), both K-major (bits 15, 16 = 0), N >> 3 in bits
 // 17-22, M >> 4 in bits 24-28.
@@ -61,6 +75,11 @@ __host__ __device__ constexpr uint32_t idesc_f16(uint32_t M, uint32_t N) {
 // SBO = the stride between 8-element N groups of the 128-byte core matrices
 // (8 K rows of 16 bytes, each holding 8 consecutive N elements).
 __host__ __device__ constexpr uint32_t idesc_f16_bmn(uint32_t M, uint32_t N) { return idesc_f16(M, N) | (1u << 16); }
+// Both operands MN-major (bits 15 and 16): D[M x N] = A^T-stored times B^T-stored, i.e. a
+// contraction over the rows of two row-major tiles.
+__host__ __device__ constexpr uint32_t idesc_f16_mn(uint32_t M, uint32_t N) {
+    return idesc_f16(M, N) | (1u << 15) | (1u << 16);
+}
 
 // ---- TMEM allocation (one full warp executes these) ----
 __device__ __forceinline__ void tmem_alloc(uint32_t* smem_dst, uint32_t ncols) {
@@ -238,6 +257,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 }
 
 // ---- registers -> TMEM: 32 lanes x 32 bit, 16 consecutive columns ----
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* r) {
     asm volatile(
         "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "

@@ -41,7 +41,7 @@ class FieldArgs(ctypes.Structure):
                 ("d_hess", c_vp), ("d_xc", c_vp), ("ld_dxc", c_i32), ("normal_col", c_i32), ("d_h0c", c_vp),
                 ("d_table", c_vp), ("d_pre0", c_vp), ("x0ext", c_vp), ("d_enc", c_vp), ("d_whead", c_vp),
                 ("d_bhead", c_vp),
-                ("err", c_vp)]
+                ("err", c_vp), ("d_w0", c_vp)]
 
 
 class RenderArgs(ctypes.Structure):
@@ -316,7 +316,10 @@ class FusedField:
                   d_pre_last=e(Ns, 8, dt=f16), dzs=[e(Ns, Hc, dt=f16) for _ in range(2)],
                   dzs_lo=[e(Ns, Hc, dt=f16) for _ in range(2)] if self.split else None,
                   dzfeat=e(Ns, 256, dt=f16), dzfeat_lo=e(Ns, 256, dt=f16) if self.split else None,
-                  dxc_tail=e(Ns, 64), d_h0c=e(Ns, 256), d_pre0=e(rows0, 256, dt=f16),
+                  dxc_tail=e(Ns, 64), d_h0c=e(Ns, 256),
+                  # K0 <= 64: the backward kernel accumulates dW0 itself; otherwise d_pre0 -> GEMM
+                  d_pre0=None if self.K0 <= 64 else e(rows0, 256, dt=f16),
+                  d_w0=e(256, self.K0 + 16) if self.K0 <= 64 else None,
                   x0ext=e(rows0, 2 * self.K0 + 16, dt=f16), d_enc=e(rows0, self.K0),
                   d_whead=torch.zeros(256, device=device),
                   d_bhead=torch.zeros(1, device=device), d_bl=torch.zeros(3, device=device),
@@ -529,11 +532,17 @@ class FusedField:
         fa.d_h0c = _p(ws['d_h0c'])
         fa.d_table, fa.d_pre0, fa.d_enc = _p(d_table), _p(ws['d_pre0']), _p(ws['d_enc'])
         fa.d_whead, fa.d_bhead = _p(ws['d_whead']), _p(ws['d_bhead'])
+        if ws['d_w0'] is not None:
+            ws['d_w0'].zero_()
+        fa.d_w0 = _p(ws['d_w0'])
         _lib.call("gbsdf_field_mlp_bwd", ctypes.byref(fa), stream)    # = gbsdf_field_bwd in two calls
         _lib.call("gbsdf_field_scatter", ctypes.byref(fa), stream)
-        gw0x = torch.empty(256, 2 * self.K0 + 16, **dev32)
-        _wgrad(ws['d_pre0'], ws['x0ext'], 256, 2 * self.K0 + 16, gw0x)
-        grads['w0ext'] = gw0x
+        if ws['d_w0'] is not None:
+            grads['w0ext'] = ws['d_w0']                               # [256, K0 + 16], lo folded in
+        else:
+            gw0x = torch.empty(256, 2 * self.K0 + 16, **dev32)
+            _wgrad(ws['d_pre0'], ws['x0ext'], 256, 2 * self.K0 + 16, gw0x)
+            grads['w0ext'] = gw0x
         grads['table'] = d_table
         if self.bg:
             grads['bg'] = self._background_backward(R, app_idx, stream)
@@ -645,8 +654,10 @@ class FusedField:
         l0, l1 = sdf.mlp.linears[0], sdf.mlp.linears[1]
         lins = m.neural_rgb.mlp.linears
         dW0 = torch.zeros_like(l0.weight_v)
-        gx = g['w0ext']      # columns: features hi | x,y,z hi, 1, x,y,z lo, 0 | features lo
-        dW0[:, 3:3 + A * F] = gx[:, :A * F] + gx[:, K0 + 16:K0 + 16 + A * F]
+        gx = g['w0ext']      # columns: features hi | x,y,z hi, 1, x,y,z lo, 0 [| features lo]
+        dW0[:, 3:3 + A * F] = gx[:, :A * F]
+        if gx.shape[1] > K0 + 16:                      # the GEMM path keeps the lo columns apart
+            dW0[:, 3:3 + A * F] += gx[:, K0 + 16:K0 + 16 + A * F]
         dW0[:, :3] = gx[:, K0:K0 + 3] + gx[:, K0 + 4:K0 + 7]
         db0 = gx[:, K0 + 3]
         # colour layer 0: undo the column reordering
