@@ -31,9 +31,12 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 // Walk (row group, K chunk) in nested loops so no integer division is needed.
+// dst_k > K: the tile's rows are dst_k columns wide and only the first K are written
 __device__ __forceinline__ void stage_rows_kmajor(uint8_t* tile, const __half* src, int64_t row0, int64_t rows,
-                                                  int ld, int K, int tid, int nthreads, int nrows = TILE_M) {
+                                                  int ld, int K, int tid, int nthreads, int nrows = TILE_M,
+                                                  int dst_k = 0) {
     const int KC = K >> 3;
+    const size_t group_bytes = (size_t)(dst_k > K ? dst_k : K) * 16;    // one 8-row group
     const int per_group = 8 * KC;                 // chunks of one 8-row group
     // each thread starts at chunk tid and strides by nthreads; decompose once, then advance
     int c = tid;
@@ -44,7 +47,7 @@ __device__ __forceinline__ void stage_rows_kmajor(uint8_t* tile, const __half* s
         const int r_lo = rem & 7;
         const int kc = rem >> 3;
         const int r = rg * 8 + r_lo;
-        uint8_t* dst = tile + (size_t)c * 16;
+        uint8_t* dst = tile + rg * group_bytes + (size_t)rem * 16;
         const int64_t gr = row0 + r;
         if (gr < rows) {
             cp_async16(dst, src + gr * (int64_t)ld + kc * 8);

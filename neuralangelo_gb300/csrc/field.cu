@@ -559,6 +559,11 @@ constexpr int DH0_LD = HID + 4;                  // d_h0c rows in shared memory,
 //     buffers (128-byte swizzle atoms of 64 hidden units x 8 rows), B = the tile's x0ext rows.
 //   * The feature tile is double-buffered: the next tile's load may not overwrite what
 //     dW0 reads.  dW0 goes before MMA2, so MMA2's completion also frees the staging rows.
+//   * The lo feature rows are K0 + 16 columns wide, the last 16 zero, so that the lo dW0
+//     MMAs have the hi MMAs' shape (MMAs into one accumulator are ordered when their
+//     shapes agree).
+//   * MMA1 of the next tile is issued as soon as MMA2 has completed (D1 is free then),
+//     under the d_enc epilogue.
 //   * Each CTA adds its dW0 into d_w0 with atomics at the end.
 template <int F, bool DW>
 __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
@@ -573,10 +578,11 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     uint8_t* stage_s = smem;                                    // [16 warps][4 KB] TMA store staging
     uint8_t* w_s = stage_s + (BWD_THREADS / 32) * BWD_STAGE_BYTES;   // [256 x KB]  w0b: B of MMA1
     uint8_t* a_s0 = w_s + HID * KB * 2;                         // [128 x KB]  features hi | tail
-    uint8_t* a3_s0 = a_s0 + TILE_M * KB * 2;                    // [128 x K0]  features lo
-    uint8_t* a_s1 = DW ? a3_s0 + TILE_M * K0 * 2 : a_s0;        // the second buffer (DW)
+    const int KL = DW ? KB : K0;                                // lo row width (DW: zero-padded)
+    uint8_t* a3_s0 = a_s0 + TILE_M * KB * 2;                    // [128 x KL]  features lo
+    uint8_t* a_s1 = DW ? a3_s0 + TILE_M * KL * 2 : a_s0;        // the second buffer (DW)
     uint8_t* a3_s1 = DW ? a_s1 + TILE_M * KB * 2 : a3_s0;
-    float* wh_s = reinterpret_cast<float*>(a3_s1 + TILE_M * K0 * 2);   // [256] head weights
+    float* wh_s = reinterpret_cast<float*>(a3_s1 + TILE_M * KL * 2);   // [256] head weights
     float* dwh_s = wh_s + HID;                                  // [256] d_whead accumulator
     float* df_s = dwh_s + HID;                                  // [2][7][18] d f per evaluation, double-buffered
     float* dh0_s = df_s + 2 * EVALS * SPT + 4;                  // [18][DH0_LD] d_h0c of the tile's samples
@@ -588,6 +594,14 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     for (int i = tid; i < HID; i += BWD_THREADS) {
         wh_s[i] = p.whead[i];
         dwh_s[i] = 0.0f;
+    }
+    if (DW) {
+        // the zero columns [K0, K0 + 16) of both lo tiles: 16 row groups x 256 bytes each
+        for (int i = tid; i < 2 * (TILE_M / 8) * 16; i += BWD_THREADS) {
+            uint8_t* base = (i >> 8) ? a3_s1 : a3_s0;
+            *reinterpret_cast<uint4*>(base + ((i >> 4) & 15) * (KL * 16) + K0 * 16 + (i & 15) * 16) =
+                make_uint4(0, 0, 0, 0);
+        }
     }
     if (tid == 0) {
         umma::mbar_init(mbar, 1);
@@ -698,7 +712,8 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     auto stage_a = [&](int64_t tt, int buf) {      // one cp.async group
         const __half* xb = (const __half*)p.x0ext;
         stage_rows_kmajor(a_buf(buf), xb, tt * (SPT * EVALS), xrows, KX, KB, tid, BWD_THREADS);
-        stage_rows_kmajor(a3_buf(buf), xb + K0 + 16, tt * (SPT * EVALS), xrows, KX, K0, tid, BWD_THREADS);
+        stage_rows_kmajor(a3_buf(buf), xb + K0 + 16, tt * (SPT * EVALS), xrows, KX, K0, tid, BWD_THREADS, TILE_M,
+                          KL);
         cp_async_commit();
     };
     auto stage_dh0 = [&](int64_t tt) {             // one cp.async group
@@ -714,7 +729,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     auto issue1 = [&](int buf) {
         if (tid == 0) {
             umma::fence_after_sync();
-            issue_tile_mma_strided(tmem, a3_addr(buf), K0, w_addr, KB, K0, idesc1);   // residuals first
+            issue_tile_mma_strided(tmem, a3_addr(buf), KL, w_addr, KB, K0, idesc1);   // residuals first
             issue_tile_mma(tmem, a_addr(buf), w_addr, KB, idesc1, true);
             umma::mma_commit(mbar);
         }
@@ -835,12 +850,12 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         if (tid == 0) {
             umma::fence_after_sync();
             if constexpr (DW) {
-                // dW0[h] += d_pre^T [x hi | tail], then += d_pre^T x lo on the first K0 columns.
+                // dW0[h] += d_pre^T [x hi | tail], then += d_pre^T [x lo | 0].
                 // A (hidden half h = staging parts 2h, 2h + 1): atoms of 64 units x 8 rows, next
                 // 64 units 16 KB on, next 8 rows 1 KB on; B (the tile's rows, MN-major): next 8
-                // rows KB*16 (K0*16) bytes on, next 8 features 128 bytes on.
+                // rows KB*16 bytes on, next 8 features 128 bytes on.
                 const uint32_t st = umma::smem_u32(stage_s);
-                const uint32_t id_b = umma::idesc_f16_mn(TILE_M, KB), id_l = umma::idesc_f16_mn(TILE_M, K0);
+                const uint32_t id_b = umma::idesc_f16_mn(TILE_M, KB);
                 for (int h = 0; h < 2; ++h) {
                     const uint32_t d = t_dw + (uint32_t)(h * KB);
                     for (int ks = 0; ks < TILE_M / 16; ++ks) {
@@ -850,8 +865,8 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
                     }
                     for (int ks = 0; ks < TILE_M / 16; ++ks) {
                         const uint64_t ad = umma::make_desc_sw128_mn(st + h * 32768u + ks * 2048u, 16384u, 1024u);
-                        const uint64_t bd = umma::make_desc(a3_addr(cb) + ks * 2u * K0 * 16u, K0 * 16u, 128u);
-                        umma::mma_f16(d, ad, bd, id_l, 1u);
+                        const uint64_t bd = umma::make_desc(a3_addr(cb) + ks * 2u * KB * 16u, KB * 16u, 128u);
+                        umma::mma_f16(d, ad, bd, id_b, 1u);
                     }
                 }
             }
@@ -871,6 +886,10 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
             stage_dh0(tn);                           // every warp has read this tile's d_h0c rows
             prologue_ray(tn, pin);
         }
+        if (DW && tn < ntiles) {
+            cp_async_wait_group<1>();                // tile tn's A tile (its d_h0c group may still be in flight)
+            umma::fence_proxy_async_smem();
+        }
         ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
         phase ^= 1u;
         if (!ok) {
@@ -878,6 +897,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
             break;
         }
         umma::fence_after_sync();
+        if (DW && tn < ntiles) issue1(nb);           // D1 is free: MMA2 has read d_pre
         // (4) d_enc rows to global for k_field_scatter: 16-column chunks dealt in turn
         // to the four warps of a lane quadrant (K0 <= 128: at most two per warp, one
         // 2 KB half of the staging buffer each; 64-byte swizzle: unit j of row r at j ^ ((r >> 1) & 3))
@@ -901,11 +921,13 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         umma::fence_before_sync();
         if (tn < ntiles) {
             prologue_finish(tn, pin, (it + 1) & 1);  // the other df buffer
-            cp_async_wait_group<1>();                // tile tn's A tile (its d_h0c group may still be in flight)
-            umma::fence_proxy_async_smem();
+            if (!DW) {
+                cp_async_wait_group<1>();            // tile tn's A tile (its d_h0c group may still be in flight)
+                umma::fence_proxy_async_smem();
+            }
         }
         __syncthreads();   // the TMEM accumulator of tile t read; tile tn's A tile and d f in place
-        if (tn < ntiles) issue1(nb);
+        if (!DW && tn < ntiles) issue1(nb);
     }
     cp_async_wait_all();
     if (lane == 0) umma::bulk_wait0();               // this warp's TMA stores have completed
@@ -1076,7 +1098,7 @@ static size_t fwd_smem(int K0) {
 static size_t bwd_smem(int K0, bool dw) {
     const size_t KB = (size_t)K0 + 16;
     const size_t need = (size_t)(BWD_THREADS / 32) * BWD_STAGE_BYTES + (size_t)HID * KB * 2 +
-                        (size_t)TILE_M * (KB + K0) * 2 * (dw ? 2 : 1) +
+                        (size_t)TILE_M * (KB + (dw ? KB : K0)) * 2 * (dw ? 2 : 1) +
                         (2 * HID + 2 * EVALS * SPT + 4 + SPT * DH0_LD) * 4 + 16;
     return need > BWD_SMEM_FLOOR ? need : BWD_SMEM_FLOOR;
 }
