@@ -28,6 +28,19 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 
 inline bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
 
+// Lets kernel k take up to the device's opt-in maximum of dynamic shared memory per
+// block.  Always the same ceiling, never the current launch's size: a per-launch value
+// would leave the attribute at the last launch's size, below what an earlier launch of
+// the same kernel recorded in a CUDA graph asks for when that node is launched on its
+// own (as a profiler does with graph nodes).
+template <typename Kernel>
+inline void allow_max_smem(Kernel k) {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+}
+
 // ---------------------------------------------------------------------------
 // hash-grid level arithmetic, shared by every kernel that evaluates the field.
 // Follows tiny-cuda-nn's HashGrid (the encoder behind modules.py:42-50):

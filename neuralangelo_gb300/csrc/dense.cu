@@ -346,7 +346,7 @@ static int launch_dense(DenseParams p, cudaStream_t s) {
         set_error("dense layer K=%d N_TILE=%d needs %zu B of shared memory", p.K, N_TILE, smem);
         return GBSDF_ERR_UNSUPPORTED;
     }
-    cudaFuncSetAttribute(k_dense<N_TILE, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_max_smem(k_dense<N_TILE, EPI>);
     const int64_t ntiles = (p.M + TILE_M - 1) / TILE_M;
     int64_t groups = sm_count() / p.n_split;
     if (groups < 1) groups = 1;

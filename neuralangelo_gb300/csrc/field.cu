@@ -1131,7 +1131,7 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
         }
         int64_t grid = num_sms() * FWD_CTAS_PER_SM;
         if (grid > ntiles) grid = ntiles;
-        cudaFuncSetAttribute(k_field_fwd<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        allow_max_smem(k_field_fwd<F>);
         k_field_fwd<F><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p);
         if (int st = launch_status("field forward")) return st;
     }
@@ -1169,10 +1169,10 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
         int64_t grid = num_sms();
         if (grid > ntiles) grid = ntiles;
         if (dw) {
-            cudaFuncSetAttribute(k_field_bwd<F, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            allow_max_smem(k_field_bwd<F, true>);
             k_field_bwd<F, true><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30);
         } else {
-            cudaFuncSetAttribute(k_field_bwd<F, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            allow_max_smem(k_field_bwd<F, false>);
             k_field_bwd<F, false><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30);
         }
         if (int st = launch_status("field backward")) return st;
@@ -1299,15 +1299,15 @@ extern "C" int gbsdf_sdf_points(const gbsdf_field_args* params, int64_t M, const
     cudaStream_t s = as_stream(stream);
     switch (p.grid.n_features) {
         case 2:
-            cudaFuncSetAttribute(k_sdf_points<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            allow_max_smem(k_sdf_points<2>);
             k_sdf_points<2><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p, q);
             break;
         case 4:
-            cudaFuncSetAttribute(k_sdf_points<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            allow_max_smem(k_sdf_points<4>);
             k_sdf_points<4><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p, q);
             break;
         default:
-            cudaFuncSetAttribute(k_sdf_points<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            allow_max_smem(k_sdf_points<8>);
             k_sdf_points<8><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p, q);
             break;
     }

@@ -239,7 +239,7 @@ extern "C" int gbsdf_sampler_round(const gbsdf_sampler_args* args, void* stream)
     if (p.R == 0) return GBSDF_OK;
     const int cap = p.n_list + p.n_merge;
     const size_t smem = (size_t)SAMPLER_WARPS * 5 * (cap > 0 ? cap : 1) * sizeof(float);
-    cudaFuncSetAttribute(k_sampler_round, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_max_smem(k_sampler_round);
     const int64_t blocks = (p.R + SAMPLER_WARPS - 1) / SAMPLER_WARPS;
     k_sampler_round<<<(unsigned)blocks, SAMPLER_WARPS * 32, smem, as_stream(stream)>>>(p);
     return launch_status("sampler_round");
