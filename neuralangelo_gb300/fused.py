@@ -163,9 +163,12 @@ def sdf_weight_args(sdf, pk, A, K0, err=None):
 class FusedField:
     """Fused FP16 forward+backward over a FieldModel's FP32 master parameters."""
 
-    def __init__(self, model, loss_scale=2.0 ** 15, split_colour_grads=False):
+    def __init__(self, model, loss_scale=2.0 ** 15, split_colour_grads=False, fused_w0_grad=True):
         check_struct_sizes()
         self.model = model
+        # the layer-0 weight gradient: accumulated by the backward kernel itself (K0 <= 64), or
+        # (False, or K0 > 64) from the kernel's fp16 d_pre0 rows by a separate GEMM
+        self.fused_w0_grad = bool(fused_w0_grad)
         # carry the colour MLP's input gradients as fp16 hi+lo pairs (costs ~9% of the step and
         # leaves the weight-gradient error unchanged: that comes from fp16 storage of the
         # forward activations, whose rounding moves ReLU gates near zero)
@@ -297,6 +300,9 @@ class FusedField:
         pk['app_bg'] = ae.weight.detach().float().contiguous() if ae is not None else None
 
     # ------------------------------------------------------------------ workspace
+    def _in_kernel_w0_grad(self):
+        return self.fused_w0_grad and self.K0 <= 64
+
     def _workspace(self, R, S, Ns, device):
         key = (R, S, Ns, self.K0, self.bg)
         if self.ws is not None and self.ws['key'] == key:
@@ -318,8 +324,8 @@ class FusedField:
                   dzfeat=e(Ns, 256, dt=f16), dzfeat_lo=e(Ns, 256, dt=f16) if self.split else None,
                   dxc_tail=e(Ns, 64), d_h0c=e(Ns, 256),
                   # K0 <= 64: the backward kernel accumulates dW0 itself; otherwise d_pre0 -> GEMM
-                  d_pre0=None if self.K0 <= 64 else e(rows0, 256, dt=f16),
-                  d_w0=e(256, self.K0 + 16) if self.K0 <= 64 else None,
+                  d_pre0=None if self._in_kernel_w0_grad() else e(rows0, 256, dt=f16),
+                  d_w0=e(256, self.K0 + 16) if self._in_kernel_w0_grad() else None,
                   x0ext=e(rows0, 2 * self.K0 + 16, dt=f16), d_enc=e(rows0, self.K0),
                   d_whead=torch.zeros(256, device=device),
                   d_bhead=torch.zeros(1, device=device), d_bl=torch.zeros(3, device=device),

@@ -77,3 +77,27 @@ def test_sampler_args_layout_and_validation_without_gpu(lib):
     a.fine_d = 16
     assert lib.gbsdf_sampler_round(ctypes.byref(a), None) == 1
     assert b"SDF values" in lib.gbsdf_last_error()
+
+
+def test_field_backward_weight_gradient_arguments_without_gpu(lib):
+    """The backward needs d_pre0, or d_w0 with K0 <= 64; both rejected before any launch."""
+    from neuralangelo_gb300.fused import FieldArgs, check_struct_sizes
+    check_struct_sizes()
+    a = FieldArgs()
+    assert lib.gbsdf_grid_init(ctypes.byref(a.grid), 16, 8, 14, 32, ctypes.c_float(1.3195079)) == 0
+    a.Ns, a.S = 100, 10
+    # non-NULL, 16-byte aligned placeholders: validation runs before anything is dereferenced
+    for f in ("center", "ray_unit", "dists", "table", "w0e", "w0b", "w0x", "b0", "whead", "bhead", "grad",
+              "d_sdf", "d_grad", "d_hess", "d_xc", "d_h0c", "x0ext", "d_enc", "d_whead", "d_bhead"):
+        setattr(a, f, 256)
+    a.active, a.K0 = 16, 128
+    a.d_w0 = 256
+    assert lib.gbsdf_field_mlp_bwd(ctypes.byref(a), None) == 1
+    assert b"K0 <= 64" in lib.gbsdf_last_error()
+    a.active, a.K0 = 8, 64
+    a.d_w0 = None
+    assert lib.gbsdf_field_mlp_bwd(ctypes.byref(a), None) == 1
+    assert b"d_pre0" in lib.gbsdf_last_error()
+    a.d_pre0 = 8                                   # misaligned
+    assert lib.gbsdf_field_mlp_bwd(ctypes.byref(a), None) == 1
+    assert b"d_pre0" in lib.gbsdf_last_error()

@@ -362,3 +362,25 @@ def test_c2_accuracy_report_512_rays():
     assert e_sdf < 1e-4 and e_rgb < 1e-4
     assert e_tab < 1.25 * e_tab32
     assert e_tab0 < 1e-3
+
+
+def test_in_kernel_layer0_weight_gradient_matches_gemm_path():
+    """K0 <= 64: the backward kernel's own dW0 (TMEM accumulators, per-CTA atomics) against the
+    d_pre0 rows + GEMM path on the same step; every other gradient must agree as well."""
+    model = build(seed=5)
+    batch = make_rays(96, 64, seed=12, miss_frac=0.2, n_images=10, device=DEV)
+    grads = []
+    for fused in (True, False):
+        ff = FusedField(model, fused_w0_grad=fused)
+        model.zero_grad(set_to_none=True)
+        ff.step(batch)
+        torch.cuda.synchronize()
+        assert ff.check_device_errors() == 0
+        assert (ff.ws['d_w0'] is not None) == fused and (ff.ws['d_pre0'] is None) == fused
+        grads.append({k: v.clone() for k, v in params_io.model_grads(model).items() if v is not None})
+    a, b = grads
+    errs = {k: rel(a[k].cpu(), b[k].cpu()) for k in b}
+    print("\nin-kernel dW0 vs GEMM:", {k: f"{v:.1e}" for k, v in errs.items()})
+    # the same fp16 products summed in another order (FP32 both ways)
+    for k, e in errs.items():
+        assert e < 1e-5, (k, e)
