@@ -534,14 +534,15 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
 //        plus the features lo against the W0e prefix), exactly as the forward;
 //   the epilogue forms d_pre = (d f w_head + [centre] d_h0c) softplus'(pre) and the
 //        head-weight gradient, writes d_pre as an fp16 hi + lo pair into TMEM (the A
-//        operand of MMA2) and its hi half to global for the layer-0 weight gradient;
+//        operand of MMA2) and its hi half to shared memory: the A operand of the in-kernel
+//        layer-0 weight gradient (DW below), or staging for the global d_pre0 rows;
 //   MMA2 d_enc = d_pre W0e (A from TMEM, B = the W0e part of MMA1's w0b tile read
 //        MN-major) goes to global for k_field_scatter.
 // The +eps and -eps taps of a sample carry large, nearly cancelling d_pre, so a
 // single fp16 rounding of d_pre would dominate the table-gradient error: hence the pair.
-// TMEM (512 columns, one CTA per SM): [0, 256) MMA1's accumulator, reused for
-// MMA2's [128 x K0] result; [256, 384) d_pre hi, [384, 512) d_pre lo.
-// d_pre0 and d_enc leave through a 4 KB staging buffer per warp and TMA stores
+// TMEM without DW (512 columns, one CTA per SM): [0, 256) MMA1's accumulator, reused
+// for MMA2's [128 x K0] result; [256, 384) d_pre hi, [384, 512) d_pre lo.
+// d_pre0 (without DW) and d_enc leave through a 4 KB staging buffer per warp and TMA stores
 // (one thread per row would touch 32 cache lines per store instruction); a tile has
 // 126 rows, so the last lane quadrant stores a 30-row box.
 constexpr size_t BWD_SMEM_FLOOR = 120 * 1024;   // > half an SM's shared memory: one CTA per SM
