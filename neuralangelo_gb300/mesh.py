@@ -216,6 +216,40 @@ def export_mesh(mesh, path, sphere_radius=1.0, sphere_center=(0.0, 0.0, 0.0), de
     return out
 
 
+def largest_component(V, F, C=None):
+    """filter_largest_cc (mesh.py:151-158) on one block's mesh: (V, F, C) of the component
+    of largest area.  Components as trimesh's ``split(only_watertight=False)`` defines them:
+    faces are joined by the edges that exactly two faces share (its face adjacency), and
+    every component counts, whatever its size.  Of equal areas the component holding the
+    lowest face index wins.  The kept vertices stay in index order (as trimesh's submesh
+    takes them) and the faces are re-indexed from 0, in ascending face order.  Host code,
+    as the reference's is (numpy + scipy); C is per-vertex colours or None."""
+    from scipy.sparse import coo_matrix
+    from scipy.sparse.csgraph import connected_components
+    V = np.asarray(V)
+    F = np.asarray(F, np.int64).reshape(-1, 3)
+    if len(F) == 0 or len(V) == 0:
+        return V[:0], F[:0], (None if C is None else np.asarray(C)[:0])
+    nf = len(F)
+    e = np.sort(F[:, [0, 1, 1, 2, 2, 0]].reshape(-1, 2), axis=1)          # 3 edges per face
+    key = e[:, 0] * np.int64(len(V)) + e[:, 1]
+    order = np.argsort(key, kind="stable")
+    ks = key[order]
+    start = np.flatnonzero(np.r_[True, ks[1:] != ks[:-1]])
+    count = np.diff(np.r_[start, len(ks)])
+    pair = start[count == 2]                                               # edges of exactly two faces
+    fa, fb = order[pair] // 3, order[pair + 1] // 3
+    graph = coo_matrix((np.ones(len(fa), np.int8), (fa, fb)), shape=(nf, nf))
+    n_comp, labels = connected_components(graph, directed=False)
+    # scipy numbers components in order of their lowest node: label order = lowest face order
+    T = V[F].astype(np.float64)
+    area = 0.5 * np.linalg.norm(np.cross(T[:, 1] - T[:, 0], T[:, 2] - T[:, 0]), axis=1)
+    keep = int(np.argmax(np.bincount(labels, weights=area, minlength=n_comp)))
+    Fk = F[labels == keep]
+    used, inv = np.unique(Fk.reshape(-1), return_inverse=True)
+    return V[used], inv.reshape(-1, 3).astype(np.int64), (None if C is None else np.asarray(C)[used])
+
+
 def lattice_axes(bounds, intv, device):
     """LatticeGrid axes: torch.arange(min, max, intv) in float32 (mesh.py:74-76)."""
     return [torch.arange(lo, hi, intv).to(device) for lo, hi in bounds]
@@ -228,9 +262,8 @@ def extract_mesh(sdf_func, bounds, intv, block_res=64, texture_func=None, filter
     trimesh.Trimesh(V, F) applies (mesh.py:124-126: coordinates equal at 8 decimals),
     keeping every face as trimesh does there.  texture_func (points [n,3] numpy -> uint8
     colours [n,3], e.g. ``inference.extract_texture`` bound to a model) colours each
-    block's vertices, as marching_cubes does before its sphere filter (mesh.py:121-128)."""
-    if filter_lcc:
-        raise NotImplementedError("largest-component filtering is outside this path")
+    block's vertices, as marching_cubes does before its sphere filter (mesh.py:121-128).
+    filter_lcc=True keeps each block's largest connected component (mesh.py:130, ``largest_component``)."""
     axes = lattice_axes(bounds, intv, device)
     nblk = [int(np.ceil(len(a) / block_res)) for a in axes]
     mc = MarchingCubes(block_res + 1, device)
@@ -253,11 +286,17 @@ def extract_mesh(sdf_func, bounds, intv, block_res=64, texture_func=None, filter
                     continue
                 if merge_vertices:
                     V, F = finalize_mesh(V, F, weld=True, min_side=-1.0)
-                Vs.append(V.cpu().numpy())
-                Fs.append(F.cpu().numpy() + off)
-                if texture_func is not None:
-                    Cs.append(np.asarray(texture_func(Vs[-1]), np.uint8).reshape(-1, 3))
-                off += V.shape[0]
+                Vb, Fb = V.cpu().numpy(), F.cpu().numpy()
+                Cb = np.asarray(texture_func(Vb), np.uint8).reshape(-1, 3) if texture_func is not None else None
+                if filter_lcc:
+                    Vb, Fb, Cb = largest_component(Vb, Fb, Cb)
+                    if len(Vb) == 0:
+                        continue
+                Vs.append(Vb)
+                Fs.append(Fb + off)
+                if Cb is not None:
+                    Cs.append(Cb)
+                off += Vb.shape[0]
     if not Vs:
         return Mesh(np.zeros((0, 3)), np.zeros((0, 3), np.int64),
                     np.zeros((0, 3), np.uint8) if texture_func is not None else None)

@@ -65,10 +65,11 @@ def block_slices(n_points, block_res):
     return [(b * block_res, min(b * block_res + block_res + 1, n_points)) for b in range(nb)]
 
 
-def extract_mesh_blocks(sdf_volume_fn, bounds, intv, block_res, iso=0.0, merge_vertices=False):
+def extract_mesh_blocks(sdf_volume_fn, bounds, intv, block_res, iso=0.0, merge_vertices=False, filter_lcc=False):
     """sdf_volume_fn(xs, ys, zs) -> float32 [len(xs), len(ys), len(zs)] (already negated
     as extract_mesh.py:85 does).  Returns the concatenated (V, F) over blocks in order;
-    merge_vertices applies trimesh's per-block merge (mesh.py:124-126, see mesh_out.py)."""
+    merge_vertices applies trimesh's per-block merge (mesh.py:124-126, see mesh_out.py),
+    filter_lcc its per-block largest component (mesh.py:130,151-158)."""
     from oracle import mesh_out
     ax = lattice_axes(bounds, intv)
     sx, sy, sz = (block_slices(len(a), block_res) for a in ax)
@@ -83,6 +84,10 @@ def extract_mesh_blocks(sdf_volume_fn, bounds, intv, block_res, iso=0.0, merge_v
                     continue
                 if merge_vertices:
                     V, F = mesh_out.merge_vertices(V, F)
+                if filter_lcc:
+                    V, F = mesh_out.largest_component(V, F)
+                    if V.shape[0] == 0:
+                        continue
                 Vs.append(V)
                 Fs.append(F + off)
                 off += V.shape[0]

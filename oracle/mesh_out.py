@@ -18,6 +18,13 @@ its documented behaviour and parity with trimesh itself is unpinned:
   and 2A / |b| (taken as 0 when that edge is not longer than the tolerance)
   exceed the tolerance (trimesh's merge tolerance, 1e-8).  Every vertex is kept,
   referenced or not.
+* projects/neuralangelo/utils/mesh.py:151-158 (``filter_largest_cc``, per block after
+  the sphere filter, :130): ``mesh.split(only_watertight=False)`` then the component
+  of largest area.  trimesh joins two faces when they share an edge that exactly two
+  faces share (its face adjacency: sorted edge rows grouped, groups of two kept),
+  keeps components of any size, and lists them by label (scipy numbers components in
+  order of their lowest face); ``argmax`` takes the first of equal areas.  A
+  component becomes a submesh: its vertices in index order, re-indexed from 0.
 """
 import numpy as np
 
@@ -88,3 +95,42 @@ def finalize(V, F, weld=False, digits=MERGE_DIGITS, scale=1.0, offset=(0.0, 0.0,
     V = transform(V, scale, offset)
     keep = nondegenerate(V, F, height)
     return V, F[keep]
+
+
+def largest_component(V, F):
+    """(V', F') of the largest-area component of (V, F), by a pure-Python union-find over
+    faces joined through edges that exactly two faces share; faces in ascending order."""
+    V = np.asarray(V, np.float64)
+    F = [tuple(int(i) for i in f) for f in np.asarray(F, np.int64).reshape(-1, 3)]
+    if not F or len(V) == 0:
+        return V[:0], np.zeros((0, 3), np.int64)
+    owners = {}
+    for fi, (a, b, c) in enumerate(F):
+        for u, v in ((a, b), (b, c), (c, a)):
+            owners.setdefault((min(u, v), max(u, v)), []).append(fi)
+    parent = list(range(len(F)))
+
+    def find(x):
+        while parent[x] != x:
+            parent[x] = parent[parent[x]]
+            x = parent[x]
+        return x
+
+    for fl in owners.values():
+        if len(fl) == 2:
+            ra, rb = find(fl[0]), find(fl[1])
+            if ra != rb:
+                parent[max(ra, rb)] = min(ra, rb)        # the root is the component's lowest face
+    area = {}
+    for fi, (a, b, c) in enumerate(F):
+        e1, e2 = V[b] - V[a], V[c] - V[a]
+        cx = e1[1] * e2[2] - e1[2] * e2[1]
+        cy = e1[2] * e2[0] - e1[0] * e2[2]
+        cz = e1[0] * e2[1] - e1[1] * e2[0]
+        r = find(fi)
+        area[r] = area.get(r, 0.0) + 0.5 * float(np.sqrt(cx * cx + cy * cy + cz * cz))
+    best = max(sorted(area), key=lambda r: area[r])    # sorted roots = lowest-face order; first max
+    keep = [f for fi, f in enumerate(F) if find(fi) == best]
+    used = sorted({i for f in keep for i in f})
+    remap = {v: k for k, v in enumerate(used)}
+    return V[used], np.array([[remap[i] for i in f] for f in keep], np.int64).reshape(-1, 3)
