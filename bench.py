@@ -9,9 +9,9 @@ Prints ONE JSON line (rank 0).  ``value`` is the device-resident throughput of
 the selected mode (default: the fused path when built, else the plain FP32
 drop-in), ``e2e`` the same step through the public API with the batch copied
 from pinned host memory and the loss read back every step.  Under torchrun
-every rank runs an independent replica (the path has no exchange step on one
-node in this build: replicas only) and ``value`` sums the ranks' samples over
-the slowest rank's time.
+every rank runs an independent replica (rays are independent, so the path has
+no exchange step: replicas only) and ``value`` sums the ranks' samples over the
+slowest rank's time.
 """
 import argparse
 import json
