@@ -201,6 +201,12 @@ typedef struct gbsdf_field_args {
                                 [0, K0) the features (hi + lo), [K0, K0 + 16) the x0ext tail.
                                 Non-NULL (K0 <= 64): the backward accumulates it itself and
                                 leaves d_pre0 unused (may be NULL); NULL: it writes d_pre0 */
+    void* h0c_lo;            /* optional fp16 [Ns, ld_h0c]: h0c's low half, so h0c + h0c_lo carries the
+                                FP32 activation to ~2^-22 (NULL: not written) */
+    void* xc_lo;             /* optional fp16 [Ns, ldxc]: the low half of the colour-input tail columns
+                                (>= 256) the forward writes; 0 in the constant-1 column (NULL: not written) */
+    void* d_pre0_lo;         /* optional fp16 [126 T, 256]: d_pre0's low half (backward without d_w0; the
+                                layer-0 weight gradient is d_pre0^T x0ext + d_pre0_lo^T [x hi | tail]) */
 } gbsdf_field_args;
 
 size_t gbsdf_field_args_size(void);
@@ -330,12 +336,15 @@ int gbsdf_mc_block(const float* vol, int nx, int ny, int nz, double iso, const d
  * their 10-level Fourier code (nerf_util.py:134-147), a constant 1 at column 84, zeros up
  * to x_cols -- and the colour MLP's input tail T [R NB, ldt] -- SH(d) (16), the appearance
  * code app_table[app_idx[r]] (app_dim, may be 0), a constant 1, zeros up to t_cols.
- * gbsdf_bg_density: sigma [M] = softplus(H [M, ldh] . w [H] + b[0]) (beta 1, threshold 20). */
+ * X_lo / T_lo (optional, same row strides): the fp16 low halves, so X + X_lo and T + T_lo carry
+ * the FP32 values to ~2^-22 (0 in the constant-1 and zero columns).
+ * gbsdf_bg_density: sigma [M] = softplus((H + H_lo) [M, ldh] . w [H] + b[0]) (beta 1, threshold
+ * 20); H_lo, the optional low half of H, has H's row stride. */
 int gbsdf_bg_encode(int64_t R, int32_t NB, const float* center, const float* ray_unit, const float* dists,
-                    const float* app_table, const int32_t* app_idx, int32_t app_dim, void* X, int32_t ldx,
-                    int32_t x_cols, void* T, int32_t ldt, int32_t t_cols, void* stream);
-int gbsdf_bg_density(int64_t M, const void* H, int32_t ldh, int32_t Hdim, const float* w, const float* b,
-                     float* sigma, void* stream);
+                    const float* app_table, const int32_t* app_idx, int32_t app_dim, void* X, void* X_lo,
+                    int32_t ldx, int32_t x_cols, void* T, void* T_lo, int32_t ldt, int32_t t_cols, void* stream);
+int gbsdf_bg_density(int64_t M, const void* H, const void* H_lo, int32_t ldh, int32_t Hdim, const float* w,
+                     const float* b, float* sigma, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Mesh output stage (scripts/extract_mesh.py:96-97 after utils/mesh.py:121-129 and

@@ -4,7 +4,8 @@
 //   of the background samples of every ray (points c + d t, camera.py:314-320, at the
 //   distances of Model.sample_dists_background, model.py:269-273): [x/|x|, 1/|x|] and
 //   its Fourier code (nerf_util.py:134-147: sin and cos of 2^k pi q, channel-major,
-//   sin block before cos block), as fp16 rows of the first MLP layer's input; and the
+//   sin block before cos block), as fp16 rows (optionally hi + lo pairs) of the first
+//   MLP layer's input; and the
 //   colour MLP's input tail (modules.py:277-281): SH(d) of degree 3, the per-image
 //   appearance code, then a constant-1 column (the bias column of the weight-gradient
 //   GEMM).
@@ -46,29 +47,37 @@ __device__ __forceinline__ void sh16(float dx, float dy, float dz, float* o) {
 // One thread per background sample s = r * NB + j.
 __global__ void k_bg_encode(int64_t R, int NB, const float* __restrict__ center, const float* __restrict__ ray_unit,
                             const float* __restrict__ dists, const float* __restrict__ app_table,
-                            const int32_t* __restrict__ app_idx, int app_dim, __half* __restrict__ X, int ldx,
-                            int x_cols, __half* __restrict__ T, int ldt, int t_cols) {
+                            const int32_t* __restrict__ app_idx, int app_dim, __half* __restrict__ X,
+                            __half* __restrict__ X_lo, int ldx, int x_cols, __half* __restrict__ T,
+                            __half* __restrict__ T_lo, int ldt, int t_cols) {
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= R * NB) return;
     const int64_t r = s / NB;
-    const float t = dists[s];
-    float p[3];
+    // The point, its normalisation and the phases are formed in double precision: at the
+    // highest frequency (2^9 pi) an FP32 rounding of q alone moves the phase by ~2e-4,
+    // which the first layers' weight gradients amplify past 1e-3.  Each phase is reduced
+    // to [-pi, pi] in double and only then evaluated in FP32 (|error| ~1e-7).
+    const double t = dists[s];
+    double p[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) p[i] = __fadd_rn(center[3 * r + i], __fmul_rn(ray_unit[3 * r + i], t));
-    const float nrm = sqrtf(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
-    float q[4] = {p[0] / nrm, p[1] / nrm, p[2] / nrm, 1.0f / nrm};
+    for (int i = 0; i < 3; ++i) p[i] = (double)center[3 * r + i] + (double)ray_unit[3 * r + i] * t;
+    const double nrm = sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+    const double q[4] = {p[0] / nrm, p[1] / nrm, p[2] / nrm, 1.0 / nrm};
     // row: q (4) | per channel c: sin(q_c f_k) k < 10, cos(q_c f_k) k < 10 | 1 | zeros
     float buf[96];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) buf[c] = q[c];
+    for (int c = 0; c < 4; ++c) buf[c] = (float)q[c];
+    constexpr double kTwoPi = 6.283185307179586476925;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
+        // 2^k pi as the reference builds it in float32 (2^k times float32(pi), exact)
+        const double base = q[c] * (double)3.14159265358979323846f;
 #pragma unroll
         for (int k = 0; k < BG_LEVELS; ++k) {
-            // 2^k pi as the reference builds it in float32 (2^k times float32(pi), exact)
-            const float f = ldexpf(3.14159265358979323846f, k);
+            const double ph = ldexp(base, k);
+            const float red = (float)(ph - kTwoPi * rint(ph * (1.0 / kTwoPi)));
             float sv, cv;
-            sincosf(q[c] * f, &sv, &cv);
+            sincosf(red, &sv, &cv);
             buf[4 + 20 * c + k] = sv;
             buf[4 + 20 * c + BG_LEVELS + k] = cv;
         }
@@ -82,10 +91,18 @@ __global__ void k_bg_encode(int64_t R, int NB, const float* __restrict__ center,
         if (8 * g < x_cols) store_half8(xr + 8 * g, buf + 8 * g);
     const float zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int c0 = 96; c0 < x_cols; c0 += 8) store_half8(xr + c0, zero8);
+    if (X_lo) {
+        __half* xl = X_lo + s * (int64_t)ldx;
+#pragma unroll
+        for (int g = 0; g < 12; ++g)
+            if (8 * g < x_cols) store_half8_lo(xl + 8 * g, buf + 8 * g);
+        for (int c0 = 96; c0 < x_cols; c0 += 8) store_half8(xl + c0, zero8);
+    }
     // colour-input tail: SH(d) 16 | app | 1 | zeros
     float o[16];
     sh16(ray_unit[3 * r], ray_unit[3 * r + 1], ray_unit[3 * r + 2], o);
     __half* tr = T + s * (int64_t)ldt;
+    __half* tl = T_lo ? T_lo + s * (int64_t)ldt : nullptr;
     const float* a = (app_table && app_dim > 0) ? app_table + (int64_t)app_idx[r] * app_dim : nullptr;
     for (int c0 = 0; c0 < t_cols; c0 += 8) {
         float v[8];
@@ -105,11 +122,13 @@ __global__ void k_bg_encode(int64_t R, int NB, const float* __restrict__ center,
             v[i] = x;
         }
         store_half8(tr + c0, v);
+        if (tl) store_half8_lo(tl + c0, v);
     }
 }
 
 // sigma = softplus(h . w + b), one warp per row; lane j owns columns [8j, 8j + 8) of H <= 256
-__global__ void __launch_bounds__(256) k_bg_density(int64_t M, const __half* __restrict__ Hm, int ldh, int H,
+__global__ void __launch_bounds__(256) k_bg_density(int64_t M, const __half* __restrict__ Hm,
+                                                    const __half* __restrict__ Hm_lo, int ldh, int H,
                                                     const float* __restrict__ w, const float* __restrict__ bias,
                                                     float* __restrict__ sigma) {
     const int lane = threadIdx.x & 31;
@@ -124,6 +143,11 @@ __global__ void __launch_bounds__(256) k_bg_density(int64_t M, const __half* __r
         float acc = 0.0f;
         if (act) {
             float h[8];
+            if (Hm_lo) {                               // the low half first (smaller addends)
+                load_half8(Hm_lo + r * (int64_t)ldh + 8 * lane, h);
+#pragma unroll
+                for (int i = 0; i < 8; ++i) acc = fmaf(h[i], wl[i], acc);
+            }
             load_half8(Hm + r * (int64_t)ldh + 8 * lane, h);
 #pragma unroll
             for (int i = 0; i < 8; ++i) acc = fmaf(h[i], wl[i], acc);
@@ -143,8 +167,8 @@ using namespace gbsdf;
 
 extern "C" int gbsdf_bg_encode(int64_t R, int32_t NB, const float* center, const float* ray_unit,
                                const float* dists, const float* app_table, const int32_t* app_idx, int32_t app_dim,
-                               void* X, int32_t ldx, int32_t x_cols, void* T, int32_t ldt, int32_t t_cols,
-                               void* stream) {
+                               void* X, void* X_lo, int32_t ldx, int32_t x_cols, void* T, void* T_lo, int32_t ldt,
+                               int32_t t_cols, void* stream) {
     clear_error();
     GBSDF_CHECK_ARG(R >= 0 && NB >= 0, "negative sizes");
     if (R == 0 || NB == 0) return GBSDF_OK;
@@ -155,21 +179,25 @@ extern "C" int gbsdf_bg_encode(int64_t R, int32_t NB, const float* center, const
                     "colour-input tail of %d columns for app_dim %d", t_cols, app_dim);
     GBSDF_CHECK_ARG(app_dim == 0 || (app_table && app_idx), "appearance table / index missing");
     GBSDF_CHECK_ARG(aligned(X, 16) && aligned(T, 16), "X / T must be 16-byte aligned");
+    GBSDF_CHECK_ARG((!X_lo || aligned(X_lo, 16)) && (!T_lo || aligned(T_lo, 16)), "X_lo / T_lo alignment");
     const int64_t n = R * NB;
     k_bg_encode<<<(unsigned)((n + 127) / 128), 128, 0, as_stream(stream)>>>(
-        R, NB, center, ray_unit, dists, app_table, app_idx, app_dim, (__half*)X, ldx, x_cols, (__half*)T, ldt, t_cols);
+        R, NB, center, ray_unit, dists, app_table, app_idx, app_dim, (__half*)X, (__half*)X_lo, ldx, x_cols,
+        (__half*)T, (__half*)T_lo, ldt, t_cols);
     return launch_status("bg_encode");
 }
 
-extern "C" int gbsdf_bg_density(int64_t M, const void* Hm, int32_t ldh, int32_t H, const float* w, const float* b,
-                                float* sigma, void* stream) {
+extern "C" int gbsdf_bg_density(int64_t M, const void* Hm, const void* Hm_lo, int32_t ldh, int32_t H, const float* w,
+                                const float* b, float* sigma, void* stream) {
     clear_error();
     GBSDF_CHECK_ARG(M >= 0, "M < 0");
     if (M == 0) return GBSDF_OK;
     GBSDF_CHECK_ARG(Hm && w && b && sigma, "NULL pointer");
     GBSDF_CHECK_ARG(H % 8 == 0 && H <= 256 && ldh >= H && ldh % 8 == 0 && aligned(Hm, 16), "hidden width %d", H);
+    GBSDF_CHECK_ARG(!Hm_lo || aligned(Hm_lo, 16), "H_lo alignment");
     int64_t blocks = (M + 7) / 8;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    k_bg_density<<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(M, (const __half*)Hm, ldh, H, w, b, sigma);
+    k_bg_density<<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(M, (const __half*)Hm, (const __half*)Hm_lo, ldh, H,
+                                                                   w, b, sigma);
     return launch_status("bg_density");
 }

@@ -71,7 +71,8 @@ constexpr int STAGE_BYTES = DENSE_EPI_WARPS * 32 * 32 * 2;  // per-warp output s
 template <int N_TILE, int EPI>
 __global__ void __launch_bounds__(DENSE_TPB, 1) k_dense(const __grid_constant__ CUtensorMap tm_x,
                                                         const __grid_constant__ CUtensorMap tm_xlo,
-                                                        const __grid_constant__ CUtensorMap tm_y, DenseParams p) {
+                                                        const __grid_constant__ CUtensorMap tm_y,
+                                                        const __grid_constant__ CUtensorMap tm_ylo, DenseParams p) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int K = p.K, nslots = p.nslots;
     uint8_t* w_s = smem;                                              // [N_TILE x K]
@@ -252,9 +253,10 @@ __global__ void __launch_bounds__(DENSE_TPB, 1) k_dense(const __grid_constant__ 
                         // coalesced write-back: the warp's block goes through a 2 KB staging
                         // buffer of 64-byte rows (64-byte swizzle: 16-byte chunk j of row r at
                         // chunk j ^ ((r >> 1) & 3)) and leaves as TMA stores; rows past M are
-                        // clipped by the TMA unit.  fp16: one 32 x 32 box; fp32: two 32 x 16 boxes.
+                        // clipped by the TMA unit.  fp16: one 32 x 32 box (then, with a low
+                        // half, a second box of the residuals into Ylo); fp32: two 32 x 16 boxes.
                         uint8_t* stg = stage_s + warp * (32 * 32 * 2);
-                        const int halves = p.y_f32 ? 2 : 1;
+                        const int halves = (p.y_f32 || p.Ylo) ? 2 : 1;
                         for (int hh = 0; hh < halves; ++hh) {
                             if (lane == 0) umma::bulk_wait_read0();      // the previous store has read it
                             __syncwarp();
@@ -268,8 +270,14 @@ __global__ void __launch_bounds__(DENSE_TPB, 1) k_dense(const __grid_constant__ 
                                 } else {
                                     __half2 h[4];
 #pragma unroll
-                                    for (int k = 0; k < 4; ++k)
-                                        h[k] = __floats2half2_rn(v[8 * j + 2 * k], v[8 * j + 2 * k + 1]);
+                                    for (int k = 0; k < 4; ++k) {
+                                        float a = v[8 * j + 2 * k], b = v[8 * j + 2 * k + 1];
+                                        if (hh == 1) {             // the low half: fp16 residuals
+                                            a -= __half2float(__float2half_rn(a));
+                                            b -= __half2float(__float2half_rn(b));
+                                        }
+                                        h[k] = __floats2half2_rn(a, b);
+                                    }
                                     u = *reinterpret_cast<const uint4*>(h);
                                 }
                                 *reinterpret_cast<uint4*>(stg + lane * 64 + ((j ^ ((lane >> 1) & 3)) * 16)) = u;
@@ -277,7 +285,10 @@ __global__ void __launch_bounds__(DENSE_TPB, 1) k_dense(const __grid_constant__ 
                             umma::fence_proxy_async_smem();
                             __syncwarp();
                             if (lane == 0) {
-                                umma::tma_store_2d(&tm_y, n0 + c0 + 16 * hh, (int)(t * TILE_M) + q * 32, stg);
+                                if (p.y_f32)
+                                    umma::tma_store_2d(&tm_y, n0 + c0 + 16 * hh, (int)(t * TILE_M) + q * 32, stg);
+                                else
+                                    umma::tma_store_2d(hh ? &tm_ylo : &tm_y, n0 + c0, (int)(t * TILE_M) + q * 32, stg);
                                 umma::bulk_commit();
                             }
                         }
@@ -336,9 +347,9 @@ static int y_tensor_map(CUtensorMap* map, void* base, int64_t rows, int cols, in
 
 template <int N_TILE, int EPI>
 static int launch_dense(DenseParams p, cudaStream_t s) {
-    // the TMA write-back needs 32-column chunks, no low output half, 16-byte row strides and
-    // the staging buffers next to at least MIN_SLOTS ring slots
-    p.tma_store = (N_TILE / 4 >= 32 && !p.Ylo && aligned(p.Y, 16) && p.ldy % (p.y_f32 ? 4 : 8) == 0 &&
+    // the TMA write-back needs 32-column chunks, 16-byte row strides and the staging buffers
+    // next to at least MIN_SLOTS ring slots
+    p.tma_store = (N_TILE / 4 >= 32 && aligned(p.Y, 16) && p.ldy % (p.y_f32 ? 4 : 8) == 0 &&
                    dense_smem_slots(N_TILE, p.K, MIN_SLOTS, true) <= DENSE_SMEM_MAX) ? 1 : 0;
     p.nslots = dense_slots(N_TILE, p.K, p.tma_store != 0);
     const size_t smem = dense_smem_slots(N_TILE, p.K, p.nslots, p.tma_store != 0);
@@ -351,7 +362,7 @@ static int launch_dense(DenseParams p, cudaStream_t s) {
     int64_t groups = sm_count() / p.n_split;
     if (groups < 1) groups = 1;
     if (groups > ntiles) groups = ntiles;
-    CUtensorMap tm_x, tm_xlo, tm_y;
+    CUtensorMap tm_x, tm_xlo, tm_y, tm_ylo;
     if (int st = a_tensor_map(&tm_x, p.X, p.M, p.K, p.ldx)) return st;
     if (int st = a_tensor_map(&tm_xlo, p.Xlo ? p.Xlo : p.X, p.M, p.K, p.ldx)) return st;
     if (p.tma_store) {
@@ -359,7 +370,12 @@ static int launch_dense(DenseParams p, cudaStream_t s) {
     } else {
         tm_y = tm_x;                                       // unused
     }
-    k_dense<N_TILE, EPI><<<(unsigned)(groups * p.n_split), DENSE_TPB, smem, s>>>(tm_x, tm_xlo, tm_y, p);
+    if (p.tma_store && p.Ylo) {
+        if (int st = y_tensor_map(&tm_ylo, p.Ylo, p.M, p.N_total, p.ldy, false)) return st;
+    } else {
+        tm_ylo = tm_y;                                     // unused
+    }
+    k_dense<N_TILE, EPI><<<(unsigned)(groups * p.n_split), DENSE_TPB, smem, s>>>(tm_x, tm_xlo, tm_y, tm_ylo, p);
     return launch_status("dense");
 }
 

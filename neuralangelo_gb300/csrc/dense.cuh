@@ -88,6 +88,14 @@ __device__ __forceinline__ void store_half8(__half* dst, const float* v) {
     for (int i = 0; i < 4; ++i) h[i] = __floats2half2_rn(v[2 * i], v[2 * i + 1]);
     *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(h);
 }
+// the fp16 residual v - fp16(v) of eight values: with store_half8's hi half, hi + lo
+// carries an FP32 value to ~2^-22 relative (the low half of an activation pair)
+__device__ __forceinline__ void store_half8_lo(__half* dst, const float* v) {
+    float lo[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) lo[i] = v[i] - __half2float(__float2half_rn(v[i]));
+    store_half8(dst, lo);
+}
 __device__ __forceinline__ void load_half8(const __half* src, float* v) {
     const uint4 u = *reinterpret_cast<const uint4*>(src);
     const __half2* h = reinterpret_cast<const __half2*>(&u);

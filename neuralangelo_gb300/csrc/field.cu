@@ -424,9 +424,15 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
                 part4[j & 3] = fmaf(wh_s[c0 + j], h, part4[j & 3]);
             }
             if (keep) {
-                __half* dst = (__half*)p.h0c + s * (int64_t)(p.ld_h0c > 0 ? p.ld_h0c : HID) + c0;
+                const int64_t off = s * (int64_t)(p.ld_h0c > 0 ? p.ld_h0c : HID) + c0;
+                __half* dst = (__half*)p.h0c + off;
 #pragma unroll
                 for (int j = 0; j < 32; j += 8) store_half8(dst + j, v + j);
+                if (p.h0c_lo) {
+                    __half* lo = (__half*)p.h0c_lo + off;
+#pragma unroll
+                    for (int j = 0; j < 32; j += 8) store_half8_lo(lo + j, v + j);
+                }
             }
         }
         part_s[half * TILE_M + row] = (part4[0] + part4[1]) + (part4[2] + part4[3]);
@@ -511,6 +517,7 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
                         o8[i] = val;
                     }
                     store_half8(dst + 8 * kc8, o8);
+                    if (p.xc_lo) store_half8_lo((__half*)p.xc_lo + ss * (int64_t)p.ldxc + HID + 8 * kc8, o8);
                 }
             }
         }
@@ -571,7 +578,9 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
                                                              const __grid_constant__ CUtensorMap tm_pre32,
                                                              const __grid_constant__ CUtensorMap tm_pre30,
                                                              const __grid_constant__ CUtensorMap tm_enc32,
-                                                             const __grid_constant__ CUtensorMap tm_enc30) {
+                                                             const __grid_constant__ CUtensorMap tm_enc30,
+                                                             const __grid_constant__ CUtensorMap tm_plo32,
+                                                             const __grid_constant__ CUtensorMap tm_plo30) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int K0 = p.K0;
     const int KB = K0 + 16;                                     // features hi + tail
@@ -588,7 +597,8 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     float* df_s = dwh_s + HID;                                  // [2][7][18] d f per evaluation, double-buffered
     float* dh0_s = df_s + 2 * EVALS * SPT + 4;                  // [18][DH0_LD] d_h0c of the tile's samples
     uint64_t* mbar = reinterpret_cast<uint64_t*>(dh0_s + SPT * DH0_LD);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+    uint64_t* mbar_lo = mbar + 1;                               // DW: the lo-half dW0 MMAs of a tile
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     stage_rows_kmajor(w_s, (const __half*)p.w0b, 0, HID, KB, KB, tid, BWD_THREADS, HID);
@@ -606,6 +616,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     }
     if (tid == 0) {
         umma::mbar_init(mbar, 1);
+        umma::mbar_init(mbar_lo, 1);
         umma::fence_mbar_init();
     }
     if (warp == 0) {
@@ -634,7 +645,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     const int q = warp & 3, part = warp >> 2;                   // lane quadrant, quarter of the hidden units
     const int row = q * 32 + lane;
     const int e_row = row / SPT, sl_row = row % SPT;
-    uint32_t phase = 0;
+    uint32_t phase = 0, phase_lo = 0;
     float dbh = 0.0f;
     bool ok = true;
 
@@ -843,6 +854,30 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
             umma::bulk_commit();
         }
         umma::tmem_wait_st();
+        if (!DW && p.d_pre0_lo) {
+            // d_pre's lo half to d_pre0_lo through the same staging rows, read back from TMEM
+            // once the hi store has read them (the layer-0 weight gradient needs the pair)
+            if (lane == 0) umma::bulk_wait_read0();
+            __syncwarp();
+#pragma unroll 1
+            for (int c0 = part * 64; c0 < part * 64 + 64; c0 += 16) {
+                float f[8];
+                umma::tmem_ld8(umma::taddr(t_lo(c0 >> 4), q * 32, 0), f);
+                const int u = (c0 - part * 64) >> 3;
+                *reinterpret_cast<uint4*>(stg + lane * 128 + ((u ^ (lane & 7)) * 16)) =
+                    make_uint4(__float_as_uint(f[0]), __float_as_uint(f[1]), __float_as_uint(f[2]),
+                               __float_as_uint(f[3]));
+                *reinterpret_cast<uint4*>(stg + lane * 128 + (((u + 1) ^ (lane & 7)) * 16)) =
+                    make_uint4(__float_as_uint(f[4]), __float_as_uint(f[5]), __float_as_uint(f[6]),
+                               __float_as_uint(f[7]));
+            }
+            umma::fence_proxy_async_smem();
+            __syncwarp();
+            if (lane == 0) {
+                umma::tma_store_2d(q == 3 ? &tm_plo30 : &tm_plo32, part * 64, y0, stg);
+                umma::bulk_commit();
+            }
+        }
         umma::fence_before_sync();
         __syncthreads();
         // (3) d_enc = d_pre * W0e  (MMA2: A = d_pre [128 x 256] in TMEM; B = W0e read
@@ -898,13 +933,55 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
             break;
         }
         umma::fence_after_sync();
+        if constexpr (DW) {
+            // dW0[h] += d_pre lo^T [x hi | tail]: the hi MMAs have completed with MMA2, so the
+            // staging rows take d_pre's lo half, read back from TMEM before the next tile's MMA1
+            // overwrites it.  The +eps / -eps taps carry large, nearly cancelling d_pre, and a
+            // single fp16 rounding of d_pre in dW0 would leave ~1e-3 of it behind.
+#pragma unroll 1
+            for (int c0 = part * 64; c0 < part * 64 + 64; c0 += 16) {
+                float f[8];
+                umma::tmem_ld8(umma::taddr(t_lo(c0 >> 4), q * 32, 0), f);
+                const int u = (c0 - part * 64) >> 3;
+                *reinterpret_cast<uint4*>(stg + lane * 128 + ((u ^ (lane & 7)) * 16)) =
+                    make_uint4(__float_as_uint(f[0]), __float_as_uint(f[1]), __float_as_uint(f[2]),
+                               __float_as_uint(f[3]));
+                *reinterpret_cast<uint4*>(stg + lane * 128 + (((u + 1) ^ (lane & 7)) * 16)) =
+                    make_uint4(__float_as_uint(f[4]), __float_as_uint(f[5]), __float_as_uint(f[6]),
+                               __float_as_uint(f[7]));
+            }
+            umma::fence_proxy_async_smem();
+            umma::fence_before_sync();
+            __syncthreads();
+            if (tid == 0) {
+                umma::fence_after_sync();
+                const uint32_t st = umma::smem_u32(stage_s);
+                const uint32_t id_b = umma::idesc_f16_mn(TILE_M, KB);
+                for (int h = 0; h < 2; ++h) {
+                    const uint32_t d = t_dw + (uint32_t)(h * KB);
+                    for (int ks = 0; ks < TILE_M / 16; ++ks) {
+                        const uint64_t ad = umma::make_desc_sw128_mn(st + h * 32768u + ks * 2048u, 16384u, 1024u);
+                        const uint64_t bd = umma::make_desc(a_addr(cb) + ks * 2u * KB * 16u, KB * 16u, 128u);
+                        umma::mma_f16(d, ad, bd, id_b, 1u);
+                    }
+                }
+                umma::mma_commit(mbar_lo);
+            }
+        }
         if (DW && tn < ntiles) issue1(nb);           // D1 is free: MMA2 has read d_pre
         // (4) d_enc rows to global for k_field_scatter: 16-column chunks dealt in turn
         // to the four warps of a lane quadrant (K0 <= 128: at most two per warp, one
         // 2 KB half of the staging buffer each; 64-byte swizzle: unit j of row r at j ^ ((r >> 1) & 3))
         if (lane == 0) umma::bulk_wait_read0();      // the d_pre0 store (or, DW, dW0's MMAs) has read it
+        if constexpr (DW) {
+            // the lo dW0 MMAs read the staging rows: wait for them before d_enc goes through
+            // (a timed-out wait skips this warp's stores; the tile's closing barrier ends the loop)
+            ok = __all_sync(0xffffffffu, umma::mbar_wait(mbar_lo, phase_lo));
+            phase_lo ^= 1u;
+            if (!ok && lane == 0) flag_timeout(p.err, 1);
+        }
         __syncwarp();
-        for (int c0 = part * 16, i = 0; c0 < K0; c0 += 64, ++i) {
+        for (int c0 = part * 16, i = 0; ok && c0 < K0; c0 += 64, ++i) {
             float v[16];
             umma::tmem_ld16(umma::taddr(t_enc, q * 32, c0), v);
             uint8_t* eb = stg + i * 2048;
@@ -927,15 +1004,15 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
                 umma::fence_proxy_async_smem();
             }
         }
-        __syncthreads();   // the TMEM accumulator of tile t read; tile tn's A tile and d f in place
-        if (!DW && tn < ntiles) issue1(nb);
+        ok = __syncthreads_and(ok);   // the TMEM accumulator of tile t read; tile tn's A tile and d f in place
+        if (ok && !DW && tn < ntiles) issue1(nb);
     }
     cp_async_wait_all();
     if (lane == 0) umma::bulk_wait0();               // this warp's TMA stores have completed
     umma::fence_before_sync();
     __syncthreads();
     if constexpr (DW) {
-        // the CTA's dW0 (complete: the last MMA2 completion covered it): warps with part 2h, 2h + 1
+        // the CTA's dW0 (complete: the last tile's lo MMAs were waited for): warps with part 2h, 2h + 1
         // read hidden half h, one half of its KB columns each
         if (!dw_first && ok) {
             umma::fence_after_sync();
@@ -1100,7 +1177,7 @@ static size_t bwd_smem(int K0, bool dw) {
     const size_t KB = (size_t)K0 + 16;
     const size_t need = (size_t)(BWD_THREADS / 32) * BWD_STAGE_BYTES + (size_t)HID * KB * 2 +
                         (size_t)TILE_M * (KB + (dw ? KB : K0)) * 2 * (dw ? 2 : 1) +
-                        (2 * HID + 2 * EVALS * SPT + 4 + SPT * DH0_LD) * 4 + 16;
+                        (2 * HID + 2 * EVALS * SPT + 4 + SPT * DH0_LD) * 4 + 24;
     return need > BWD_SMEM_FLOOR ? need : BWD_SMEM_FLOOR;
 }
 
@@ -1150,7 +1227,7 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
             set_error("%lld backward rows exceed the TMA coordinate range", (long long)rows);
             return GBSDF_ERR_UNSUPPORTED;
         }
-        CUtensorMap tm_pre32, tm_pre30, tm_enc32, tm_enc30;
+        CUtensorMap tm_pre32, tm_pre30, tm_enc32, tm_enc30, tm_plo32, tm_plo30;
         const CUtensorMapL2promotion l2n = CU_TENSOR_MAP_L2_PROMOTION_NONE;
         if (!dw) {
             if (int st = tensor_map_2d(&tm_pre32, false, p.d_pre0, rows, HID, HID, 64, 32,
@@ -1167,14 +1244,26 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
                                    "d_enc"))
             return st;
         if (dw) tm_pre32 = tm_pre30 = tm_enc32;
+        if (!dw && p.d_pre0_lo) {
+            if (int st = tensor_map_2d(&tm_plo32, false, p.d_pre0_lo, rows, HID, HID, 64, 32,
+                                       CU_TENSOR_MAP_SWIZZLE_128B, l2n, "d_pre0_lo"))
+                return st;
+            if (int st = tensor_map_2d(&tm_plo30, false, p.d_pre0_lo, rows, HID, HID, 64, 30,
+                                       CU_TENSOR_MAP_SWIZZLE_128B, l2n, "d_pre0_lo"))
+                return st;
+        } else {
+            tm_plo32 = tm_plo30 = tm_pre32;              // unused
+        }
         int64_t grid = num_sms();
         if (grid > ntiles) grid = ntiles;
         if (dw) {
             allow_max_smem(k_field_bwd<F, true>);
-            k_field_bwd<F, true><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30);
+            k_field_bwd<F, true><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30,
+                                                                             tm_plo32, tm_plo30);
         } else {
             allow_max_smem(k_field_bwd<F, false>);
-            k_field_bwd<F, false><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30);
+            k_field_bwd<F, false><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30,
+                                                                              tm_plo32, tm_plo30);
         }
         if (int st = launch_status("field backward")) return st;
     }
@@ -1228,6 +1317,8 @@ static int check_fwd(const FieldParams& p, int which) {
         GBSDF_CHECK_ARG(!p.xc || (p.ldxc % 16 == 0 && p.ldxc - HID >= 23 + p.app_dim && p.ldxc - HID <= 48),
                         "xc leading dimension %d (needs 256 + 23 + app_dim <= ldxc <= 304, multiple of 16)", p.ldxc);
         GBSDF_CHECK_ARG(!p.xc || p.app_dim == 0 || (p.app_table && p.app_idx), "appearance table / index missing");
+        GBSDF_CHECK_ARG(!p.h0c_lo || aligned(p.h0c_lo, 16), "h0c_lo misaligned");
+        GBSDF_CHECK_ARG(!p.xc_lo || (p.xc && aligned(p.xc_lo, 16)), "xc_lo needs xc and 16-byte alignment");
     }
     return GBSDF_OK;
 }
@@ -1243,6 +1334,7 @@ static int check_bwd(const FieldParams& p, int which) {
         GBSDF_CHECK_ARG(p.d_w0 || (p.d_pre0 && aligned(p.d_pre0, 16)), "d_pre0 missing or misaligned (no d_w0)");
         GBSDF_CHECK_ARG(!p.d_w0 || p.K0 <= 64, "d_w0 needs K0 <= 64 (K0 %d): pass d_pre0 instead", p.K0);
         GBSDF_CHECK_ARG(aligned(p.d_h0c, 16), "d_h0c alignment");
+        GBSDF_CHECK_ARG(!p.d_pre0_lo || aligned(p.d_pre0_lo, 16), "d_pre0_lo alignment");
     }
     if (which & FK_SCATTER) GBSDF_CHECK_ARG(p.d_table && aligned(p.d_table, 16), "d_table missing or misaligned");
     return GBSDF_OK;

@@ -41,7 +41,7 @@ class FieldArgs(ctypes.Structure):
                 ("d_hess", c_vp), ("d_xc", c_vp), ("ld_dxc", c_i32), ("normal_col", c_i32), ("d_h0c", c_vp),
                 ("d_table", c_vp), ("d_pre0", c_vp), ("x0ext", c_vp), ("d_enc", c_vp), ("d_whead", c_vp),
                 ("d_bhead", c_vp),
-                ("err", c_vp), ("d_w0", c_vp)]
+                ("err", c_vp), ("d_w0", c_vp), ("h0c_lo", c_vp), ("xc_lo", c_vp), ("d_pre0_lo", c_vp)]
 
 
 class RenderArgs(ctypes.Structure):
@@ -68,9 +68,9 @@ _lib.register("gbsdf_rgb_head_bwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp
 _lib.register("gbsdf_app_grad", [c_i64, c_i32, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_vp])
 _lib.register("gbsdf_sdf_points", [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_f32, c_vp, c_vp])
 _lib.register("gbsdf_gemm_wgrad", [c_i64, c_i32, c_i32, c_vp, c_i32, c_vp, c_i32, c_vp, c_i32, c_f32, c_f32, c_vp])
-_lib.register("gbsdf_bg_encode", [c_i64, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i32,
-                                  c_i32, c_vp])
-_lib.register("gbsdf_bg_density", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp])
+_lib.register("gbsdf_bg_encode", [c_i64, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_i32, c_i32, c_vp,
+                                  c_vp, c_i32, c_i32, c_vp])
+_lib.register("gbsdf_bg_density", [c_i64, c_vp, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp])
 
 BG_X_COLS = 96        # background input: 84 encoding columns, the ones column at 84, zeros
 BG_S_COLS = 256 + BG_X_COLS    # [h4 | background input]: the skip layer's input (modules.py:258-261)
@@ -100,10 +100,11 @@ def _dense(X, Wt, N, K, out, bias=None, epi=EPI_IDENTITY, beta=100.0, G=None, er
               int(epi), float(beta), c_vp(_p(err)), _lib.stream_ptr(X.device))
 
 
-def _wgrad(dZ, X, N, K, dW):
-    """dW[N, K] = dZ[:, :N]^T X[:, :K] (fp32 out)."""
+def _wgrad(dZ, X, N, K, dW, accumulate=False):
+    """dW[N, K] (+)= dZ[:, :N]^T X[:, :K] (fp32 out)."""
     _lib.call("gbsdf_gemm_wgrad", dZ.shape[0], N, K, c_vp(dZ.data_ptr()), dZ.stride(0), c_vp(X.data_ptr()),
-              X.stride(0), c_vp(dW.data_ptr()), dW.stride(0), 1.0, 0.0, _lib.stream_ptr(dZ.device))
+              X.stride(0), c_vp(dW.data_ptr()), dW.stride(0), 1.0, 1.0 if accumulate else 0.0,
+              _lib.stream_ptr(dZ.device))
 
 
 def pack_sdf(sdf):
@@ -163,9 +164,17 @@ def sdf_weight_args(sdf, pk, A, K0, err=None):
 class FusedField:
     """Fused FP16 forward+backward over a FieldModel's FP32 master parameters."""
 
-    def __init__(self, model, loss_scale=2.0 ** 15, split_colour_grads=False, fused_w0_grad=True):
+    def __init__(self, model, loss_scale=2.0 ** 15, split_colour_grads=False, fused_w0_grad=True,
+                 activation_pairs=True):
         check_struct_sizes()
         self.model = model
+        # forward activations that feed another layer's forward stored as fp16 hi + lo pairs
+        # (the SDF layer-0 output, the colour input, the colour hidden layers but the last):
+        # with single fp16 storage the next layer's pre-activations move by the fp16 rounding
+        # and single weight gradients miss the float64 oracle by up to ~4e-3; with the pairs
+        # they agree to ~1e-7 in the oracle's own emulation.  The weight gradients read the hi
+        # halves only (that costs <= 2e-4).  False: single fp16 storage (faster, less accurate).
+        self.pairs = bool(activation_pairs)
         # the layer-0 weight gradient: accumulated by the backward kernel itself (K0 <= 64), or
         # (False, or K0 > 64) from the kernel's fp16 d_pre0 rows by a separate GEMM
         self.fused_w0_grad = bool(fused_w0_grad)
@@ -304,7 +313,7 @@ class FusedField:
         return self.fused_w0_grad and self.K0 <= 64
 
     def _workspace(self, R, S, Ns, device):
-        key = (R, S, Ns, self.K0, self.bg)
+        key = (R, S, Ns, self.K0, self.bg, self.pairs)
         if self.ws is not None and self.ws['key'] == key:
             return self.ws
         self.ws = None                      # release the previous shape's buffers first
@@ -325,11 +334,18 @@ class FusedField:
                   dxc_tail=e(Ns, 64), d_h0c=e(Ns, 256),
                   # K0 <= 64: the backward kernel accumulates dW0 itself; otherwise d_pre0 -> GEMM
                   d_pre0=None if self._in_kernel_w0_grad() else e(rows0, 256, dt=f16),
+                  d_pre0_lo=None if self._in_kernel_w0_grad() else e(rows0, 256, dt=f16),
                   d_w0=e(256, self.K0 + 16) if self._in_kernel_w0_grad() else None,
                   x0ext=e(rows0, 2 * self.K0 + 16, dt=f16), d_enc=e(rows0, self.K0),
                   d_whead=torch.zeros(256, device=device),
                   d_bhead=torch.zeros(1, device=device), d_bl=torch.zeros(3, device=device),
                   err=torch.zeros(1, device=device, dtype=torch.int32))
+        if self.pairs:
+            # low halves, with the row strides of their hi buffers (the constant-1 column's lo is 0)
+            ws.update(h0c_lo=e(Ns, 264, dt=f16).zero_(), xc_lo=e(Ns, self.Kc0, dt=f16),
+                      ys_lo=[e(Ns, Hc + 8, dt=f16) for _ in range(self.n_rgb_hidden - 1)])
+        else:
+            ws.update(h0c_lo=None, xc_lo=None, ys_lo=[None] * (self.n_rgb_hidden - 1))
         if self.bg:
             Nb = R * self.n_bg
             Hbr = self.Hbr
@@ -341,6 +357,18 @@ class FusedField:
                       bg_d_pre_last=e(Nb, 8, dt=f16), bg_dz_r=e(Nb, Hbr, dt=f16),
                       bg_dz=[e(Nb, 256, dt=f16) for _ in range(2)],
                       bg_d_tail=e(Nb, 64) if self.app_dim else None, bg_d_bl=torch.zeros(3, device=device))
+            if self.pairs:
+                # low halves of every background activation that feeds another layer's forward
+                # (or the density head); the colour hidden layer feeds the FP32 head only
+                z = lambda *sh: torch.zeros(*sh, device=device, dtype=f16)  # noqa: E731
+                ws.update(bg_S_lo=z(Nb, BG_S_COLS), bg_h_lo={i: z(Nb, 264) for i in (1, 2, 3, 5, 6, 7)},
+                          bg_G_lo=z(Nb, self.Kr0),
+                          # the backward's input gradients too: they pass through up to eight layers
+                          # (the density column of dZ7 stays a single fp16 value: its lo is 0)
+                          bg_dz_r_lo=z(Nb, Hbr), bg_dZ7_lo=z(Nb, 272), bg_dz_lo=[z(Nb, 256) for _ in range(2)])
+            else:
+                ws.update(bg_S_lo=None, bg_h_lo={i: None for i in (1, 2, 3, 5, 6, 7)}, bg_G_lo=None,
+                          bg_dz_r_lo=None, bg_dZ7_lo=None, bg_dz_lo=[None, None])
         self.ws = ws
         return ws
 
@@ -417,6 +445,7 @@ class FusedField:
         fa.app_dim, fa.app_table = self.app_dim, _p(pk['app'])
         fa.sdf, fa.grad, fa.hess, fa.h0c = _p(ws['sdf']), _p(ws['grad']), _p(ws['hess']), _p(ws['h0c'])
         fa.ld_h0c = ws['h0c'].stride(0)
+        fa.h0c_lo, fa.xc_lo = _p(ws['h0c_lo']), _p(ws['xc_lo'])
         fa.x0ext = _p(ws['x0ext'])
         fa.err = _p(ws['err'])
         # ---------------- forward ----------------
@@ -424,11 +453,15 @@ class FusedField:
         _lib.call("gbsdf_field_mlp_fwd", ctypes.byref(fa), stream)
         # SDF feature layer, written into the colour input's first 256 columns
         _dense(ws['h0c'], pk['w1'], 256, 256, ws['xc'], bias=pk['b1'], epi=EPI_SOFTPLUS, beta=fa.beta,
-               err=ws['err'])
-        X, K = ws['xc'], self.Kc0
+               err=ws['err'], X_lo=ws['h0c_lo'], out_lo=ws['xc_lo'])
+        X, Xl, K = ws['xc'], ws['xc_lo'], self.Kc0
+        n_last = self.n_rgb_hidden - 1
         for i in range(self.n_rgb_hidden):
-            _dense(X, pk['wc'][i], Hc, K, ws['ys'][i], bias=pk['bc'][i], epi=EPI_RELU, err=ws['err'])
-            X, K = ws['ys'][i], Hc
+            # the last hidden layer feeds only the FP32 colour head: single fp16 storage suffices
+            Yl = ws['ys_lo'][i] if i < n_last else None
+            _dense(X, pk['wc'][i], Hc, K, ws['ys'][i], bias=pk['bc'][i], epi=EPI_RELU, err=ws['err'], X_lo=Xl,
+                   out_lo=Yl)
+            X, Xl, K = ws['ys'][i], Yl, Hc
         ylast = ws['ys'][-1]
         _lib.call("gbsdf_rgb_head_fwd", Ns, c_vp(ylast.data_ptr()), ylast.stride(0), Hc, c_vp(pk['wl'].data_ptr()),
                   c_vp(pk['bl'].data_ptr()), c_vp(ws['rgbs'].data_ptr()), stream)
@@ -537,6 +570,7 @@ class FusedField:
         fa.d_xc, fa.ld_dxc, fa.normal_col = _p(ws['dxc_tail']), 64, 19
         fa.d_h0c = _p(ws['d_h0c'])
         fa.d_table, fa.d_pre0, fa.d_enc = _p(d_table), _p(ws['d_pre0']), _p(ws['d_enc'])
+        fa.d_pre0_lo = _p(ws['d_pre0_lo'])
         fa.d_whead, fa.d_bhead = _p(ws['d_whead']), _p(ws['d_bhead'])
         if ws['d_w0'] is not None:
             ws['d_w0'].zero_()
@@ -548,6 +582,8 @@ class FusedField:
         else:
             gw0x = torch.empty(256, 2 * self.K0 + 16, **dev32)
             _wgrad(ws['d_pre0'], ws['x0ext'], 256, 2 * self.K0 + 16, gw0x)
+            # d_pre's lo half against the hi features and the position/bias tail
+            _wgrad(ws['d_pre0_lo'], ws['x0ext'], 256, self.K0 + 16, gw0x, accumulate=True)
             grads['w0ext'] = gw0x
         grads['table'] = d_table
         if self.bg:
@@ -566,25 +602,32 @@ class FusedField:
         ws, pk = self.ws, self.pk
         NB, Nb, Hbr, Kr0 = self.n_bg, R * self.n_bg, self.Hbr, self.Kr0
         S, G, h = ws['bg_S'], ws['bg_G'], ws['bg_h']
+        Sl, Gl, hl = ws['bg_S_lo'], ws['bg_G_lo'], ws['bg_h_lo']
         X = S[:, 256:]
+        Xl = Sl[:, 256:] if Sl is not None else None
         Gt = G[:, 256:]
+        Gtl = Gl[:, 256:] if Gl is not None else None
         _lib.call("gbsdf_bg_encode", R, NB, c_vp(center.data_ptr()), c_vp(ray_unit.data_ptr()),
                   c_vp(dists_bg.data_ptr()), c_vp(_p(pk['app_bg'])), c_vp(_p(app_idx)), self.app_dim,
-                  c_vp(X.data_ptr()), S.stride(0), BG_X_COLS, c_vp(Gt.data_ptr()), G.stride(0), Kr0 - 256, stream)
+                  c_vp(X.data_ptr()), c_vp(_p(Xl)), S.stride(0), BG_X_COLS, c_vp(Gt.data_ptr()), c_vp(_p(Gtl)),
+                  G.stride(0), Kr0 - 256, stream)
         err = ws['err']
         w, b = pk['bw'], pk['bb']
-        _dense(X, w[0], 256, BG_X_COLS, h[1], bias=b[0], epi=EPI_RELU, err=err)
-        _dense(h[1], w[1], 256, 256, h[2], bias=b[1], epi=EPI_RELU, err=err)
-        _dense(h[2], w[2], 256, 256, h[3], bias=b[2], epi=EPI_RELU, err=err)
-        _dense(h[3], w[3], 256, 256, S, bias=b[3], epi=EPI_RELU, err=err)            # h4 into S[:, :256]
-        _dense(S, w[4], 256, BG_S_COLS, h[5], bias=b[4], epi=EPI_RELU, err=err)      # skip: [h4 | input]
-        _dense(h[5], w[5], 256, 256, h[6], bias=b[5], epi=EPI_RELU, err=err)
-        _dense(h[6], w[6], 256, 256, h[7], bias=b[6], epi=EPI_RELU, err=err)
-        _dense(h[7], w[7], 256, 256, G, bias=b[7], epi=EPI_RELU, err=err)            # features into G[:, :256]
-        _lib.call("gbsdf_bg_density", Nb, c_vp(h[7].data_ptr()), h[7].stride(0), 256, c_vp(pk['bw7d'].data_ptr()),
-                  c_vp(pk['bb7d'].data_ptr()), c_vp(ws['bg_sigma'].data_ptr()), stream)
+        _dense(X, w[0], 256, BG_X_COLS, h[1], bias=b[0], epi=EPI_RELU, err=err, X_lo=Xl, out_lo=hl[1])
+        _dense(h[1], w[1], 256, 256, h[2], bias=b[1], epi=EPI_RELU, err=err, X_lo=hl[1], out_lo=hl[2])
+        _dense(h[2], w[2], 256, 256, h[3], bias=b[2], epi=EPI_RELU, err=err, X_lo=hl[2], out_lo=hl[3])
+        _dense(h[3], w[3], 256, 256, S, bias=b[3], epi=EPI_RELU, err=err,             # h4 into S[:, :256]
+               X_lo=hl[3], out_lo=Sl)
+        _dense(S, w[4], 256, BG_S_COLS, h[5], bias=b[4], epi=EPI_RELU, err=err,       # skip: [h4 | input]
+               X_lo=Sl, out_lo=hl[5])
+        _dense(h[5], w[5], 256, 256, h[6], bias=b[5], epi=EPI_RELU, err=err, X_lo=hl[5], out_lo=hl[6])
+        _dense(h[6], w[6], 256, 256, h[7], bias=b[6], epi=EPI_RELU, err=err, X_lo=hl[6], out_lo=hl[7])
+        _dense(h[7], w[7], 256, 256, G, bias=b[7], epi=EPI_RELU, err=err,             # features into G[:, :256]
+               X_lo=hl[7], out_lo=Gl)
+        _lib.call("gbsdf_bg_density", Nb, c_vp(h[7].data_ptr()), c_vp(_p(hl[7])), h[7].stride(0), 256,
+                  c_vp(pk['bw7d'].data_ptr()), c_vp(pk['bb7d'].data_ptr()), c_vp(ws['bg_sigma'].data_ptr()), stream)
         hr = ws['bg_hr']
-        _dense(G, pk['bwr0'], Hbr, Kr0, hr, bias=pk['bbr0'], epi=EPI_RELU, err=err)
+        _dense(G, pk['bwr0'], Hbr, Kr0, hr, bias=pk['bbr0'], epi=EPI_RELU, err=err, X_lo=Gl)
         _lib.call("gbsdf_rgb_head_fwd", Nb, c_vp(hr.data_ptr()), hr.stride(0), Hbr, c_vp(pk['bwr1'].data_ptr()),
                   c_vp(pk['bbr1'].data_ptr()), c_vp(ws['bg_rgbs'].data_ptr()), stream)
 
@@ -601,29 +644,34 @@ class FusedField:
         err = ws['err']
         g = {}
         ws['bg_d_bl'].zero_()
+        dzr_lo, dZ7_lo, dz_lo = ws['bg_dz_r_lo'], ws['bg_dZ7_lo'], ws['bg_dz_lo']
         _lib.call("gbsdf_rgb_head_bwd", Nb, c_vp(hr.data_ptr()), hr.stride(0), Hbr, c_vp(pk['bwr1'].data_ptr()),
                   c_vp(ws['bg_rgbs'].data_ptr()), c_vp(ws['bg_d_rgbs'].data_ptr()),
-                  c_vp(ws['bg_d_pre_last'].data_ptr()), c_vp(ws['bg_dz_r'].data_ptr()), None,
+                  c_vp(ws['bg_d_pre_last'].data_ptr()), c_vp(ws['bg_dz_r'].data_ptr()), c_vp(_p(dzr_lo)),
                   c_vp(ws['bg_d_bl'].data_ptr()), stream)
         g['r1'] = torch.empty(3, Hbr, **dev32)
         _wgrad(ws['bg_d_pre_last'], hr, 3, Hbr, g['r1'])
         g['r0'] = torch.empty(Hbr, Kr0, **dev32)
         _wgrad(ws['bg_dz_r'], G, Hbr, Kr0, g['r0'])                                 # bias column 256 + 16 + app
-        _dense(ws['bg_dz_r'], pk['bwr0T_feat'], 256, Hbr, dZ7, epi=EPI_DRELU, G=G, err=err)   # d feature pre-act
+        _dense(ws['bg_dz_r'], pk['bwr0T_feat'], 256, Hbr, dZ7, epi=EPI_DRELU, G=G, err=err,   # d feature pre-act
+               X_lo=dzr_lo, out_lo=dZ7_lo)
         if self.app_dim:
-            _dense(ws['bg_dz_r'], pk['bwr0T_tail'], 64, Hbr, ws['bg_d_tail'], epi=EPI_IDENTITY, err=err)
+            _dense(ws['bg_dz_r'], pk['bwr0T_tail'], 64, Hbr, ws['bg_d_tail'], epi=EPI_IDENTITY, err=err,
+                   X_lo=dzr_lo)
             g['app'] = torch.zeros_like(pk['app_bg'])
             _lib.call("gbsdf_app_grad", R, self.n_bg, None, c_vp(app_idx.data_ptr()),
                       c_vp(ws['bg_d_tail'].data_ptr()), 64, 16, self.app_dim, c_vp(g['app'].data_ptr()), stream)
         g[7] = torch.empty(272, 264, **dev32)
         _wgrad(dZ7, h[7], 272, 264, g[7])
-        _dense(dZ7, pk['bw7extT'], 256, 272, dz[0], epi=EPI_DRELU, G=h[7], err=err)       # dZ6
+        _dense(dZ7, pk['bw7extT'], 256, 272, dz[0], epi=EPI_DRELU, G=h[7], err=err,       # dZ6
+               X_lo=dZ7_lo, out_lo=dz_lo[0])
         cur = 0
         for i, gate in ((6, h[6]), (5, h[5]), (4, S), (3, h[3]), (2, h[2]), (1, h[1])):
             X = S if i == 4 else h[i]
             g[i] = torch.empty(256, X.shape[1], **dev32)
             _wgrad(dz[cur], X, 256, X.shape[1], g[i])
-            _dense(dz[cur], pk['bwT'][i], 256, 256, dz[1 - cur], epi=EPI_DRELU, G=gate, err=err)
+            _dense(dz[cur], pk['bwT'][i], 256, 256, dz[1 - cur], epi=EPI_DRELU, G=gate, err=err,
+                   X_lo=dz_lo[cur], out_lo=dz_lo[1 - cur] if i > 1 else None)
             cur = 1 - cur
         g[0] = torch.empty(256, BG_X_COLS, **dev32)
         _wgrad(dz[cur], S[:, 256:], 256, BG_X_COLS, g[0])

@@ -38,7 +38,7 @@ def build(log2T=14, n_images=10, seed=0):
     return model
 
 
-def oracle_run(model, batch, effective=True):
+def oracle_run(model, batch, effective=True, dtype=torch.float64):
     c = model.cfg
     hg = c.sdf.encoding.hashgrid
     b = c.background.mlp
@@ -50,9 +50,9 @@ def oracle_run(model, batch, effective=True):
                           bg_hidden=b.hidden_dim, bg_hidden_rgb=b.hidden_dim_rgb)
     layout = hgo.level_layout(ocfg['n_levels'], ocfg['n_features'], ocfg['log2_hashmap_size'],
                               ocfg['base_resolution'], ocfg['per_level_scale'])
-    p = {k: (v.double().clone().requires_grad_(True) if v is not None else None)
+    p = {k: (v.to(dtype).clone().requires_grad_(True) if v is not None else None)
          for k, v in params_io.model_to_oracle(model, True, effective).items()}
-    bt = {k: (v.double().cpu() if v.is_floating_point() else v.cpu()) for k, v in batch.items()}
+    bt = {k: (v.to(dtype).cpu() if v.is_floating_point() else v.cpu()) for k, v in batch.items()}
     if 'ray_offsets' in bt:
         out = of.render_step_ragged(p, ocfg, layout, bt, model.neural_sdf.normal_eps, model.progress, 0.1,
                                     model.w_curv)
@@ -90,7 +90,10 @@ def test_fused_background_matches_oracle():
     print({k: f"{v:.1e}" for k, v in e_w.items()})
     assert e_rgb < 1e-4 and e_loss < 1e-5
     assert e_tab < 1e-3
-    assert e_all < 1e-2 and e_app < 1e-2
+    # every background weight gradient on its own (activations stored as fp16 hi + lo pairs)
+    for k, e in e_w.items():
+        assert e < 1e-3, (k, e)
+    assert e_all < 1e-3 and e_app < 1e-3
 
 
 def test_fused_background_matches_plain():
@@ -131,8 +134,10 @@ def test_fused_background_ragged_matches_oracle():
     mine = params_io.model_grads(model)
     e_rgb = rel(res['rgb'].cpu(), out['rgb'].detach())
     e_tab = rel(mine['table'], g['table'])
-    _, e_all = bg_weight_errors(ff, g)
+    e_w, e_all = bg_weight_errors(ff, g)
     e_s = rel(mine['s_var'], g['s_var'])
+    model_curv = model
+    w_curv = model.w_curv
     model.w_curv = 0.0
     model.zero_grad(set_to_none=True)
     ff.step(batch)
@@ -140,7 +145,16 @@ def test_fused_background_ragged_matches_oracle():
     mine0 = params_io.model_grads(model)
     _, g0 = oracle_run(model, batch)
     e_tab0 = rel(mine0['table'], g0['table'])
+    model.w_curv = w_curv
+    print({k: f"{v:.1e}" for k, v in e_w.items()})
     print(f"\nragged background: rgb {e_rgb:.2e} table {e_tab:.2e} (without curvature {e_tab0:.2e}) "
           f"bg weights {e_all:.2e} s_var {e_s:.2e}")
-    assert e_rgb < 1e-3 and e_all < 2e-2 and e_s < 1e-3
-    assert e_tab0 < 1e-3 and e_tab < 5e-3
+    assert e_rgb < 1e-3 and e_all < 1e-3 and e_s < 1e-3
+    for k, e in e_w.items():
+        assert e < 1e-3, (k, e)
+    assert e_tab0 < 1e-3
+    # with curvature: within 1.25x of the float32 reference arithmetic's own error on the table
+    _, g32 = oracle_run(model_curv, batch, dtype=torch.float32)
+    e_tab32 = rel(g32['table'], g['table'])
+    print(f"float32 reference table-gradient error {e_tab32:.2e}")
+    assert e_tab < max(1e-3, 1.25 * e_tab32)

@@ -58,8 +58,11 @@ def test_dense_strided_output_and_input():
     assert torch.all(out[:, :256] == 0)
 
 
-def test_dense_split_operand_and_output():
-    """X = X_hi + X_lo and Y = Y_hi + Y_lo: the pair reproduces an fp32 product far below fp16 precision."""
+@pytest.mark.parametrize("pad,epi", [(0, D.EPI_DRELU), (8, D.EPI_RELU)])
+def test_dense_split_operand_and_output(pad, epi):
+    """X = X_hi + X_lo and Y = Y_hi + Y_lo: the pair reproduces an fp32 product far below fp16
+    precision.  pad 8: outputs in [M, N + 8] buffers (the activation layout of the fused step,
+    written back through TMA stores of both halves)."""
     M, K, N = 700, 256, 256
     g = torch.Generator(DEV).manual_seed(11)
     Xf = torch.randn(M, K, device=DEV, generator=g)
@@ -67,10 +70,17 @@ def test_dense_split_operand_and_output():
     X_lo = (Xf - X_hi.float()).half()
     W = (torch.randn(N, K, device=DEV, generator=g) / 16).half()
     G = torch.randn(M, N, device=DEV, generator=g).half()
-    hi = torch.empty(M, N, device=DEV, dtype=torch.float16)
-    lo = torch.empty(M, N, device=DEV, dtype=torch.float16)
-    D.dense(X_hi, W, None, epi=D.EPI_DRELU, G=G, out=hi, X_lo=X_lo, out_lo=lo)
-    R = (Xf.double() @ W.double().t()) * (G.double() > 0)
+    b = torch.randn(N, device=DEV, generator=g)
+    hi = torch.full((M, N + pad), 7.0, device=DEV, dtype=torch.float16)
+    lo = torch.full((M, N + pad), 7.0, device=DEV, dtype=torch.float16)
+    if epi == D.EPI_DRELU:
+        D.dense(X_hi, W, None, epi=epi, G=G, out=hi[:, :N], X_lo=X_lo, out_lo=lo[:, :N])
+        R = (Xf.double() @ W.double().t()) * (G.double() > 0)
+    else:
+        D.dense(X_hi, W, b, epi=epi, out=hi[:, :N], X_lo=X_lo, out_lo=lo[:, :N])
+        R = torch.relu(Xf.double() @ W.double().t() + b.double())
+    assert torch.all(hi[:, N:] == 7) and torch.all(lo[:, N:] == 7)      # padding columns untouched
+    hi, lo = hi[:, :N], lo[:, :N]
     e_pair = ((hi.double() + lo.double()) - R).norm() / R.norm()
     e_hi = (hi.double() - R).norm() / R.norm()
     assert e_pair < 1e-5, float(e_pair)

@@ -1,10 +1,12 @@
 """Fused FP16 step (tcgen05 kernels, C ABI) against the float64 oracle and the
 plain FP32 drop-in.
 
-Gates (from the field's accuracy targets): SDF relative error <= 1e-4 and
-table-gradient relative error <= 1e-3 against the float64 oracle evaluated on
-the same fp16-rounded parameters; every other gradient within 1e-2 of the
-oracle evaluated on the FP32 masters (fp16 weight rounding included)."""
+Gates (the field's accuracy targets), against the float64 oracle evaluated on the
+same fp16-rounded parameters: SDF relative error <= 1e-4, and every gradient tensor
+-- the table and each MLP weight on its own -- within 1e-3.  With the curvature
+term on, the table gradient is a second difference over the taps whose float32
+conditioning is above 1e-3: there the gate is 1.25x the float32 reference
+arithmetic's own error on the same tensor."""
 import numpy as np
 import pytest
 import torch
@@ -112,34 +114,38 @@ def test_fused_matches_oracle(small):
         d_normal=rel(ff.ws['dxc_tail'][:, 19:22].reshape(R, S, 3).cpu() / sc, out_e['normals'].grad),
         d_hess=rel((ff.ws['d_hess'].reshape(R, S, 3).cpu() / sc)[ins], out_e['hess'].grad[ins]),
     )
-    # the same oracle with the fused path's fp16 activation storage emulated: isolates the
-    # arithmetic of the fused backward from the precision of fp16 activation storage
-    out_s, g_s = oracle_run(model, batch, fp16=True, effective=True, fp16_storage=True)
-    storage = {}
-    for name, (dW, db) in ff.eff_grads.items():
-        storage[name + '.W'] = rel(dW.double().cpu(), g_s[name + '.v'])
     tgt = batch['target'].cpu().double()
     flips = int(((rgb_mine.double() - tgt).sign() != (out_q['rgb'].detach() - tgt).sign()).sum())
     margin = float((out_q['rgb'].detach() - tgt).abs().min())
     print(f"\nsdf {e_sdf:.2e} table {e_tab:.2e} rgb {e_rgb:.2e} loss {e_loss:.2e} all-params {allp:.2e} "
           f"L1-sign flips {flips} min |rgb - target| {margin:.1e}")
     print("vs fp16-weight oracle", {k: f"{v:.1e}" for k, v in worst.items()})
-    print("vs fp16-storage oracle", {k: f"{v:.1e}" for k, v in storage.items()})
     print({k: f"{v:.1e}" for k, v in diag.items()})
     assert e_sdf < 1e-4                      # SDF gate
     assert e_tab < 1e-3                      # table-gradient gate
     assert e_rgb < 1e-4
     assert e_loss < 1e-5
-    assert allp < 5e-3
-    for k, e in worst.items():               # bounded by fp16 activation storage (see below)
-        assert e < 2e-2, (k, e)
-    # The backward arithmetic itself, against the oracle that rounds its activations to fp16 at
-    # the same points.  The colour MLP's ReLU gates [y > 0] are discontinuous: a pre-activation
-    # within ~1e-5 of zero can land on either side in two valid fp16 computations, and a few
-    # such flips at heavily weighted samples move the small field's colour-weight gradients by
-    # up to ~8e-3 (two builds of this step that differ only in FP32 rounding differ by as much).
-    for k, e in storage.items():
-        assert e < 1e-2, (k, e)
+    assert allp < 1e-3
+    for k, e in worst.items():               # every gradient tensor on its own
+        assert e < 1e-3, (k, e)
+
+
+def test_single_fp16_activations_miss_the_gate_that_pairs_meet():
+    """The same step with the activations stored as single fp16 values: the next layer's
+    pre-activations move by the fp16 rounding and single weight gradients leave the 1e-3
+    band, which the hi + lo pairs of the default step close."""
+    model = build()
+    batch = make_rays(48, 32, seed=3, miss_frac=0.1, n_images=10, device=DEV)
+    errs = {}
+    _, g_e = oracle_run(model, batch, fp16=True, effective=True)
+    for pairs in (True, False):
+        ff = FusedField(model, activation_pairs=pairs)
+        model.zero_grad(set_to_none=True)
+        ff.step(batch)
+        torch.cuda.synchronize()
+        errs[pairs] = max(rel(dW.double().cpu(), g_e[n + '.v']) for n, (dW, db) in ff.eff_grads.items())
+    print(f"\nworst MLP weight-gradient error: pairs {errs[True]:.1e}, single fp16 {errs[False]:.1e}")
+    assert errs[True] < 1e-3 and errs[False] > 2 * errs[True]
 
 
 @pytest.mark.parametrize("active", [10, 16])
@@ -315,12 +321,12 @@ def test_c2_accuracy_report_512_rays():
     MLP 4x256, 100 images) for a 512-ray x 128-sample subset against the float64 oracle
     on the same fp16 parameters.
 
-    SDF <= 1e-4 and colour <= 1e-4 (relative).  The table gradient of the numerical
-    curvature loss is a second difference over the taps, (df+ + df- - 2 df0) / eps^2,
-    which amplifies FP32 rounding by up to 1/eps^2: the reference's own arithmetic run
-    in float32 on these inputs misses float64 by ~1.5e-3.  Gates: the fused table
-    gradient is within 1.25x of that float32 error, and meets 1e-3 outright with the
-    curvature weight at 0."""
+    SDF <= 1e-4 and colour <= 1e-4 (relative); each MLP weight and bias gradient <= 1e-3.
+    The table gradient of the numerical curvature loss is a second difference over the
+    taps, (df+ + df- - 2 df0) / eps^2, which amplifies FP32 rounding by up to 1/eps^2:
+    the reference's own arithmetic run in float32 on these inputs misses float64 by
+    ~1.5e-3.  Gates: with the curvature term each gradient tensor is within 1e-3 or
+    1.25x of the float32 error on that tensor; without it, the table meets 1e-3."""
     model = build(log2T=22, n_images=100, table_range=1e-2)
     batch = make_rays(512, 128, seed=11, miss_frac=0.05, n_images=100, device=DEV)
     ff = FusedField(model)
@@ -336,6 +342,9 @@ def test_c2_accuracy_report_512_rays():
     e_rgb = rel(res['rgb'].cpu(), out_q['rgb'].detach())
     e_tab = rel(mine['table'], g_q['table'])
     e_tab32 = rel(g_32['table'], g_q['table'])
+    eff_curv = {n: (dW.clone(), db.clone()) for n, (dW, db) in ff.eff_grads.items()}
+    _, g_ec = oracle_run(model, batch, fp16=True, effective=True)
+    _, g_ec32 = oracle_run(model, batch, fp16=True, effective=True, dtype=torch.float32)
     # the same step without the curvature term
     model.w_curv = 0.0
     model.zero_grad(set_to_none=True)
@@ -350,14 +359,22 @@ def test_c2_accuracy_report_512_rays():
     # the same fp16 weights, curvature off as in the step just taken
     _, g_e = oracle_run(model, batch, fp16=True, effective=True)
     e_w = {n: rel(dW.double().cpu(), g_e[n + '.v']) for n, (dW, db) in ff.eff_grads.items()}
+    e_b = {n: rel(db.double().cpu(), g_e[n + '.b']) for n, (dW, db) in ff.eff_grads.items()}
     allp = rel(np.concatenate([ff.eff_grads[n][0].double().cpu().reshape(-1) for n in ff.eff_grads]),
                np.concatenate([g_e[n + '.v'].reshape(-1) for n in ff.eff_grads]))
     print("C2 MLP weight gradients:", {k: f"{v:.1e}" for k, v in e_w.items()}, f"all MLP weights {allp:.2e}")
-    # All MLP weights together are within 1e-3.  Single colour layers and the SDF feature
-    # layer reach a few 1e-3: fp16 storage of the forward activations moves pre-activations
-    # near zero across a ReLU gate (the oracle that rounds activations to fp16 at the same
-    # points agrees to ~2e-4), and carrying the backward input gradients as hi + lo pairs
-    # leaves these figures unchanged.
+    print("C2 MLP bias gradients:", {k: f"{v:.1e}" for k, v in e_b.items()})
+    # with the curvature term on: each MLP weight gradient against the same float64 oracle,
+    # gated at 1e-3 or 1.25x the float32 reference arithmetic's error on that tensor
+    e_wc = {n: rel(dW.double().cpu(), g_ec[n + '.v']) for n, (dW, db) in eff_curv.items()}
+    e_wc32 = {n: rel(g_ec32[n + '.v'], g_ec[n + '.v']) for n in eff_curv}
+    print("C2 MLP weight gradients, curvature on:", {k: f"{v:.1e}" for k, v in e_wc.items()},
+          "float32 reference:", {k: f"{v:.1e}" for k, v in e_wc32.items()})
+    # every tensor on its own (the activations are stored as fp16 hi + lo pairs)
+    for k, e in list(e_w.items()) + list(e_b.items()):
+        assert e < 1e-3, (k, e)
+    for k, e in e_wc.items():
+        assert e < max(1e-3, 1.25 * e_wc32[k]), (k, e, e_wc32[k])
     assert allp < 1e-3
     assert e_sdf < 1e-4 and e_rgb < 1e-4
     assert e_tab < 1.25 * e_tab32
