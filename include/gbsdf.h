@@ -289,11 +289,13 @@ int gbsdf_render_fused(const gbsdf_render_args* args, void* stream);
 int gbsdf_rgb_head_fwd(int64_t Ns, const void* Y, int ldy, int H, const float* W, const float* b, float* rgbs,
                        void* stream);
 
-/* Its backward: d_rgbs [Ns,3] -> d_pre [Ns, 8] fp16 (columns 0-2, rest 0),
- * dZ = (d_pre W) * [Y > 0] as an fp16 pair dZ = dZ_hi + dZ_lo [Ns, H]
- * (dZ_lo may be NULL), d_b [3] accumulated. */
+/* Its backward: d_rgbs [Ns,3] -> d_pre = d_rgbs rgbs (1 - rgbs), optionally written to
+ * d_pre [Ns, 8] fp16 (columns 0-2, rest 0; may be NULL), dZ = (d_pre W) * [Y > 0] as an
+ * fp16 pair dZ = dZ_hi + dZ_lo [Ns, H] (dZ_lo may be NULL), d_b [3] accumulated, and the
+ * head's weight gradient d_W [3, H] += d_pre^T Y accumulated (may be NULL). */
 int gbsdf_rgb_head_bwd(int64_t Ns, const void* Y, int ldy, int H, const float* W, const float* rgbs,
-                       const float* d_rgbs, void* d_pre, void* dZ, void* dZ_lo, float* d_b, void* stream);
+                       const float* d_rgbs, void* d_pre, void* dZ, void* dZ_lo, float* d_b, float* d_W,
+                       void* stream);
 
 /* Appearance-embedding gradient: d_app[app_idx[r]] += sum over ray r's samples of
  * d_xc[s, col0 : col0 + app_dim] (fp32). */
@@ -418,10 +420,14 @@ int gbsdf_sampler_coarse(const gbsdf_sampler_args* args, int n, const float* u, 
  * n_fine = 0 the call only merges (the final round). */
 int gbsdf_sampler_round(const gbsdf_sampler_args* args, void* stream);
 
-/* Weight gradient dW [N, K] = alpha * dZ[M, N]^T X[M, K] + beta * dW (fp16 in,
- * fp32 out; cuBLAS).  dW of every MLP layer of the fused step. */
-int gbsdf_gemm_wgrad(int64_t M, int N, int K, const void* dZ, int ldz, const void* X, int ldx, float* dW,
-                     int ldw, float alpha, float beta, void* stream);
+/* Weight gradient of a dense layer on the tensor cores (the autograd weight gradient of
+ * torch.nn.Linear behind nerf_util.py:187-196, mlp.py:55-69 and modules.py:268-284):
+ * dW [N, K] (row stride ldw) = (accumulate ? dW : 0) + (dZ + dZ_lo)[M, N]^T X[M, K].
+ * dZ, the optional low half dZ_lo (same strides) and X are fp16 row-major; FP32
+ * accumulation and output.  N, K <= 512; the bias gradient is the column of X holding a
+ * constant 1.  err: device flag set when a bounded wait times out (may be NULL). */
+int gbsdf_wgrad(int64_t M, int N, int K, const void* dZ, const void* dZ_lo, int ldz, const void* X, int ldx,
+                float* dW, int ldw, int accumulate, int* err, void* stream);
 
 #ifdef __cplusplus
 }

@@ -80,9 +80,16 @@ class KernelTimer:
     def __init__(self):
         self.enabled = False
         self.events = {}
+        self.bytes = {}
 
     def reset(self):
         self.events = {}
+        self.bytes = {}
+
+    def count_bytes(self, name, nbytes):
+        """Algorithmic bytes one call of `name` must move (summed per name while enabled)."""
+        if self.enabled:
+            self.bytes[name] = self.bytes.get(name, 0) + int(nbytes)
 
     def summary(self):
         """{name: (calls, total_ms)}; call after a device synchronize."""

@@ -71,7 +71,7 @@ def build(force=False, verbose=False, extra_flags=()):
     with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB + ".tmp"
-    cmd = [cc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-lcublas"]
+    cmd = [cc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -285,49 +285,81 @@ __global__ void k_rgb_head_fwd(int64_t Ns, const __half* __restrict__ Y, int ldy
     rgbs[3 * s + 2] = sigmoidf_(a2);
 }
 
-// d_pre = d_rgb * rgb (1 - rgb);  dZ = (d_pre W) * [Y > 0];  d_b += d_pre.
-// One warp per row at a time: lane j owns hidden columns [8j, 8j + 8) (H <= 256)
-// and keeps its slice of W [3, H] in registers, so every row's activations and
-// gradients move as one coalesced 512-byte access.
-__global__ void __launch_bounds__(256) k_rgb_head_bwd(int64_t Ns, const __half* __restrict__ Y, int ldy, int H,
-                                                      const float* __restrict__ W, const float* __restrict__ rgbs,
-                                                      const float* __restrict__ d_rgbs, __half* __restrict__ d_pre,
-                                                      __half* __restrict__ dZ, __half* __restrict__ dZlo,
-                                                      float* __restrict__ d_b) {
+// d_pre = d_rgb * rgb (1 - rgb);  dZ = (d_pre W) * [Y > 0];  d_b += d_pre;  d_W += d_pre^T Y.
+// One warp per row at a time, the next row's loads issued before this row's work (two rows
+// in flight per warp): lane j owns hidden columns [8j, 8j + 8) (H <= 256), so every row's
+// activations and gradients move as coalesced 512-byte accesses; W [3, H] sits in shared
+// memory.  The head's weight gradient is accumulated per lane (3 x 8 registers) and added
+// once per warp.
+__device__ __forceinline__ void head_row_load(int64_t s, int64_t Ns, const __half* __restrict__ Y, int ldy, int c0,
+                                              bool act, const float* __restrict__ rgbs,
+                                              const float* __restrict__ d_rgbs, uint4& u, float* g) {
+    const bool live = s < Ns;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float r = live ? rgbs[3 * s + k] : 0.0f;
+        g[k] = live ? d_rgbs[3 * s + k] * r * (1.0f - r) : 0.0f;
+    }
+    u = (live && act) ? *reinterpret_cast<const uint4*>(Y + s * ldy + c0) : make_uint4(0, 0, 0, 0);
+}
+
+__global__ void __launch_bounds__(256, 3) k_rgb_head_bwd(int64_t Ns, const __half* __restrict__ Y, int ldy, int H,
+                                                         const float* __restrict__ W, const float* __restrict__ rgbs,
+                                                         const float* __restrict__ d_rgbs, __half* __restrict__ d_pre,
+                                                         __half* __restrict__ dZ, __half* __restrict__ dZlo,
+                                                         float* __restrict__ d_b, float* __restrict__ d_W) {
     const int lane = threadIdx.x & 31;
     const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int c0 = lane * 8;
     const bool act = c0 < H;
-    float wr[3][8];
+    __shared__ __align__(16) float w_s[3][256];
+    for (int i = threadIdx.x; i < 3 * 256; i += blockDim.x) {
+        const int k = i >> 8, c = i & 255;
+        w_s[k][c] = c < H ? W[k * H + c] : 0.0f;
+    }
+    __syncthreads();
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+    float dw[3][8];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int i = 0; i < 8; ++i) wr[k][i] = act ? W[k * H + c0 + i] : 0.0f;
-    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+        for (int i = 0; i < 8; ++i) dw[k][i] = 0.0f;
+    uint4 un;
+    float gn[3];
+    head_row_load(w0, Ns, Y, ldy, c0, act, rgbs, d_rgbs, un, gn);
     for (int64_t s = w0; s < Ns; s += nw) {
-        const float r0 = rgbs[3 * s], r1 = rgbs[3 * s + 1], r2 = rgbs[3 * s + 2];
-        const float g0 = d_rgbs[3 * s] * r0 * (1.0f - r0);
-        const float g1 = d_rgbs[3 * s + 1] * r1 * (1.0f - r1);
-        const float g2 = d_rgbs[3 * s + 2] * r2 * (1.0f - r2);
+        const uint4 u = un;
+        const float g0 = gn[0], g1 = gn[1], g2 = gn[2];
+        head_row_load(s + nw, Ns, Y, ldy, c0, act, rgbs, d_rgbs, un, gn);
         if (lane == 0) {
-            __half2 hp[4] = {__floats2half2_rn(g0, g1), __floats2half2_rn(g2, 0.f), __floats2half2_rn(0.f, 0.f),
-                             __floats2half2_rn(0.f, 0.f)};
-            *reinterpret_cast<uint4*>(d_pre + s * 8) = *reinterpret_cast<const uint4*>(hp);
+            if (d_pre) {
+                __half2 hp[4] = {__floats2half2_rn(g0, g1), __floats2half2_rn(g2, 0.f), __floats2half2_rn(0.f, 0.f),
+                                 __floats2half2_rn(0.f, 0.f)};
+                *reinterpret_cast<uint4*>(d_pre + s * 8) = *reinterpret_cast<const uint4*>(hp);
+            }
             s0 += g0;
             s1 += g1;
             s2 += g2;
         }
         if (act) {
-            const uint4 u = *reinterpret_cast<const uint4*>(Y + s * ldy + c0);
             const __half2* h = reinterpret_cast<const __half2*>(&u);
             __half2 o[4], ol[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 const float2 f = __half22float2(h[i]);
                 const int c = 2 * i;
-                const float v0 = f.x > 0.0f ? g0 * wr[0][c] + g1 * wr[1][c] + g2 * wr[2][c] : 0.0f;
-                const float v1 = f.y > 0.0f ? g0 * wr[0][c + 1] + g1 * wr[1][c + 1] + g2 * wr[2][c + 1] : 0.0f;
+                const float2 wa = *reinterpret_cast<const float2*>(&w_s[0][c0 + c]);
+                const float2 wb = *reinterpret_cast<const float2*>(&w_s[1][c0 + c]);
+                const float2 wc = *reinterpret_cast<const float2*>(&w_s[2][c0 + c]);
+                dw[0][c] = fmaf(g0, f.x, dw[0][c]);
+                dw[1][c] = fmaf(g1, f.x, dw[1][c]);
+                dw[2][c] = fmaf(g2, f.x, dw[2][c]);
+                dw[0][c + 1] = fmaf(g0, f.y, dw[0][c + 1]);
+                dw[1][c + 1] = fmaf(g1, f.y, dw[1][c + 1]);
+                dw[2][c + 1] = fmaf(g2, f.y, dw[2][c + 1]);
+                const float v0 = f.x > 0.0f ? g0 * wa.x + g1 * wb.x + g2 * wc.x : 0.0f;
+                const float v1 = f.y > 0.0f ? g0 * wa.y + g1 * wb.y + g2 * wc.y : 0.0f;
                 o[i] = __floats2half2_rn(v0, v1);
                 const float2 r = __half22float2(o[i]);
                 ol[i] = __floats2half2_rn(v0 - r.x, v1 - r.y);
@@ -340,6 +372,13 @@ __global__ void __launch_bounds__(256) k_rgb_head_bwd(int64_t Ns, const __half* 
         atomicAdd(d_b, s0);
         atomicAdd(d_b + 1, s1);
         atomicAdd(d_b + 2, s2);
+    }
+    if (d_W && act) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (dw[k][i] != 0.0f) atomicAdd(d_W + k * H + c0 + i, dw[k][i]);
     }
 }
 
@@ -414,16 +453,18 @@ extern "C" int gbsdf_rgb_head_fwd(int64_t Ns, const void* Y, int ldy, int H, con
 }
 
 extern "C" int gbsdf_rgb_head_bwd(int64_t Ns, const void* Y, int ldy, int H, const float* W, const float* rgbs,
-                                  const float* d_rgbs, void* d_pre, void* dZ, void* dZ_lo, float* d_b, void* stream) {
+                                  const float* d_rgbs, void* d_pre, void* dZ, void* dZ_lo, float* d_b, float* d_W,
+                                  void* stream) {
     clear_error();
     GBSDF_CHECK_ARG(Ns >= 0, "Ns < 0");
     if (Ns == 0) return GBSDF_OK;
-    GBSDF_CHECK_ARG(Y && W && rgbs && d_rgbs && d_pre && dZ && d_b, "NULL pointer");
+    GBSDF_CHECK_ARG(Y && W && rgbs && d_rgbs && dZ && d_b, "NULL pointer");
     GBSDF_CHECK_ARG(H % 8 == 0 && H <= 256 && H > 0, "hidden width %d", H);
-    GBSDF_CHECK_ARG(ldy % 8 == 0 && ldy >= H && aligned(Y, 16) && aligned(dZ, 16) && aligned(d_pre, 16), "layout");
+    GBSDF_CHECK_ARG(ldy % 8 == 0 && ldy >= H && aligned(Y, 16) && aligned(dZ, 16), "layout");
+    GBSDF_CHECK_ARG(!d_pre || aligned(d_pre, 16), "d_pre alignment");
     GBSDF_CHECK_ARG(!dZ_lo || aligned(dZ_lo, 16), "dZ_lo alignment");
     k_rgb_head_bwd<<<head_blocks(Ns), 256, 0, as_stream(stream)>>>(
-        Ns, (const __half*)Y, ldy, H, W, rgbs, d_rgbs, (__half*)d_pre, (__half*)dZ, (__half*)dZ_lo, d_b);
+        Ns, (const __half*)Y, ldy, H, W, rgbs, d_rgbs, (__half*)d_pre, (__half*)dZ, (__half*)dZ_lo, d_b, d_W);
     return launch_status("rgb_head_bwd");
 }
 

@@ -17,8 +17,8 @@ reports an overflow so a caller can skip the step and lower the scale
 
 Kernels per step (all on the current stream):
   field_fwd, dense x (1 + colour layers), rgb_head_fwd, render_fused,
-  rgb_head_bwd, dense x (colour layers + 2), app_grad, field_bwd, and the
-  weight-gradient GEMMs (cuBLAS, fp16 in / fp32 out).
+  rgb_head_bwd (with the colour head's weight gradient), dense x (colour layers + 2),
+  app_grad, field_bwd, and the weight gradients (tcgen05, fp16 in / fp32 out).
 """
 import ctypes
 
@@ -64,10 +64,11 @@ for _name in ("gbsdf_field_fwd", "gbsdf_field_bwd", "gbsdf_field_encode", "gbsdf
     _lib.register(_name, [c_vp, c_vp])
 _lib.register("gbsdf_render_fused", [c_vp, c_vp])
 _lib.register("gbsdf_rgb_head_fwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp])
-_lib.register("gbsdf_rgb_head_bwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp])
+_lib.register("gbsdf_rgb_head_bwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                     c_vp])
 _lib.register("gbsdf_app_grad", [c_i64, c_i32, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_vp])
 _lib.register("gbsdf_sdf_points", [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_f32, c_vp, c_vp])
-_lib.register("gbsdf_gemm_wgrad", [c_i64, c_i32, c_i32, c_vp, c_i32, c_vp, c_i32, c_vp, c_i32, c_f32, c_f32, c_vp])
+_lib.register("gbsdf_wgrad", [c_i64, c_i32, c_i32, c_vp, c_vp, c_i32, c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_vp])
 _lib.register("gbsdf_bg_encode", [c_i64, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_i32, c_i32, c_vp,
                                   c_vp, c_i32, c_i32, c_vp])
 _lib.register("gbsdf_bg_density", [c_i64, c_vp, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp])
@@ -94,17 +95,21 @@ def _round16(n):
 
 def _dense(X, Wt, N, K, out, bias=None, epi=EPI_IDENTITY, beta=100.0, G=None, err=None, X_lo=None, out_lo=None):
     """out[:, :N] = epi((X + X_lo)[:, :K] @ Wt[:N, :K].T + bias ; G) on the tcgen05 kernel."""
+    M = X.shape[0]
+    _lib.TIMER.count_bytes("gbsdf_dense", M * (K * 2 * (2 if X_lo is not None else 1) + (N * 2 if G is not None else 0)
+                                               + N * out.element_size() * (2 if out_lo is not None else 1)))
     _lib.call("gbsdf_dense", X.shape[0], K, N, c_vp(X.data_ptr()), c_vp(_p(X_lo)), X.stride(0),
               c_vp(Wt.data_ptr()), c_vp(_p(bias)), c_vp(_p(G)), G.stride(0) if G is not None else 0,
               c_vp(out.data_ptr()), c_vp(_p(out_lo)), out.stride(0), 1 if out.dtype == torch.float32 else 0,
               int(epi), float(beta), c_vp(_p(err)), _lib.stream_ptr(X.device))
 
 
-def _wgrad(dZ, X, N, K, dW, accumulate=False):
-    """dW[N, K] (+)= dZ[:, :N]^T X[:, :K] (fp32 out)."""
-    _lib.call("gbsdf_gemm_wgrad", dZ.shape[0], N, K, c_vp(dZ.data_ptr()), dZ.stride(0), c_vp(X.data_ptr()),
-              X.stride(0), c_vp(dW.data_ptr()), dW.stride(0), 1.0, 1.0 if accumulate else 0.0,
-              _lib.stream_ptr(dZ.device))
+def _wgrad(dZ, X, N, K, dW, accumulate=False, dZ_lo=None, err=None):
+    """dW[N, K] (+)= (dZ + dZ_lo)[:, :N]^T X[:, :K] (fp32 out) on the tcgen05 weight-gradient kernel."""
+    _lib.TIMER.count_bytes("gbsdf_wgrad", dZ.shape[0] * (N * 2 * (2 if dZ_lo is not None else 1) + K * 2))
+    _lib.call("gbsdf_wgrad", dZ.shape[0], N, K, c_vp(dZ.data_ptr()), c_vp(_p(dZ_lo)), dZ.stride(0),
+              c_vp(X.data_ptr()), X.stride(0), c_vp(dW.data_ptr()), dW.stride(0), 1 if accumulate else 0,
+              c_vp(_p(err)), _lib.stream_ptr(dZ.device))
 
 
 def pack_sdf(sdf):
@@ -328,7 +333,7 @@ class FusedField:
                   rgbs=e(Ns, 3), rgb=e(R, 3),
                   weights=e(Ns), d_rgbs=e(Ns, 3), d_sdf=e(Ns), d_grad=e(Ns, 3), d_hess=e(Ns, 3),
                   loss_sums=torch.zeros(4, device=device, dtype=torch.float64), d_s_var=torch.zeros(1, device=device),
-                  d_pre_last=e(Ns, 8, dt=f16), dzs=[e(Ns, Hc, dt=f16) for _ in range(2)],
+                  d_wl=torch.zeros(3, Hc, device=device), dzs=[e(Ns, Hc, dt=f16) for _ in range(2)],
                   dzs_lo=[e(Ns, Hc, dt=f16) for _ in range(2)] if self.split else None,
                   dzfeat=e(Ns, 256, dt=f16), dzfeat_lo=e(Ns, 256, dt=f16) if self.split else None,
                   dxc_tail=e(Ns, 64), d_h0c=e(Ns, 256),
@@ -353,8 +358,7 @@ class FusedField:
                       bg_h={i: self._with_ones(e(Nb, 264, dt=f16), 256) for i in (1, 2, 3, 5, 6, 7)},
                       bg_G=e(Nb, self.Kr0, dt=f16), bg_hr=self._with_ones(e(Nb, Hbr + 8, dt=f16), Hbr),
                       bg_sigma=e(Nb), bg_rgbs=e(Nb, 3), bg_weights=e(Nb), bg_d_rgbs=e(Nb, 3),
-                      bg_dZ7=torch.zeros(Nb, 272, device=device, dtype=f16),
-                      bg_d_pre_last=e(Nb, 8, dt=f16), bg_dz_r=e(Nb, Hbr, dt=f16),
+                      bg_dZ7=torch.zeros(Nb, 272, device=device, dtype=f16), bg_dz_r=e(Nb, Hbr, dt=f16),
                       bg_dz=[e(Nb, 256, dt=f16) for _ in range(2)],
                       bg_d_tail=e(Nb, 64) if self.app_dim else None, bg_d_bl=torch.zeros(3, device=device))
             if self.pairs:
@@ -463,6 +467,7 @@ class FusedField:
                    out_lo=Yl)
             X, Xl, K = ws['ys'][i], Yl, Hc
         ylast = ws['ys'][-1]
+        _lib.TIMER.count_bytes("gbsdf_rgb_head_fwd", Ns * (Hc * 2 + 12))
         _lib.call("gbsdf_rgb_head_fwd", Ns, c_vp(ylast.data_ptr()), ylast.stride(0), Hc, c_vp(pk['wl'].data_ptr()),
                   c_vp(pk['bl'].data_ptr()), c_vp(ws['rgbs'].data_ptr()), stream)
         dists_bg = None
@@ -509,23 +514,24 @@ class FusedField:
         _lib.call("gbsdf_render_fused", ctypes.byref(ra), stream)
         # ---------------- colour MLP backward ----------------
         ws['d_bl'].zero_()
+        ws['d_wl'].zero_()
         dz = ws['dzs'][0]
+        # Y row in, dZ row (and its lo half) out, the per-sample colour and its gradient
+        _lib.TIMER.count_bytes("gbsdf_rgb_head_bwd", Ns * (Hc * 2 * (3 if self.split else 2) + 24))
         _lib.call("gbsdf_rgb_head_bwd", Ns, c_vp(ylast.data_ptr()), ylast.stride(0), Hc, c_vp(pk['wl'].data_ptr()),
-                  c_vp(ws['rgbs'].data_ptr()), c_vp(ws['d_rgbs'].data_ptr()), c_vp(ws['d_pre_last'].data_ptr()),
+                  c_vp(ws['rgbs'].data_ptr()), c_vp(ws['d_rgbs'].data_ptr()), None,
                   c_vp(dz.data_ptr()), c_vp(_p(ws['dzs_lo'][0] if self.split else None)), c_vp(ws['d_bl'].data_ptr()),
-                  stream)
+                  c_vp(ws['d_wl'].data_ptr()), stream)
         grads = {}
         dev32 = dict(device=dev, dtype=torch.float32)
         n = self.n_rgb_hidden
-        # last colour layer weight gradient
-        gl = torch.empty(3, Hc, **dev32)
-        _wgrad(ws['d_pre_last'], ylast, 3, Hc, gl)
-        grads['wl'], grads['bl'] = gl, ws['d_bl']
+        # the last colour layer's weight gradient came with its backward
+        grads['wl'], grads['bl'] = ws['d_wl'], ws['d_bl']
         cur = 0
         for i in range(n - 1, 0, -1):
             dzi = ws['dzs'][cur]
             gw = torch.empty(Hc, Hc + 8, **dev32)
-            _wgrad(dzi, ws['ys'][i - 1], Hc, Hc + 8, gw)          # column Hc: the bias gradient
+            _wgrad(dzi, ws['ys'][i - 1], Hc, Hc + 8, gw, err=ws['err'])   # column Hc: the bias gradient
             grads[f'wc{i}'], grads[f'bc{i}'] = gw[:, :Hc], gw[:, Hc]
             nxt = ws['dzs'][1 - cur]
             _dense(dzi, pk['wcT'][i], Hc, Hc, nxt, epi=EPI_DRELU, G=ws['ys'][i - 1], err=ws['err'],
@@ -535,7 +541,7 @@ class FusedField:
         dz0 = ws['dzs'][cur]
         dz0_lo = ws['dzs_lo'][cur] if self.split else None
         gw0 = torch.empty(Hc, self.Kc0, **dev32)
-        _wgrad(dz0, ws['xc'], Hc, self.Kc0, gw0)               # last column: the bias gradient
+        _wgrad(dz0, ws['xc'], Hc, self.Kc0, gw0, err=ws['err'])   # last column: the bias gradient
         grads['wc0'], grads['bc0'] = gw0, gw0[:, self.Kc0 - 1]
         # input gradient of colour layer 0: feature part through softplus', tail (x, SH, n, app) as is
         _dense(dz0, pk['wc0T_feat'], 256, Hc, ws['dzfeat'], epi=EPI_DSOFTPLUS, beta=fa.beta, G=ws['xc'],
@@ -543,7 +549,7 @@ class FusedField:
         _dense(dz0, pk['wc0T_tail'], 64, Hc, ws['dxc_tail'], epi=EPI_IDENTITY, err=ws['err'], X_lo=dz0_lo)
         # SDF feature layer
         gw1 = torch.empty(256, 264, **dev32)
-        _wgrad(ws['dzfeat'], ws['h0c'], 256, 264, gw1)             # column 256: the bias gradient
+        _wgrad(ws['dzfeat'], ws['h0c'], 256, 264, gw1, err=ws['err'])   # column 256: the bias gradient
         grads['w1'], grads['b1'] = gw1[:, :256], gw1[:, 256]
         _dense(ws['dzfeat'], pk['w1T'], 256, 256, ws['d_h0c'], epi=EPI_IDENTITY, err=ws['err'],
                X_lo=ws['dzfeat_lo'] if self.split else None)
@@ -581,9 +587,8 @@ class FusedField:
             grads['w0ext'] = ws['d_w0']                               # [256, K0 + 16], lo folded in
         else:
             gw0x = torch.empty(256, 2 * self.K0 + 16, **dev32)
-            _wgrad(ws['d_pre0'], ws['x0ext'], 256, 2 * self.K0 + 16, gw0x)
-            # d_pre's lo half against the hi features and the position/bias tail
-            _wgrad(ws['d_pre0_lo'], ws['x0ext'], 256, self.K0 + 16, gw0x, accumulate=True)
+            # d_pre as its hi + lo pair against every x0ext column (features hi, tail, features lo)
+            _wgrad(ws['d_pre0'], ws['x0ext'], 256, 2 * self.K0 + 16, gw0x, dZ_lo=ws['d_pre0_lo'], err=ws['err'])
             grads['w0ext'] = gw0x
         grads['table'] = d_table
         if self.bg:
@@ -644,15 +649,14 @@ class FusedField:
         err = ws['err']
         g = {}
         ws['bg_d_bl'].zero_()
+        g['r1'] = torch.zeros(3, Hbr, **dev32)
         dzr_lo, dZ7_lo, dz_lo = ws['bg_dz_r_lo'], ws['bg_dZ7_lo'], ws['bg_dz_lo']
         _lib.call("gbsdf_rgb_head_bwd", Nb, c_vp(hr.data_ptr()), hr.stride(0), Hbr, c_vp(pk['bwr1'].data_ptr()),
-                  c_vp(ws['bg_rgbs'].data_ptr()), c_vp(ws['bg_d_rgbs'].data_ptr()),
-                  c_vp(ws['bg_d_pre_last'].data_ptr()), c_vp(ws['bg_dz_r'].data_ptr()), c_vp(_p(dzr_lo)),
-                  c_vp(ws['bg_d_bl'].data_ptr()), stream)
-        g['r1'] = torch.empty(3, Hbr, **dev32)
-        _wgrad(ws['bg_d_pre_last'], hr, 3, Hbr, g['r1'])
+                  c_vp(ws['bg_rgbs'].data_ptr()), c_vp(ws['bg_d_rgbs'].data_ptr()), None,
+                  c_vp(ws['bg_dz_r'].data_ptr()), c_vp(_p(dzr_lo)), c_vp(ws['bg_d_bl'].data_ptr()),
+                  c_vp(g['r1'].data_ptr()), stream)
         g['r0'] = torch.empty(Hbr, Kr0, **dev32)
-        _wgrad(ws['bg_dz_r'], G, Hbr, Kr0, g['r0'])                                 # bias column 256 + 16 + app
+        _wgrad(ws['bg_dz_r'], G, Hbr, Kr0, g['r0'], err=err)                        # bias column 256 + 16 + app
         _dense(ws['bg_dz_r'], pk['bwr0T_feat'], 256, Hbr, dZ7, epi=EPI_DRELU, G=G, err=err,   # d feature pre-act
                X_lo=dzr_lo, out_lo=dZ7_lo)
         if self.app_dim:
@@ -662,19 +666,19 @@ class FusedField:
             _lib.call("gbsdf_app_grad", R, self.n_bg, None, c_vp(app_idx.data_ptr()),
                       c_vp(ws['bg_d_tail'].data_ptr()), 64, 16, self.app_dim, c_vp(g['app'].data_ptr()), stream)
         g[7] = torch.empty(272, 264, **dev32)
-        _wgrad(dZ7, h[7], 272, 264, g[7])
+        _wgrad(dZ7, h[7], 272, 264, g[7], err=err)
         _dense(dZ7, pk['bw7extT'], 256, 272, dz[0], epi=EPI_DRELU, G=h[7], err=err,       # dZ6
                X_lo=dZ7_lo, out_lo=dz_lo[0])
         cur = 0
         for i, gate in ((6, h[6]), (5, h[5]), (4, S), (3, h[3]), (2, h[2]), (1, h[1])):
             X = S if i == 4 else h[i]
             g[i] = torch.empty(256, X.shape[1], **dev32)
-            _wgrad(dz[cur], X, 256, X.shape[1], g[i])
+            _wgrad(dz[cur], X, 256, X.shape[1], g[i], err=err)
             _dense(dz[cur], pk['bwT'][i], 256, 256, dz[1 - cur], epi=EPI_DRELU, G=gate, err=err,
                    X_lo=dz_lo[cur], out_lo=dz_lo[1 - cur] if i > 1 else None)
             cur = 1 - cur
         g[0] = torch.empty(256, BG_X_COLS, **dev32)
-        _wgrad(dz[cur], S[:, 256:], 256, BG_X_COLS, g[0])
+        _wgrad(dz[cur], S[:, 256:], 256, BG_X_COLS, g[0], err=err)
         return g
 
     def losses(self):
