@@ -242,8 +242,17 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index=0):
-        self.index = index
+    def __init__(self, device=0):
+        # nvidia-smi numbers GPUs physically: query by UUID so a CUDA_VISIBLE_DEVICES
+        # remapping still samples the GPU this process runs on
+        self.index = str(device)
+        try:
+            import torch
+            uuid = str(torch.cuda.get_device_properties(device).uuid)
+            if uuid:
+                self.index = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+        except Exception:                      # noqa: BLE001 (no CUDA or no uuid: fall back to the ordinal)
+            pass
         self.proc = None
         self.path = os.path.join(tempfile.gettempdir(), f"gbsdf_clocks_{os.getpid()}.csv")
 
@@ -251,7 +260,7 @@ class ClockSampler:
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", self.index, "--query-gpu=" + self.FIELDS,
                                           "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):

@@ -284,7 +284,10 @@ def extract_mesh(sdf_func, bounds, intv, block_res=64, texture_func=None, filter
                 V, F = mc(vol, origin, intv)
                 if V.shape[0] == 0:
                     continue
-                if merge_vertices:
+                if merge_vertices or filter_lcc:
+                    # the reference's trimesh.Trimesh(V, F) merges equal vertices before split():
+                    # without the weld, vertices that several edges emit at an exact-zero lattice
+                    # value would cut face adjacency and could change the component kept
                     V, F = finalize_mesh(V, F, weld=True, min_side=-1.0)
                 Vb, Fb = V.cpu().numpy(), F.cpu().numpy()
                 Cb = np.asarray(texture_func(Vb), np.uint8).reshape(-1, 3) if texture_func is not None else None
