@@ -50,22 +50,26 @@ def parse():
 # --------------------------------------------------------------------------- ncu-measured traffic
 
 def profiled_traffic(kernel):
-    """DRAM bytes per sample of a C-ABI call's kernels from the committed ncu summaries
-    (a line 'roofline-traffic <call> bytes_per_sample=<v> source=<capture>' in profiles/*.md),
-    or (None, None).  bench.py cannot run ncu itself; the figure comes from one capture of
-    the same kernels on a smaller case, scaled by the samples processed."""
-    import glob
-    import re
-    for f in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
-        for line in open(f):
-            m = re.match(r"\s*roofline-traffic\s+(\S+)\s+bytes_per_sample=([0-9.eE+-]+)\s+source=(.*)", line)
-            if m and m.group(1) == kernel:
-                return float(m.group(2)), os.path.basename(f) + ": " + m.group(3).strip()
-    return None, None
+    """(DRAM bytes per sample, source, L2 throughput % or None) of a C-ABI call's kernel from
+    measured_traffic.json, or (None, None, None).  bench.py cannot run ncu itself: the figures
+    come from one ncu capture of the same kernels on a smaller case of the same field,
+    scaled by the samples a step processes."""
+    try:
+        data = json.load(open(os.path.join(ROOT, "measured_traffic.json")))
+    except (OSError, ValueError):
+        return None, None, None
+    c = data.get("calls", {}).get(kernel)
+    if not c:
+        return None, None, None
+    return float(c["dram_bytes_per_sample"]), f"{c.get('kernel', kernel)}: {c['source']}", c.get("l2_throughput_pct")
 
 
 # kernels of this library launched by one call of each entry point (cuBLAS excluded)
-KERNELS_PER_CALL = {"gbsdf_field_fwd": 2, "gbsdf_field_bwd": 2, "gbsdf_gemm_wgrad": 0}   # others: 1
+KERNELS_PER_CALL = {"gbsdf_field_fwd": 2, "gbsdf_field_bwd": 2}   # others: 1
+
+
+# calls whose algorithmic bytes count every table-corner touch (mostly served by L2)
+GATHER_SCATTER = ("gbsdf_field_encode", "gbsdf_field_scatter")
 
 
 # --------------------------------------------------------------------------- extra workloads
@@ -188,9 +192,11 @@ def bench_mesh(model, device, res=512, block_res=128):
 
 # --------------------------------------------------------------------------- CPU baseline
 
-def cpu_port_sample(rays=64, samples=N_SAMPLES, steps=1, warmup=1):
-    """Time the CPU restatement of the reference path (oracle, float32 torch on the
-    host cores + numpy hash grid) on a bounded sample of the same workload."""
+def cpu_port_sample(rays=64, samples=N_SAMPLES, steps=5, warmup=2):
+    """The reference's path on the host cores: the oracle's float32 restatement of the
+    reference modules (pinned to them by golden vectors; the reference itself is not on
+    the GPU machine and its encoder is a CUDA-only third-party package) on a bounded sample of
+    the full-field workload, all host threads, `warmup` untimed steps, median of `steps`."""
     import torch
     from oracle import field as of
     from neuralangelo_gb300.workloads import full_field_iteration, make_rays
@@ -215,23 +221,34 @@ def cpu_port_sample(rays=64, samples=N_SAMPLES, steps=1, warmup=1):
             v.grad = None
     t = statistics.median(times)
     return dict(value=rays * samples / t, unit="samples/s", cores=threads, kind="port",
-                sample=f"{rays} rays x {samples} samples of the same field, float32, oracle restatement "
-                       f"(torch CPU + numpy hash grid), median of {steps} after {warmup} warm-up",
-                seconds_per_step=t)
+                sample=f"{rays} rays x {samples} samples of the full field (L16 F8 T2^22, 8 active), float32, "
+                       f"oracle restatement of the reference modules (torch CPU + numpy hash grid), "
+                       f"median of {steps} after {warmup} warm-up",
+                seconds_per_step=t, mean_seconds_per_step=sum(times) / len(times))
+
+
+REF_RAYS = 32          # rays per reference-arm step (a bounded sample of the 16384-ray workload)
 
 
 def run_reference(args):
+    """The reference arm: the reference's path on the host cores (the oracle's restatement,
+    see cpu_port_sample), --warmup untimed and --steps timed steps, each a bounded sample of
+    REF_RAYS rays x 128 samples of the full-field workload.  Under torchrun only rank 0 runs."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    cb = cpu_port_sample(steps=max(1, min(args.steps, 3)), warmup=1)
-    line = dict(metric=METRIC, value=cb["value"], unit="samples/s", n_gpus=args.gpus, steps=args.steps,
-                warmup=args.warmup, ms_per_step=cb["seconds_per_step"] * 1e3, higher_is_better=True,
+    steps, warmup = max(1, args.steps), max(0, args.warmup)
+    cb = cpu_port_sample(rays=REF_RAYS, steps=steps, warmup=warmup)
+    value = REF_RAYS * N_SAMPLES / cb["mean_seconds_per_step"]
+    cb_line = dict(value=round(value, 1), unit="samples/s", cores=cb["cores"], kind=cb["kind"], sample=cb["sample"])
+    line = dict(metric=METRIC, value=round(value, 1), unit="samples/s", n_gpus=args.gpus, steps=steps,
+                warmup=warmup, ms_per_step=round(cb["mean_seconds_per_step"] * 1e3, 3), higher_is_better=True,
                 scaling="weak", vs_baseline=None, dtype="f32", data="synthetic",
-                config=dict(workload="full field, 16384 rays x 128 samples (CPU sample: 64 rays)",
-                            parallelism="host cores"),
-                impl="reference", cpu_baseline=cb,
-                e2e=dict(value=cb["value"], unit="samples/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+                config=dict(workload=f"full field L16 F8 T2^22 (8 active), 16384 rays x 128 samples; "
+                                     f"each step a {REF_RAYS}-ray sample on the host cores",
+                            rays_per_step=REF_RAYS, samples_per_ray=N_SAMPLES, parallelism="host cores"),
+                impl="reference", cpu_baseline=cb_line,
+                e2e=dict(value=round(value, 1), unit="samples/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
     print(json.dumps(line), flush=True)
 
 
@@ -391,17 +408,27 @@ def main():
         torch.cuda.synchronize()
         return ms_, _lib.TIMER.summary()
 
-    # the plain FP32 drop-in (the denominator of the fused speed-up)
-    plain_ms = float("nan")
+    # the plain FP32 drop-in (the denominator of the fused speed-up): torch's default FP32
+    # matmuls, and the same with TF32 tensor-core matmuls, as the reference's trainer sets by
+    # default (imaginaire/trainers/base.py:172-175)
+    plain_ms = plain_tf32_ms = float("nan")
     if not args.no_plain or fused is None:
+        tf32 = (torch.backends.cuda.matmul.allow_tf32, torch.backends.cudnn.allow_tf32)
+        torch.backends.cuda.matmul.allow_tf32 = torch.backends.cudnn.allow_tf32 = False
         plain_ms, plain_k = measure(lambda: step_plain(model, batch), max(2, args.steps // 2), args.warmup)
         plain_ms = max_over_ranks(plain_ms)
+        if fused is not None:
+            torch.backends.cuda.matmul.allow_tf32 = torch.backends.cudnn.allow_tf32 = True
+            plain_tf32_ms, _ = measure(lambda: step_plain(model, batch), max(2, args.steps // 2), args.warmup)
+            plain_tf32_ms = max_over_ranks(plain_tf32_ms)
+        torch.backends.cuda.matmul.allow_tf32, torch.backends.cudnn.allow_tf32 = tf32
     cap = None
     if fused is not None:
         # per-call device times (CUDA events around every C-ABI call) from eager steps;
         # the headline then times the same step launched as one CUDA graph (CapturedStep)
         ksteps = max(3, args.steps // 2)
         _, ksum = measure(lambda: step_fused(batch), ksteps, args.warmup)
+        kbytes = dict(_lib.TIMER.bytes)
         from neuralangelo_gb300.fused import CapturedStep
         cap = CapturedStep(fused, batch)
     clocks = ClockSampler(local)
@@ -410,6 +437,7 @@ def main():
         ms = time_steps(cap.replay, args.steps, args.warmup, barrier)
     else:
         ms, ksum = measure(lambda: step_plain(model, batch), args.steps, args.warmup)
+        kbytes = dict(_lib.TIMER.bytes)
         ksteps = args.steps
     clock = clocks.stop()
     ms = max_over_ranks(ms)
@@ -435,13 +463,14 @@ def main():
     K0 = 16 * ((A * F + 15) // 16)
     KX = 2 * K0 + 16                                     # x0ext row: features hi | tail | lo
     enc_read = A * 8 * F * (2 if mode == "fused" else 4)
+    pair = 2 if (fused is not None and fused.pairs) else 1     # h0c and colour-tail rows as hi + lo
     work = {
         "gbsdf_hashgrid_fwd": (n_samples * (A * 8 * F * 4 + 16 * F * 4 + 12), 0),
         "gbsdf_hashgrid_bwd": (n_samples * (A * 8 * F * 8 + 16 * F * 4), 0),
         # table corners of 7 evaluations -> x0ext rows
         "gbsdf_field_encode": (n_samples * (7 * enc_read + 7 * KX * 2 + 4), 0),
         # x0ext rows -> SDF, gradient, Hessian, h0c row, colour-input tail
-        "gbsdf_field_mlp_fwd": (n_samples * (7 * KX * 2 + 4 + 12 + 12 + (H + 8) * 2 + 48 * 2),
+        "gbsdf_field_mlp_fwd": (n_samples * (7 * KX * 2 + 4 + 12 + 12 + ((H + 8) * 2 + 48 * 2) * pair),
                                 n_samples * 7 * 2 * H * (K0 + 4 + 1)),
         # x0ext rows, d_h0c and the per-sample output gradients -> d_enc (fp32) and, K0 <= 64,
         # the layer-0 weight gradient in-kernel (extra MACs, no traffic), else d_pre0 (fp16)
@@ -450,6 +479,12 @@ def main():
         # d_enc -> FP32 read-modify-write of every corner touch
         "gbsdf_field_scatter": (n_samples * (7 * K0 * 4 + 7 * A * 8 * F * 8 + 4), 0),
     }
+    # the dense layers, weight gradients and colour head: their algorithmic bytes as each call
+    # reported them (fused.py: operand and output rows, hi + lo halves counted); their tensor
+    # work is far below their HBM floor
+    for name in ("gbsdf_dense", "gbsdf_wgrad", "gbsdf_rgb_head_fwd", "gbsdf_rgb_head_bwd"):
+        if name in kbytes and name in ksum:
+            work[name] = (kbytes[name] / ksum[name][0], 0)
     tensor_peak = peaks.get("bf16_tflops_sustained", 1700.0)
 
     def roofline_of(name, calls, tot_ms):
@@ -468,8 +503,15 @@ def main():
             r = dict(kernel=name, bound="hbm", achieved=round(by / t / 1e9, 1), peak=hbm_peak, unit="GB/s",
                      frac=round(by / t / 1e9 / hbm_peak, 4),
                      peak_source="MEASURED_PEAKS.json hbm_gbs (burst, of measured)")
-        tps, tsrc = profiled_traffic(name)
-        traffic = round(tps * n_samples) if tps is not None else None
+        tps, tsrc, l2pct = profiled_traffic(name)           # DRAM bytes per sample over a step's launches
+        traffic = round(tps * n_samples * ksteps / calls) if tps is not None else None
+        if name in GATHER_SCATTER and traffic:
+            # gather and scatter touch every table corner of 7 evaluations; L2 serves most of those
+            # touches (coarse levels, taps of one sample), so their HBM position is the measured DRAM
+            # traffic over the time, and the per-touch rate is reported beside it
+            r.update(achieved=round(traffic / t / 1e9, 1), frac=round(traffic / t / 1e9 / hbm_peak, 4),
+                     touch_gbs=round(by / t / 1e9, 1), l2_throughput_pct=l2pct,
+                     basis="measured DRAM bytes (ncu) per launch")
         r.update(traffic=traffic, traffic_source=tsrc,
                  dram_gbs=round(traffic / t / 1e9, 1) if traffic else None,
                  per_launch_ms=round(per_launch_ms, 4), algorithmic_bytes_per_launch=by, flops_per_launch=fl,
@@ -481,7 +523,8 @@ def main():
     roof = roofline_of(dom[0], *dom[1]) if dom else None
     # the same for every timed field kernel (the dominant one is `roofline`)
     rooflines = {k: {x: y for x, y in roofline_of(k, *v).items()
-                     if x in ("bound", "achieved", "unit", "frac", "per_launch_ms", "dram_gbs")}
+                     if x in ("bound", "achieved", "unit", "frac", "per_launch_ms", "dram_gbs", "touch_gbs",
+                              "l2_throughput_pct", "basis", "launches_per_step")}
                  for k, v in timed}
     launches = int(sum(c * KERNELS_PER_CALL.get(k, 1) for k, (c, _) in ksum.items()) / ksteps)
     extras = {}
@@ -498,6 +541,7 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_port_sample()
         cb.pop("seconds_per_step", None)
+        cb.pop("mean_seconds_per_step", None)
     if rank == 0:
         line = dict(metric=METRIC, value=round(value, 1), unit="samples/s", n_gpus=world, steps=args.steps,
                     warmup=args.warmup, ms_per_step=round(ms, 3), higher_is_better=True, scaling="weak",
@@ -505,6 +549,11 @@ def main():
                     plain_fp32=(dict(value=round(world * n_samples / (plain_ms * 1e-3), 1), unit="samples/s",
                                      ms_per_step=round(plain_ms, 3)) if plain_ms == plain_ms else None),
                     speedup_vs_plain=round(plain_ms / ms, 3) if plain_ms == plain_ms else None,
+                    plain_tf32=(dict(value=round(world * n_samples / (plain_tf32_ms * 1e-3), 1), unit="samples/s",
+                                     ms_per_step=round(plain_tf32_ms, 3),
+                                     note="plain drop-in with TF32 tensor-core matmuls (the reference "
+                                          "trainer's default)") if plain_tf32_ms == plain_tf32_ms else None),
+                    speedup_vs_plain_tf32=round(plain_tf32_ms / ms, 3) if plain_tf32_ms == plain_tf32_ms else None,
                     config=dict(workload=f"full field L16 F8 T2^22 (8 active), {R} rays x {N} samples, mode={mode}",
                                 rays=R, samples_per_ray=N, active_levels=ACTIVE, mode=mode,
                                 split_colour_grads=bool(args.split_colour_grads),
