@@ -207,6 +207,10 @@ typedef struct gbsdf_field_args {
                                 (>= 256) the forward writes; 0 in the constant-1 column (NULL: not written) */
     void* d_pre0_lo;         /* optional fp16 [126 T, 256]: d_pre0's low half (backward without d_w0; the
                                 layer-0 weight gradient is d_pre0^T x0ext + d_pre0_lo^T [x hi | tail]) */
+    const float* d_table_scale_dev;  /* optional device scalar used in place of d_table_scale (e.g. the
+                                        inverse of a loss scale the device updates) */
+    float* found_inf;        /* optional: the scatter sets *found_inf = 1 when it reads a non-finite d_enc
+                                value (the table gradient would be non-finite) */
 } gbsdf_field_args;
 
 size_t gbsdf_field_args_size(void);
@@ -278,6 +282,10 @@ typedef struct gbsdf_render_args {
     float* out_opacity;          /* [R]    sum of the object samples' weights */
     float* out_gradient;         /* [R, 3] sum of the object samples' weights x (unnormalised) gradient */
     float* out_dist;             /* [R]    sum of weights x distance over object and background samples */
+    /* Optional device scalars read in place of the host fields above (NULL: the host fields):
+     * dyn[0] loss_scale, dyn[1] anneal, dyn[2] w_curv.  A captured CUDA graph then follows a
+     * loss scale that the device updates and a schedule that the host refreshes between replays. */
+    const float* dyn;
 } gbsdf_render_args;
 
 size_t gbsdf_render_args_size(void);

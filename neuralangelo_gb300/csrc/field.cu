@@ -237,7 +237,8 @@ __global__ void __launch_bounds__(256, CPT >= 8 ? 2 : (CPT == 4 ? 3 : 4)) k_fiel
     sample_point(p, s, c);
     const LevelDesc d = level_desc(p.grid, l);
     float* base = p.d_table + d.offset * F;
-    const float gscale = p.d_table_scale != 0.0f ? p.d_table_scale : 1.0f;
+    const float gscale = p.d_table_scale_dev ? *p.d_table_scale_dev : (p.d_table_scale != 0.0f ? p.d_table_scale : 1.0f);
+    bool nonfinite = false;
     const int lane = threadIdx.x & 31;
     // Final flush.  With 8 active levels the lanes l, l + 8, l + 16, l + 24 of a warp hold
     // level l of four consecutive samples, which at coarse levels often end in the same
@@ -279,6 +280,10 @@ __global__ void __launch_bounds__(256, CPT >= 8 ? 2 : (CPT == 4 ? 3 : 4)) k_fiel
 #pragma unroll
                 for (int f = 0; f < F; ++f) g[f] = __ldg(dv + f);
             }
+            if (c0 == 0) {
+#pragma unroll
+                for (int f = 0; f < F; ++f) nonfinite |= !isfinite(g[f]);
+            }
 #pragma unroll
             for (int cc = 0; cc < CPT; ++cc) {
                 const int corner = c0 + cc;
@@ -319,6 +324,7 @@ __global__ void __launch_bounds__(256, CPT >= 8 ? 2 : (CPT == 4 ? 3 : 4)) k_fiel
             if (mine) scatter_add<F>(base + (uint64_t)pidx[cc] * F, pacc[cc]);
         }
     }
+    if (nonfinite && p.found_inf) *p.found_inf = 1.0f;     // any writer stores the same value
 }
 
 // ---------------------------------------------------------------------------

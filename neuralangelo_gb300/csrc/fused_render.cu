@@ -37,6 +37,10 @@ __global__ void __launch_bounds__(RENDER_WARPS * 32) k_render_fused(gbsdf_render
     const int n = (int)(end - beg);
     const int nb = p.n_bg;                     // background samples follow the object samples
     const int ntot = n + nb;
+    // the loss scale, anneal ratio and curvature weight: device scalars when given
+    const float loss_scale = p.dyn ? p.dyn[0] : p.loss_scale;
+    const float anneal = p.dyn ? p.dyn[1] : p.anneal;
+    const float w_curv = p.dyn ? p.dyn[2] : p.w_curv;
     if (ntot > MAX_RAY_SAMPLES) {   // longer rays do not fit the per-warp buffers: report, skip
         if (lane == 0 && p.err) atomicCAS(p.err, 0, 2);
         return;
@@ -69,7 +73,7 @@ __global__ void __launch_bounds__(RENDER_WARPS * 32) k_render_fused(gbsdf_render
             const float cosv = rx * gx + ry * gy + rz * gz;
             const float dnext = (k + 1 < n) ? p.dists[s + 1] : far;
             const float intv = dnext - p.dists[s];
-            const float ic = iter_cos_f(cosv, p.anneal);
+            const float ic = iter_cos_f(cosv, anneal);
             const float sdf = p.sdf[s];
             const float P = 1.0f / (1.0f + expf(-(sdf - ic * intv * 0.5f) * inv_s));
             const float Q = 1.0f / (1.0f + expf(-(sdf + ic * intv * 0.5f) * inv_s));
@@ -160,10 +164,10 @@ __global__ void __launch_bounds__(RENDER_WARPS * 32) k_render_fused(gbsdf_render
     }
     __syncwarp();
     // d L / d rgb (L1Loss mean x 3, loss-scaled)
-    const float gsc = p.loss_scale * p.w_render * p.l1_scale;
+    const float gsc = loss_scale * p.w_render * p.l1_scale;
     const float dr0 = gsc * signf_(c0 - t0), dr1 = gsc * signf_(c1 - t1), dr2 = gsc * signf_(c2 - t2);
-    const float eik_c = p.loss_scale * p.w_eik * p.mean_scale * 2.0f;
-    const float curv_c = p.loss_scale * p.w_curv * p.mean_scale;
+    const float eik_c = loss_scale * p.w_eik * p.mean_scale * 2.0f;
+    const float curv_c = loss_scale * w_curv * p.mean_scale;
 
     // ---------------- backward (reverse chunks) ----------------
     float Snext = 0.0f;    // S of the first sample after the current chunk
@@ -216,7 +220,7 @@ __global__ void __launch_bounds__(RENDER_WARPS * 32) k_render_fused(gbsdf_render
             const float cosv = rx * gx + ry * gy + rz * gz;
             const float dnext = (k + 1 < n) ? p.dists[s + 1] : far;
             const float intv = dnext - p.dists[s];
-            const float ic = iter_cos_f(cosv, p.anneal);
+            const float ic = iter_cos_f(cosv, anneal);
             const float sdf = p.sdf[s];
             const float ep = sdf - ic * intv * 0.5f, en = sdf + ic * intv * 0.5f;
             const float P = 1.0f / (1.0f + expf(-ep * inv_s));
@@ -229,7 +233,7 @@ __global__ void __launch_bounds__(RENDER_WARPS * 32) k_render_fused(gbsdf_render
             const float dep = dP * P * (1.0f - P), den_ = dQ * Q * (1.0f - Q);
             ds_acc += (dep * ep + den_ * en) * inv_s;
             const float d_sdf = (dep + den_) * inv_s;
-            const float d_cos = (den_ - dep) * inv_s * intv * 0.5f * iter_cos_g(cosv, p.anneal);
+            const float d_cos = (den_ - dep) * inv_s * intv * 0.5f * iter_cos_g(cosv, anneal);
             float dgx = d_cos * rx, dgy = d_cos * ry, dgz = d_cos * rz;
             float dh = 0.0f;
             if (inside) {
@@ -289,8 +293,10 @@ __global__ void k_rgb_head_fwd(int64_t Ns, const __half* __restrict__ Y, int ldy
 // One warp per row at a time, the next row's loads issued before this row's work (two rows
 // in flight per warp): lane j owns hidden columns [8j, 8j + 8) (H <= 256), so every row's
 // activations and gradients move as coalesced 512-byte accesses; W [3, H] sits in shared
-// memory.  The head's weight gradient is accumulated per lane (3 x 8 registers) and added
-// once per warp.
+// memory.  The head's weight gradient is accumulated per lane (3 x 8 registers), summed over
+// the block in shared memory and added to d_W once per block (the grid holds only as many
+// blocks as are resident, so each of the 3 x H addresses takes one atomic per block).
+constexpr int HEAD_BWD_BLOCKS_PER_SM = 3;
 __device__ __forceinline__ void head_row_load(int64_t s, int64_t Ns, const __half* __restrict__ Y, int ldy, int c0,
                                               bool act, const float* __restrict__ rgbs,
                                               const float* __restrict__ d_rgbs, uint4& u, float* g) {
@@ -303,7 +309,7 @@ __device__ __forceinline__ void head_row_load(int64_t s, int64_t Ns, const __hal
     u = (live && act) ? *reinterpret_cast<const uint4*>(Y + s * ldy + c0) : make_uint4(0, 0, 0, 0);
 }
 
-__global__ void __launch_bounds__(256, 3) k_rgb_head_bwd(int64_t Ns, const __half* __restrict__ Y, int ldy, int H,
+__global__ void __launch_bounds__(256, HEAD_BWD_BLOCKS_PER_SM) k_rgb_head_bwd(int64_t Ns, const __half* __restrict__ Y, int ldy, int H,
                                                          const float* __restrict__ W, const float* __restrict__ rgbs,
                                                          const float* __restrict__ d_rgbs, __half* __restrict__ d_pre,
                                                          __half* __restrict__ dZ, __half* __restrict__ dZlo,
@@ -314,10 +320,12 @@ __global__ void __launch_bounds__(256, 3) k_rgb_head_bwd(int64_t Ns, const __hal
     const int c0 = lane * 8;
     const bool act = c0 < H;
     __shared__ __align__(16) float w_s[3][256];
+    __shared__ float dw_s[3 * 256 + 3];                 // the block's d_W, then its d_b
     for (int i = threadIdx.x; i < 3 * 256; i += blockDim.x) {
         const int k = i >> 8, c = i & 255;
         w_s[k][c] = c < H ? W[k * H + c] : 0.0f;
     }
+    for (int i = threadIdx.x; i < 3 * 256 + 3; i += blockDim.x) dw_s[i] = 0.0f;
     __syncthreads();
     float s0 = 0.f, s1 = 0.f, s2 = 0.f;
     float dw[3][8];
@@ -368,17 +376,23 @@ __global__ void __launch_bounds__(256, 3) k_rgb_head_bwd(int64_t Ns, const __hal
             if (dZlo) *reinterpret_cast<uint4*>(dZlo + s * H + c0) = *reinterpret_cast<const uint4*>(ol);
         }
     }
-    if (lane == 0 && (s0 != 0.f || s1 != 0.f || s2 != 0.f)) {
-        atomicAdd(d_b, s0);
-        atomicAdd(d_b + 1, s1);
-        atomicAdd(d_b + 2, s2);
+    if (lane == 0) {
+        atomicAdd(&dw_s[3 * 256], s0);
+        atomicAdd(&dw_s[3 * 256 + 1], s1);
+        atomicAdd(&dw_s[3 * 256 + 2], s2);
     }
     if (d_W && act) {
 #pragma unroll
         for (int k = 0; k < 3; ++k)
 #pragma unroll
-            for (int i = 0; i < 8; ++i)
-                if (dw[k][i] != 0.0f) atomicAdd(d_W + k * H + c0 + i, dw[k][i]);
+            for (int i = 0; i < 8; ++i) atomicAdd(&dw_s[k * 256 + c0 + i], dw[k][i]);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 3 * 256 + 3; i += blockDim.x) {
+        const float v = dw_s[i];
+        if (v == 0.0f) continue;
+        if (i >= 3 * 256) atomicAdd(d_b + (i - 3 * 256), v);
+        else if (d_W && (i & 255) < H) atomicAdd(d_W + (i >> 8) * H + (i & 255), v);
     }
 }
 
@@ -463,7 +477,15 @@ extern "C" int gbsdf_rgb_head_bwd(int64_t Ns, const void* Y, int ldy, int H, con
     GBSDF_CHECK_ARG(ldy % 8 == 0 && ldy >= H && aligned(Y, 16) && aligned(dZ, 16), "layout");
     GBSDF_CHECK_ARG(!d_pre || aligned(d_pre, 16), "d_pre alignment");
     GBSDF_CHECK_ARG(!dZ_lo || aligned(dZ_lo, 16), "dZ_lo alignment");
-    k_rgb_head_bwd<<<head_blocks(Ns), 256, 0, as_stream(stream)>>>(
+    unsigned blocks = head_blocks(Ns);
+    {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const unsigned resident = (unsigned)((sms > 0 ? sms : 1) * HEAD_BWD_BLOCKS_PER_SM);
+        if (blocks > resident) blocks = resident;
+    }
+    k_rgb_head_bwd<<<blocks, 256, 0, as_stream(stream)>>>(
         Ns, (const __half*)Y, ldy, H, W, rgbs, d_rgbs, (__half*)d_pre, (__half*)dZ, (__half*)dZ_lo, d_b, d_W);
     return launch_status("rgb_head_bwd");
 }

@@ -11,9 +11,11 @@ Precision: the hash table and the MLP weights are used as FP16 copies of the
 FP32 masters; every contraction accumulates in FP32 (tcgen05 TMEM); the SDF
 head, positions, tap differences, transmittance (log space) and losses stay
 FP32; the loss sums are accumulated in FP64.  Gradients are computed with a
-static loss scale (2^15 by default) and unscaled into FP32; ``found_inf``
-reports an overflow so a caller can skip the step and lower the scale
-(dynamic loss scaling).
+loss scale and unscaled into FP32.  With dynamic loss scaling (the default, as the
+reference's GradScaler: imaginaire/trainers/base.py:186-193,447-454) the scale lives
+in a device scalar that starts at 2^15: a step whose gradients are not finite sets a
+device flag (``found_inf``) and halves the scale, and growth_interval clean steps in
+a row double it; the update runs on the device, inside a captured graph too.
 
 Kernels per step (all on the current stream):
   field_fwd, dense x (1 + colour layers), rgb_head_fwd, render_fused,
@@ -41,7 +43,8 @@ class FieldArgs(ctypes.Structure):
                 ("d_hess", c_vp), ("d_xc", c_vp), ("ld_dxc", c_i32), ("normal_col", c_i32), ("d_h0c", c_vp),
                 ("d_table", c_vp), ("d_pre0", c_vp), ("x0ext", c_vp), ("d_enc", c_vp), ("d_whead", c_vp),
                 ("d_bhead", c_vp),
-                ("err", c_vp), ("d_w0", c_vp), ("h0c_lo", c_vp), ("xc_lo", c_vp), ("d_pre0_lo", c_vp)]
+                ("err", c_vp), ("d_w0", c_vp), ("h0c_lo", c_vp), ("xc_lo", c_vp), ("d_pre0_lo", c_vp),
+                ("d_table_scale_dev", c_vp), ("found_inf", c_vp)]
 
 
 class RenderArgs(ctypes.Structure):
@@ -54,7 +57,7 @@ class RenderArgs(ctypes.Structure):
                 ("loss_sums", c_vp), ("err", c_vp), ("n_bg", c_i32), ("ld_d_bg_pre", c_i32), ("bg_dists", c_vp),
                 ("bg_sigma", c_vp), ("bg_rgbs", c_vp), ("bg_weights", c_vp), ("d_bg_rgbs", c_vp), ("d_bg_pre", c_vp),
                 ("forward_only", c_i32), ("pad2", c_i32), ("out_opacity", c_vp), ("out_gradient", c_vp),
-                ("out_dist", c_vp)]
+                ("out_dist", c_vp), ("dyn", c_vp)]
 
 
 _lib.register("gbsdf_field_args_size", [])
@@ -170,9 +173,15 @@ class FusedField:
     """Fused FP16 forward+backward over a FieldModel's FP32 master parameters."""
 
     def __init__(self, model, loss_scale=2.0 ** 15, split_colour_grads=False, fused_w0_grad=True,
-                 activation_pairs=True):
+                 activation_pairs=True, dynamic_loss_scale=True, growth_interval=2000):
         check_struct_sizes()
         self.model = model
+        # dynamic loss scaling: the scale, the schedule scalars and the overflow flag in one device
+        # buffer (created at the first step): [0] loss scale, [1] anneal, [2] curvature weight,
+        # [3] 1 / loss scale, [4] found_inf; an int32 growth tracker beside it
+        self.dynamic = bool(dynamic_loss_scale)
+        self.growth_interval = int(growth_interval)
+        self._scal = self._growth = self._one = None
         # forward activations that feed another layer's forward stored as fp16 hi + lo pairs
         # (the SDF layer-0 output, the colour input, the colour hidden layers but the last):
         # with single fp16 storage the next layer's pre-activations move by the fp16 rounding
@@ -393,7 +402,7 @@ class FusedField:
         of the distances over object and background samples).  ``target`` may be absent."""
         return self.step(batch, compute_loss=False, _evaluate=True)
 
-    def step(self, batch, compute_loss=True, _evaluate=False):
+    def step(self, batch, compute_loss=True, _evaluate=False, _refresh=True):
         """Forward + backward on a batch (same keys as FieldModel.render_step).
 
         Ragged batches pass ``ray_offsets`` [R+1] (int64) and flat ``dists`` [Ns];
@@ -418,6 +427,12 @@ class FusedField:
             offs = None
             sample_ray = None
         ws = self._workspace(R, S, Ns, dev)
+        scal = self._scalars(dev) if self.dynamic else None
+        if scal is not None:
+            if _refresh:
+                self.refresh_scalars()
+            scal[4:5].zero_()                                        # found_inf of this step
+            torch.reciprocal(scal[0:1], out=scal[3:4])               # 1 / loss scale
         dists_f = dists.reshape(-1).contiguous().float()
         center = batch['center'].contiguous().float()
         ray_unit = batch['ray_unit'].contiguous().float()
@@ -491,6 +506,7 @@ class FusedField:
         ra.l1_scale = 3.0 / (3.0 * R)
         ra.mean_scale = 1.0 / n_mean
         ra.loss_scale = self.loss_scale
+        ra.dyn = _p(scal)
         ra.rgb, ra.weights = _p(ws['rgb']), _p(ws['weights'])
         ra.d_rgbs, ra.d_sdf, ra.d_grad, ra.d_hess = _p(ws['d_rgbs']), _p(ws['d_sdf']), _p(ws['d_grad']), \
             _p(ws['d_hess'])
@@ -570,6 +586,8 @@ class FusedField:
         else:
             d_table = torch.zeros(table.shape, device=dev, dtype=torch.float32)
         fa.d_table_scale = 1.0 / self.loss_scale
+        fa.d_table_scale_dev = scal[3:4].data_ptr() if scal is not None else None
+        fa.found_inf = scal[4:5].data_ptr() if scal is not None else None
         ws['d_whead'].zero_()
         ws['d_bhead'].zero_()
         fa.d_sdf, fa.d_grad, fa.d_hess = _p(ws['d_sdf']), _p(ws['d_grad']), _p(ws['d_hess'])
@@ -594,7 +612,9 @@ class FusedField:
         if self.bg:
             grads['bg'] = self._background_backward(R, app_idx, stream)
         self._scatter_grads(grads)
-        self._loss_norm = (R, n_mean, float(lw.render), float(lw.eikonal), float(m.w_curv or 0.0))
+        if scal is not None:
+            self._check_and_update_scale(scal)
+        self._loss_norm = (R, n_mean, float(lw.render), float(lw.eikonal))
         out = self.losses() if compute_loss else {}
         out['rgb'] = ws['rgb']
         return out
@@ -683,7 +703,8 @@ class FusedField:
 
     def losses(self):
         """Loss terms of the last step (reads the FP64 device sums: synchronises)."""
-        R, n_mean, w_r, w_e, w_c = self._loss_norm
+        R, n_mean, w_r, w_e = self._loss_norm
+        w_c = float(self.model.w_curv or 0.0)
         sums = self.ws['loss_sums'].tolist()
         l_render = 3.0 * sums[0] / (3.0 * R)
         l_eik = sums[1] / n_mean
@@ -705,7 +726,7 @@ class FusedField:
         """Unscale, map effective-weight gradients onto the weight-norm parameters
         (W = g v / ||v||) with autograd, and accumulate into the masters' .grad."""
         m = self.model
-        inv = 1.0 / self.loss_scale
+        inv = self._scal[3:4] if self.dynamic else 1.0 / self.loss_scale
         sdf = m.neural_sdf
         A, F = self.A, self.F
         K0 = self.K0
@@ -777,12 +798,55 @@ class FusedField:
         if self.app_dim:
             _acc(self.model.appear_embed_outside.weight, g['app'] * inv)
 
+    # ------------------------------------------------------------------ dynamic loss scaling
+    def _scalars(self, device):
+        if self._scal is None or self._scal.device != torch.device(device):
+            self._scal = torch.zeros(8, device=device, dtype=torch.float32)
+            self._scal[0] = self.loss_scale
+            self._growth = torch.zeros(1, device=device, dtype=torch.int32)
+            self._one = torch.ones(1, device=device, dtype=torch.float32)
+            self.refresh_scalars()
+        return self._scal
+
+    def refresh_scalars(self):
+        """Copy the schedule's per-iteration scalars (the anneal ratio of iter_cos and the
+        curvature weight) into the device buffer the render kernel reads.  Eager steps do this
+        themselves; CapturedStep.replay calls it before every replay."""
+        if self._scal is None:
+            return
+        m = self.model
+        self._scal[1].fill_(min(m.progress / m.anneal_end, 1.0))
+        self._scal[2].fill_(float(m.w_curv or 0.0))
+
+    def _check_and_update_scale(self, scal):
+        """found_inf |= any non-finite master gradient (the scatter already flagged the table's);
+        then the scale update of GradScaler.update: x 0.5 on overflow, x 2 after growth_interval
+        clean steps in a row.  Device work only, no host synchronisation."""
+        table = self.model.neural_sdf.tcnn_encoding.params
+        small = [p.grad for p in self.model.parameters()
+                 if p.grad is not None and p is not table and p.grad.dtype == torch.float32]
+        if small:
+            torch._amp_foreach_non_finite_check_and_unscale_(small, scal[4:5], self._one)
+        torch._amp_update_scale_(scal[0:1], self._growth, scal[4:5], 2.0, 0.5, self.growth_interval)
+
     def found_inf(self):
-        """True when any master gradient is non-finite (skip the step, halve the scale)."""
+        """True when the last step's gradients were not finite (skip that optimizer step; the
+        scale has already been halved).  One device read."""
+        if self.dynamic:
+            return bool(self._scal[4].item() > 0) if self._scal is not None else False
         for prm in self.model.parameters():
             if prm.grad is not None and not torch.isfinite(prm.grad).all():
                 return True
         return False
+
+    def current_loss_scale(self):
+        return float(self._scal[0].item()) if (self.dynamic and self._scal is not None) else self.loss_scale
+
+    def schedule_key(self):
+        """The schedule values baked into a step's launches (normal epsilon, active levels):
+        a captured graph is valid while these are unchanged."""
+        sdfm = self.model.neural_sdf
+        return (float(sdfm.normal_eps), int(sdfm.active_levels))
 
 
 def _acc(param, grad):
@@ -795,21 +859,34 @@ def _acc(param, grad):
 
 class CapturedStep:
     """One training step of a FusedField -- zero the master gradients, forward,
-    backward -- captured once in a CUDA graph and replayed.
+    backward (and, with dynamic loss scaling, the overflow check and the scale update) --
+    captured in a CUDA graph and replayed.
 
     The batch is copied into static device buffers at capture time; ``replay(batch)``
     copies a new batch of the same shapes into them (host tensors are copied from
     pinned memory asynchronously) and launches the whole step as one graph.  The
     gradients land in the masters' ``.grad`` tensors, which must not be replaced
     (zero_grad(set_to_none=True) between replays would detach them from the graph).
+
+    Schedule: the per-iteration scalars (iter_cos anneal ratio, curvature weight) are read
+    from a device buffer that every replay refreshes from the model, and the loss scale is a
+    device scalar; the normal epsilon and the active levels are baked into the launches, so
+    replay() captures the step again when model.schedule() has changed them (every few
+    thousand iterations of the coarse-to-fine schedule).
     """
 
     def __init__(self, fused, batch, warmup=2):
         self.fused = fused
-        model = fused.model
-        dev = batch['center'].device
         self.static = {k: v.clone() for k, v in batch.items() if torch.is_tensor(v)}
         self.static.update({k: v for k, v in batch.items() if not torch.is_tensor(v)})
+        self.graph = None
+        self.recaptures = 0
+        self._capture(warmup)
+
+    def _capture(self, warmup):
+        fused, model = self.fused, self.fused.model
+        dev = self.static['center'].device
+        self.graph = None
         side = torch.cuda.Stream(dev)
         side.wait_stream(torch.cuda.current_stream(dev))
         with torch.cuda.stream(side):
@@ -822,17 +899,25 @@ class CapturedStep:
         for p in self.params:
             if p.grad is None:
                 p.grad = torch.zeros_like(p)
+        if fused.dynamic:
+            fused._scalars(dev)           # created eagerly: a scale set inside the capture would reset at replays
+        fused.refresh_scalars()
+        self.key = fused.schedule_key()
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
             for p in self.params:
                 p.grad.zero_()
-            self.out = fused.step(self.static, compute_loss=False)
+            self.out = fused.step(self.static, compute_loss=False, _refresh=False)
 
     def replay(self, batch=None):
+        if self.fused.schedule_key() != self.key:
+            self.recaptures += 1
+            self._capture(warmup=1)
         if batch is not None:
             for k, v in batch.items():
                 if torch.is_tensor(v):
                     self.static[k].copy_(v, non_blocking=True)
+        self.fused.refresh_scalars()
         self.graph.replay()
         return self.out
 

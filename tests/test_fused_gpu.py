@@ -401,3 +401,95 @@ def test_in_kernel_layer0_weight_gradient_matches_gemm_path():
     # the same fp16 products summed in another order (FP32 both ways)
     for k, e in errs.items():
         assert e < 1e-5, (k, e)
+
+
+def test_captured_step_follows_the_schedule():
+    """A captured step replayed after model.schedule(): the anneal ratio and curvature weight
+    come from a device buffer refreshed at every replay (the replay equals an eager step at
+    the new iteration), and a change of active levels / normal epsilon re-captures."""
+    model = build()
+    batch = make_rays(32, 24, seed=9, miss_frac=0.1, n_images=10, device=DEV)
+    model.schedule(2000)                                  # warm-up: w_curv ramps with the iteration
+    ff = FusedField(model)
+    cap = CapturedStep(ff, batch)
+    model.zero_grad(set_to_none=False)
+    l_2000 = ff.step(batch)['loss']
+    model.schedule(3000)
+    assert ff.schedule_key() == cap.key
+    cap.replay()
+    torch.cuda.synchronize()
+    l_graph = cap.losses()['loss']
+    g_graph = {k: v.clone() for k, v in fused_grads(model).items()}
+    model.zero_grad(set_to_none=False)
+    l_eager = ff.step(batch)['loss']
+    g_eager = fused_grads(model)
+    print(f"\nloss at 2000 {l_2000:.6e}, at 3000: graph {l_graph:.6e} eager {l_eager:.6e}")
+    assert abs(l_2000 - l_eager) > 1e-4 * abs(l_eager)     # the schedule moved the loss
+    assert abs(l_graph - l_eager) <= 1e-6 * abs(l_eager)
+    for k in ('table', 'sdf.l0.v', 'rgb.l0.v', 's_var'):
+        assert rel(g_graph[k], g_eager[k]) < 1e-5, k
+    # coarse-to-fine: more active levels (and a new epsilon) -> the replay captures again
+    model.schedule(full_field_iteration(8))
+    assert ff.schedule_key() != cap.key
+    cap.replay()
+    torch.cuda.synchronize()
+    assert cap.recaptures == 1
+    l_graph = cap.losses()['loss']
+    g_graph = {k: v.clone() for k, v in fused_grads(model).items()}
+    model.zero_grad(set_to_none=False)
+    l_eager = ff.step(batch)['loss']
+    g_eager = fused_grads(model)
+    assert abs(l_graph - l_eager) <= 1e-6 * abs(l_eager)
+    for k in ('table', 'sdf.l0.v', 'rgb.l0.v'):
+        assert rel(g_graph[k], g_eager[k]) < 1e-5, k
+
+
+def test_dynamic_loss_scale_inside_the_graph():
+    """GradScaler's rule on the device, replay by replay: an overflowing scale halves until the
+    gradients are finite, growth_interval clean steps double it; an inf planted in an input
+    between replays raises found_inf and halves the scale; gradients of clean steps match an
+    eager step at the default scale."""
+    model = build()
+    batch = make_rays(32, 16, seed=1, n_images=10, device=DEV)
+    ref = FusedField(model)
+    model.zero_grad(set_to_none=True)
+    ref.step(batch)
+    g_ref = {k: v.clone() for k, v in fused_grads(model).items()}
+    ff = FusedField(model, loss_scale=2.0 ** 40, growth_interval=3)
+    cap = CapturedStep(ff, batch, warmup=0)
+    scale, tracker, seen = 2.0 ** 40, 0, []
+    for _ in range(30):
+        cap.replay()
+        inf = ff.found_inf()
+        new = ff.current_loss_scale()
+        seen.append((scale, inf))
+        # GradScaler.update: back off on overflow, grow after growth_interval clean steps
+        if inf:
+            want, tracker = scale * 0.5, 0
+        else:
+            tracker += 1
+            want = scale * 2.0 if tracker == 3 else scale
+            tracker = 0 if tracker == 3 else tracker
+        assert new == want, (seen, new, want)
+        if not inf:
+            g = fused_grads(model)
+            for k in ('table', 'sdf.l0.v', 'rgb.l4.v', 's_var'):
+                assert torch.isfinite(g[k]).all() and rel(g[k], g_ref[k]) < 1e-3, k
+        scale = new
+    flags = [f for _, f in seen]
+    assert flags[0] and not all(flags) and any(not f for f in flags[-6:])
+    print("\nscale / found_inf per replay:", [(int(round(torch.log2(torch.tensor(s)).item())), f) for s, f in seen])
+    # an inf in an input (an appearance code used by the batch) between replays
+    img = int(batch['app_idx'][0])
+    while ff.found_inf():
+        cap.replay()
+    before = ff.current_loss_scale()
+    with torch.no_grad():
+        saved = model.appear_embed.weight[img].clone()
+        model.appear_embed.weight[img, 0] = float('inf')
+    cap.replay()
+    assert ff.found_inf() and ff.current_loss_scale() == before * 0.5
+    with torch.no_grad():
+        model.appear_embed.weight[img] = saved
+    cap.replay()
+    assert not ff.found_inf()
