@@ -135,6 +135,24 @@ def bench_background(device, steps, warmup, rays=R_RAYS, samples=N_SAMPLES, n_bg
                 speedup_vs_plain=round(ms_plain / ms, 3))
 
 
+def bench_taps4(device, steps, warmup, rays=R_RAYS, samples=N_SAMPLES, seed=0):
+    """The same full-field step with the 4-tap tetrahedral stencil, the reference's default
+    configuration (projects/neuralangelo/configs/base.yaml:68): 5 evaluations per sample
+    instead of 7, replayed from a captured CUDA graph."""
+    import torch
+    from neuralangelo_gb300.fused import CapturedStep, FusedField
+    from neuralangelo_gb300.workloads import make_rays
+    model = make_plain(device, seed, taps=4)
+    batch = make_rays(rays, samples, seed=seed, n_images=100, device=device)
+    cap = CapturedStep(FusedField(model), batch)
+    ms = time_steps(cap.replay, steps, warmup, lambda: None)
+    out = dict(samples=rays * samples, ms_per_step=round(ms, 3),
+               value=round(rays * samples / (ms * 1e-3), 1), unit="samples/s")
+    del cap
+    torch.cuda.empty_cache()
+    return out
+
+
 def bench_sampler(model, device, steps=5, warmup=2, rays=R_RAYS, seed=0):
     """The no-grad hierarchical pre-pass (64 coarse + 4 x 16 importance samples per ray,
     SDF of the fused field kernel), timed separately from the training step."""
@@ -152,13 +170,20 @@ def bench_sampler(model, device, steps=5, warmup=2, rays=R_RAYS, seed=0):
                 rays_per_s=round(rays / (ms * 1e-3), 1), sdf_evals_per_s=round(evals / (ms * 1e-3), 1))
 
 
-def bench_mesh(model, device, res=512, block_res=128):
-    """Mesh extraction of the field's geometric-init surface (a sphere of radius 0.5) on a
-    512^3 lattice in 128^3 blocks: lattice SDF kernel + GPU marching cubes per block,
+def bench_mesh(model, device, res=512, block_res=128, shapes_seed=7, fit_steps=300):
+    """Mesh extraction from a trained-shape field: a fresh full field (L16 F8 T2^22) whose SDF
+    is fitted to a seeded union of 3 spheres and 2 boxes (workloads.shapes_union, Adam on L1),
+    then a 512^3 lattice in 128^3 blocks: lattice SDF kernel + GPU marching cubes per block,
     each block's mesh copied to the host as the reference does (mesh.py:33-46)."""
     import torch
     from neuralangelo_gb300.mesh import FieldSDF, extract_mesh
-    f = FieldSDF(model.neural_sdf, sign=-1.0)
+    from neuralangelo_gb300.workloads import fit_sdf, shapes_union
+    target = shapes_union(shapes_seed)
+    field = make_plain(device, seed=1)
+    t_fit = time.perf_counter()
+    fit_loss = fit_sdf(field.neural_sdf, target, steps=fit_steps)
+    t_fit = time.perf_counter() - t_fit
+    f = FieldSDF(field.neural_sdf, sign=-1.0)
     intv = 2.0 / res
     bounds = [(-1.0, 1.0)] * 3
     extract_mesh(f, [(-1.0, -0.5)] * 3, intv, block_res, device=device)   # warm-up
@@ -184,7 +209,12 @@ def bench_mesh(model, device, res=512, block_res=128):
         t2 = time.perf_counter()
         write_ply(os.path.join(d, "mesh.ply"), Vo.cpu().numpy(), Fo.cpu().numpy())
         t_ply = time.perf_counter() - t2
-    return dict(resolution=res, block_res=block_res, seconds=round(dt, 4), lattice_points=pts,
+    with torch.no_grad():
+        err = target(torch.from_numpy(mesh.vertices).to(device)).abs()
+    return dict(field=f"full field fitted to shapes_union({shapes_seed}) in {fit_steps} Adam steps "
+                      f"({t_fit:.1f} s, final L1 {fit_loss:.4f}); surface vertices' distance to the target "
+                      f"surface: median {float(err.median()):.4f}",
+                resolution=res, block_res=block_res, seconds=round(dt, 4), lattice_points=pts,
                 points_per_s=round(pts / dt, 1), vertices=int(mesh.vertices.shape[0]),
                 faces=int(mesh.faces.shape[0]), welded_vertices=int(Vo.shape[0]),
                 finalize_seconds=round(t_fin, 5), ply_write_seconds=round(t_ply, 4))
@@ -317,13 +347,15 @@ class ClockSampler:
 
 # --------------------------------------------------------------------------- GPU arm
 
-def make_plain(device, seed=0):
+def make_plain(device, seed=0, taps=6):
     import torch
     from neuralangelo_gb300.config import field_config
     from neuralangelo_gb300.model import FieldModel
     from neuralangelo_gb300.workloads import full_field_iteration, init_field_params
     torch.manual_seed(seed)
-    model = FieldModel(field_config("full")).to(device)
+    cfg = field_config("full")
+    cfg.sdf.gradient.taps = taps
+    model = FieldModel(cfg).to(device)
     init_field_params(model, seed)
     model.schedule(full_field_iteration(ACTIVE))
     assert model.neural_sdf.active_levels == ACTIVE
@@ -533,6 +565,7 @@ def main():
         fused.release()
         torch.cuda.empty_cache()
         torch.cuda.empty_cache()
+        extras["taps4"] = bench_taps4(device, max(3, args.steps // 2), args.warmup)
         extras["ragged"] = bench_ragged(model, device, max(3, args.steps // 2), args.warmup)
         extras["background"] = bench_background(device, max(3, args.steps // 2), args.warmup)
         extras["sampler"] = bench_sampler(model, device)

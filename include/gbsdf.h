@@ -211,6 +211,13 @@ typedef struct gbsdf_field_args {
                                         inverse of a loss scale the device updates) */
     float* found_inf;        /* optional: the scatter sets *found_inf = 1 when it reads a non-finite d_enc
                                 value (the table gradient would be non-finite) */
+    int32_t taps;            /* numerical-gradient stencil: 6 (or 0) = +-eps along each axis, 18 samples of
+                                7 evaluations per 126-row tile (modules.py:132-156); 4 = the tetrahedral
+                                stencil, 25 samples of 5 evaluations per 125-row tile (modules.py:157-175):
+                                then eps = the tap displacement normal_eps / sqrt(3), two_eps = 4 eps and
+                                eps2 = eps^2.  x0ext, d_enc and d_pre0 hold ceil(Ns / samples per tile)
+                                tiles of rows. */
+    int32_t pad_taps;
 } gbsdf_field_args;
 
 size_t gbsdf_field_args_size(void);

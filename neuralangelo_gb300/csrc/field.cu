@@ -7,9 +7,10 @@
 // (projects/neuralangelo/model.py:163) and the input of NeuralRGB
 // (modules.py:209-220: x, SH(view dir), normalize(gradient), feature, appearance).
 //
-// Tile = 18 samples x 7 evaluations (centre + 6 taps) = 126 rows (+2 zero rows)
+// Tile = 18 samples x 7 evaluations (centre + 6 taps) = 126 rows (+2 dead rows)
 // of a 128-row tcgen05 tile.  Row r holds evaluation e = r / 18 of sample r % 18:
-// e = 0 centre, 1 +x, 2 -x, 3 +y, 4 -y, 5 +z, 6 -z.  The hash-grid features of
+// e = 0 centre, 1 +x, 2 -x, 3 +y, 4 -y, 5 +z, 6 -z.  With 4 taps (the tetrahedral
+// stencil, modules.py:157-175) a tile is 25 samples x 5 evaluations = 125 rows.  The hash-grid features of
 // the active levels are gathered straight into the shared-memory A tile
 // (fp16, K-major core-matrix layout); W0's encoding columns are resident; the
 // three position columns, bias, softplus and the SDF head run in fp32 in the
@@ -19,8 +20,20 @@
 
 namespace gbsdf {
 
-constexpr int SPT = 18;          // samples per tile
-constexpr int EVALS = 7;
+// Evaluations of one sample (the centre, then the taps) and samples per 128-row tile:
+// 6 taps (modules.py:132-156): 18 samples x 7 = 126 rows; 4 taps (modules.py:157-175):
+// 25 samples x 5 = 125 rows.
+template <int TAPS>
+struct TapTile {
+    static_assert(TAPS == 6 || TAPS == 4, "4 or 6 taps");
+    static constexpr int EVALS = TAPS + 1;
+    static constexpr int SPT = TAPS == 6 ? 18 : 25;
+    static constexpr int ROWS = SPT * EVALS;
+    // the backward's double-buffered d f per evaluation row (+4 floats of slack), rounded up to
+    // 4 floats so the d_h0c rows after it stay 16-byte aligned (cp.async and float4 accesses)
+    static constexpr int DF_FLOATS = (2 * ROWS + 4 + 3) / 4 * 4;
+};
+constexpr int FWD_SDF_FLOATS = 128;   // forward's per-evaluation SDF values (<= 126) + padding
 constexpr int FIELD_THREADS = 256;
 constexpr int HID = 256;         // SDF hidden width (base.yaml:41)
 
@@ -39,12 +52,22 @@ __device__ __forceinline__ void sample_point(const FieldParams& p, int64_t s, fl
     for (int i = 0; i < 3; ++i) x[i] = __fadd_rn(p.center[3 * r + i], __fmul_rn(p.ray_unit[3 * r + i], t));
 }
 
-// evaluation position: the reference adds a float32 [eps,0,0]-style vector (modules.py:135-143)
+// evaluation position: the reference adds a float32 tap vector to the point.
+// 6 taps: e = 1..6 -> +x, -x, +y, -y, +z, -z by eps (modules.py:135-143).
+// 4 taps: e = 1..4 -> k1 (1,-1,-1), k2 (-1,-1,1), k3 (-1,1,-1), k4 (1,1,1) times the
+// displacement eps / sqrt(3), which the caller passes as `eps` (modules.py:158-166).
+template <int TAPS>
 __device__ __forceinline__ void eval_point(const float* c, int e, float eps, float* x) {
     x[0] = c[0]; x[1] = c[1]; x[2] = c[2];
-    if (e > 0) {
+    if (e == 0) return;
+    if constexpr (TAPS == 6) {
         const int d = (e - 1) >> 1;
         x[d] = (e & 1) ? __fadd_rn(x[d], eps) : __fsub_rn(x[d], eps);
+    } else {
+        const bool px = e == 1 || e == 4, py = e == 3 || e == 4, pz = e == 2 || e == 4;
+        x[0] = px ? __fadd_rn(x[0], eps) : __fsub_rn(x[0], eps);
+        x[1] = py ? __fadd_rn(x[1], eps) : __fsub_rn(x[1], eps);
+        x[2] = pz ? __fadd_rn(x[2], eps) : __fsub_rn(x[2], eps);
     }
 }
 
@@ -122,30 +145,6 @@ __device__ __forceinline__ void scatter_add(float* dst, const float* v) {
     }
 }
 
-// Stage the encoder features of one tile (126 rows) into the A tile.
-template <int F>
-__device__ void stage_encoding(const FieldParams& p, int64_t s0, uint8_t* a_s, uint8_t* a2_s) {
-    const int pairs = SPT * EVALS * p.active;
-    for (int i = threadIdx.x; i < pairs; i += blockDim.x) {
-        const int row = i / p.active, l = i % p.active;
-        const int e = row / SPT, sl = row % SPT;
-        const int64_t s = s0 + sl;
-        float v[F];
-        if (s < p.Ns) {
-            float c[3], x[3], xu[3];
-            sample_point(p, s, c);
-            eval_point(c, e, p.eps, x);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) xu[k] = to_unit(x[k]);
-            gather_level<F>(p, xu, l, v);
-        } else {
-#pragma unroll
-            for (int f = 0; f < F; ++f) v[f] = 0.0f;
-        }
-        write_tile_features<F>(a_s, a2_s, row, l, p.K0, v);
-    }
-}
-
 // ---------------------------------------------------------------------------
 // hash-grid gather and table-gradient scatter as their own kernels: one thread
 // per (row, level) / (sample, level, corner) keeps thousands of independent
@@ -158,8 +157,9 @@ __device__ void stage_encoding(const FieldParams& p, int64_t s0, uint8_t* a_s, u
 // zeroes the padding columns.  Rows of samples past the end are zeros.
 // Six blocks per SM (at most 40 registers): the gather waits on L2 latency, and the
 // extra resident warps keep more corner loads in flight.
-template <int F>
+template <int F, int TAPS>
 __global__ void __launch_bounds__(256, 6) k_field_gather(FieldParams p, int64_t ntiles) {
+    constexpr int EVALS = TapTile<TAPS>::EVALS, SPT = TapTile<TAPS>::SPT;
     const int A = p.active, K0 = p.K0, KX = 2 * K0 + 16;
     // 32-bit index arithmetic: the launcher checks rows * A < 2^32
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(256, 6) k_field_gather(FieldParams p, int64_t 
     if (live) {
         float c[3], xu[3];
         sample_point(p, s, c);
-        eval_point(c, e, p.eps, x);
+        eval_point<TAPS>(c, e, p.eps, x);
 #pragma unroll
         for (int k = 0; k < 3; ++k) xu[k] = to_unit(x[k]);
         gather_level<F>(p, xu, l, v);
@@ -222,8 +222,9 @@ __global__ void __launch_bounds__(256, 6) k_field_gather(FieldParams p, int64_t 
 // are read again per pass, from L1): fewer accumulator registers, more resident warps.
 constexpr int SCATTER_CPT = 2;
 
-template <int F, int CPT>
+template <int F, int CPT, int TAPS>
 __global__ void __launch_bounds__(256, CPT >= 8 ? 2 : (CPT == 4 ? 3 : 4)) k_field_scatter(FieldParams p) {
+    constexpr int EVALS = TapTile<TAPS>::EVALS, SPT = TapTile<TAPS>::SPT;
     const int A = p.active, K0 = p.K0;
     // 32-bit index arithmetic: the launcher checks Ns * active * 8 < 2^32
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -260,7 +261,7 @@ __global__ void __launch_bounds__(256, CPT >= 8 ? 2 : (CPT == 4 ? 3 : 4)) k_fiel
 #pragma unroll 1
         for (int e = 0; e < EVALS; ++e) {
             float x[3], xu[3];
-            eval_point(c, e, p.eps, x);
+            eval_point<TAPS>(c, e, p.eps, x);
 #pragma unroll
             for (int k = 0; k < 3; ++k) xu[k] = to_unit(x[k]);
             uint32_t bx, by, bz;
@@ -337,8 +338,9 @@ __global__ void __launch_bounds__(256, CPT >= 8 ? 2 : (CPT == 4 ? 3 : 4)) k_fiel
 // nothing; the fp16 residual of the features is a second MMA over the W0e prefix.
 constexpr int FWD_CTAS_PER_SM = 2;
 
-template <int F>
+template <int F, int TAPS>
 __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(FieldParams p) {
+    constexpr int EVALS = TapTile<TAPS>::EVALS, SPT = TapTile<TAPS>::SPT;
     extern __shared__ __align__(1024) uint8_t smem[];
     const int K0 = p.K0;
     const int KB = K0 + 16;                                     // features hi + tail
@@ -349,7 +351,9 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
     float* wh_s = reinterpret_cast<float*>(a2_s + TILE_M * K0 * 2);   // [256]
     float* part_s = wh_s + HID;                                 // [2][128] partial head sums
     float* sdf_s = part_s + 2 * TILE_M;                         // [7][18]
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(sdf_s + EVALS * SPT + 2);
+    // the mbarrier 8-byte aligned whatever the tile's row count: 128 floats past sdf_s
+    // (125 or 126 evaluation rows + padding)
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sdf_s + FWD_SDF_FLOATS);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -459,11 +463,28 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
                 const bool out = p.outside && p.outside[r];
                 const float fc = out ? p.outside_val : sdf_s[js];
                 float g[3], hh[3];
+                if constexpr (TAPS == 6) {
+                    // g_d = (f+ - f-) / (2 eps); H_dd = (f+ + f- - 2 f) / eps^2 (modules.py:144-155)
 #pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    const float fp = sdf_s[(1 + 2 * d) * SPT + js], fm = sdf_s[(2 + 2 * d) * SPT + js];
-                    g[d] = __fdiv_rn(__fsub_rn(fp, fm), p.two_eps);
-                    hh[d] = __fdiv_rn(__fsub_rn(__fadd_rn(fp, fm), __fmul_rn(2.0f, fc)), p.eps2);
+                    for (int d = 0; d < 3; ++d) {
+                        const float fp = sdf_s[(1 + 2 * d) * SPT + js], fm = sdf_s[(2 + 2 * d) * SPT + js];
+                        g[d] = __fdiv_rn(__fsub_rn(fp, fm), p.two_eps);
+                        hh[d] = __fdiv_rn(__fsub_rn(__fadd_rn(fp, fm), __fmul_rn(2.0f, fc)), p.eps2);
+                    }
+                } else {
+                    // g = (k1 f1 + k2 f2 + k3 f3 + k4 f4) / (4 e); H_xx = ((f1 + f2 + f3 + f4) / 2 - 2 f) / e^2,
+                    // every diagonal entry H_xx / 3 (modules.py:167-174); two_eps = 4 e, eps2 = e^2
+                    const float f1 = sdf_s[SPT + js], f2 = sdf_s[2 * SPT + js];
+                    const float f3 = sdf_s[3 * SPT + js], f4 = sdf_s[4 * SPT + js];
+                    const float sx = __fadd_rn(__fsub_rn(__fsub_rn(f1, f2), f3), f4);
+                    const float sy = __fadd_rn(__fadd_rn(__fsub_rn(-f1, f2), f3), f4);
+                    const float sz = __fadd_rn(__fsub_rn(__fadd_rn(-f1, f2), f3), f4);
+                    g[0] = __fdiv_rn(sx, p.two_eps);
+                    g[1] = __fdiv_rn(sy, p.two_eps);
+                    g[2] = __fdiv_rn(sz, p.two_eps);
+                    const float sum = __fadd_rn(__fadd_rn(__fadd_rn(f1, f2), f3), f4);
+                    const float hxx = __fdiv_rn(__fsub_rn(__fmul_rn(sum, 0.5f), __fmul_rn(2.0f, fc)), p.eps2);
+                    hh[0] = hh[1] = hh[2] = __fdiv_rn(hxx, 3.0f);
                 }
                 if (kc8 == 0) {
                     p.sdf[ss] = fc;
@@ -561,7 +582,6 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
 constexpr size_t BWD_SMEM_FLOOR = 120 * 1024;   // > half an SM's shared memory: one CTA per SM
 constexpr int BWD_THREADS = 512;                 // 16 warps: 4 lane quadrants x 4 quarters of the hidden units
 constexpr int BWD_STAGE_BYTES = 4096;            // per warp: 32 rows x 128 bytes
-constexpr int TILE_ROWS = SPT * EVALS;           // 126
 constexpr int DH0_LD = HID + 4;                  // d_h0c rows in shared memory, padded against bank conflicts
 
 // DW (K0 <= 64, the caller passes d_w0): the layer-0 weight gradient dW0 = d_pre^T [x hi |
@@ -579,7 +599,7 @@ constexpr int DH0_LD = HID + 4;                  // d_h0c rows in shared memory,
 //   * MMA1 of the next tile is issued as soon as MMA2 has completed (D1 is free then),
 //     under the d_enc epilogue.
 //   * Each CTA adds its dW0 into d_w0 with atomics at the end.
-template <int F, bool DW>
+template <int F, bool DW, int TAPS>
 __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
                                                              const __grid_constant__ CUtensorMap tm_pre32,
                                                              const __grid_constant__ CUtensorMap tm_pre30,
@@ -587,6 +607,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
                                                              const __grid_constant__ CUtensorMap tm_enc30,
                                                              const __grid_constant__ CUtensorMap tm_plo32,
                                                              const __grid_constant__ CUtensorMap tm_plo30) {
+    constexpr int EVALS = TapTile<TAPS>::EVALS, SPT = TapTile<TAPS>::SPT, TILE_ROWS = TapTile<TAPS>::ROWS;
     extern __shared__ __align__(1024) uint8_t smem[];
     const int K0 = p.K0;
     const int KB = K0 + 16;                                     // features hi + tail
@@ -601,7 +622,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     float* wh_s = reinterpret_cast<float*>(a3_s1 + TILE_M * KL * 2);   // [256] head weights
     float* dwh_s = wh_s + HID;                                  // [256] d_whead accumulator
     float* df_s = dwh_s + HID;                                  // [2][7][18] d f per evaluation, double-buffered
-    float* dh0_s = df_s + 2 * EVALS * SPT + 4;                  // [18][DH0_LD] d_h0c of the tile's samples
+    float* dh0_s = df_s + TapTile<TAPS>::DF_FLOATS;              // [SPT][DH0_LD] d_h0c of the tile's samples
     uint64_t* mbar = reinterpret_cast<uint64_t*>(dh0_s + SPT * DH0_LD);
     uint64_t* mbar_lo = mbar + 1;                               // DW: the lo-half dW0 MMAs of a tile
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
@@ -688,7 +709,9 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         if (tid < SPT) {
             const int64_t s = tt * SPT + tid;
             float* dfb = df_s + buf * (EVALS * SPT);
-            float df[EVALS] = {0, 0, 0, 0, 0, 0, 0};
+            float df[EVALS];
+#pragma unroll
+            for (int e = 0; e < EVALS; ++e) df[e] = 0.0f;
             if (s < p.Ns) {
                 const float g0 = in.g[0], g1 = in.g[1], g2 = in.g[2];
                 const float n0 = in.n[0], n1 = in.n[1], n2 = in.n[2];
@@ -705,12 +728,24 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
                     dg[0] += n0 * 1e12f; dg[1] += n1 * 1e12f; dg[2] += n2 * 1e12f;
                 }
                 float hsum = 0.0f;
+                if constexpr (TAPS == 6) {
 #pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    const float a = dg[d] / p.two_eps, b = in.dh[d] / p.eps2;
-                    df[1 + 2 * d] = a + b;
-                    df[2 + 2 * d] = -a + b;
-                    hsum += b;
+                    for (int d = 0; d < 3; ++d) {
+                        const float a = dg[d] / p.two_eps, b = in.dh[d] / p.eps2;
+                        df[1 + 2 * d] = a + b;
+                        df[2 + 2 * d] = -a + b;
+                        hsum += b;
+                    }
+                } else {
+                    // d H_xx = (dH_x + dH_y + dH_z) / 3; tap i: k_i . dg / (4 e) + d H_xx / (2 e^2)
+                    const float dhxx = (in.dh[0] + in.dh[1] + in.dh[2]) / 3.0f;
+                    const float b = 0.5f * dhxx / p.eps2;
+                    const float ax = dg[0] / p.two_eps, ay = dg[1] / p.two_eps, az = dg[2] / p.two_eps;
+                    df[1] = ax - ay - az + b;
+                    df[2] = -ax - ay + az + b;
+                    df[3] = -ax + ay - az + b;
+                    df[4] = ax + ay + az + b;
+                    hsum = dhxx / p.eps2;
                 }
                 // the centre feeds alpha and the Hessian only where it was not overwritten
                 df[0] = in.out ? 0.0f : (in.dsdf - 2.0f * hsum);
@@ -1175,15 +1210,18 @@ static int num_sms() {
     return n > 0 ? n : 1;
 }
 
+template <int TAPS>
 static size_t fwd_smem(int K0) {
     const size_t KB = (size_t)K0 + 16;
-    return (size_t)HID * KB * 2 + (size_t)TILE_M * (KB + K0) * 2 + (HID + 2 * TILE_M + EVALS * SPT + 2) * 4 + 16;
+    return (size_t)HID * KB * 2 + (size_t)TILE_M * (KB + K0) * 2 +
+           (HID + 2 * TILE_M + FWD_SDF_FLOATS) * 4 + 16;
 }
+template <int TAPS>
 static size_t bwd_smem(int K0, bool dw) {
     const size_t KB = (size_t)K0 + 16;
     const size_t need = (size_t)(BWD_THREADS / 32) * BWD_STAGE_BYTES + (size_t)HID * KB * 2 +
                         (size_t)TILE_M * (KB + (dw ? KB : K0)) * 2 * (dw ? 2 : 1) +
-                        (2 * HID + 2 * EVALS * SPT + 4 + SPT * DH0_LD) * 4 + 24;
+                        (2 * HID + TapTile<TAPS>::DF_FLOATS + TapTile<TAPS>::SPT * DH0_LD) * 4 + 24;
     return need > BWD_SMEM_FLOOR ? need : BWD_SMEM_FLOOR;
 }
 
@@ -1191,10 +1229,12 @@ static size_t bwd_smem(int K0, bool dw) {
 // bit 1 the MLP forward, bit 2 the MLP backward, bit 3 the table-gradient scatter.
 enum FieldKernels : int { FK_GATHER = 1, FK_MLP_FWD = 2, FK_MLP_BWD = 4, FK_SCATTER = 8 };
 
-template <int F>
+template <int F, int TAPS>
 static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
+    constexpr int EVALS = TapTile<TAPS>::EVALS, SPT = TapTile<TAPS>::SPT, TILE_ROWS = TapTile<TAPS>::ROWS;
+    constexpr int LAST_BOX = TILE_ROWS - 96;          // rows of a tile's last 32-row lane quadrant
     const int64_t ntiles = (p.Ns + SPT - 1) / SPT;
-    // largest thread index: gather ntiles * 126 * active, scatter Ns * active * 8
+    // largest thread index: gather ntiles * rows per tile * active, scatter Ns * active * 8
     const int64_t gather_items = ntiles * (SPT * EVALS) * (int64_t)p.active;
     const int64_t scatter_items = p.Ns * (int64_t)p.active * 8;
     if ((gather_items > scatter_items ? gather_items : scatter_items) >= ((int64_t)1 << 32)) {
@@ -1204,30 +1244,31 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
     }
     if (which & FK_GATHER) {
         const int64_t items = ntiles * (SPT * EVALS) * p.active;
-        k_field_gather<F><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p, ntiles);
+        k_field_gather<F, TAPS><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p, ntiles);
         if (int st = launch_status("field gather")) return st;
     }
     if (which & FK_MLP_FWD) {
-        const size_t smem = fwd_smem(p.K0);
+        const size_t smem = fwd_smem<TAPS>(p.K0);
         if (smem > 227 * 1024) {
             set_error("field forward needs %zu B of shared memory", smem);
             return GBSDF_ERR_UNSUPPORTED;
         }
         int64_t grid = num_sms() * FWD_CTAS_PER_SM;
         if (grid > ntiles) grid = ntiles;
-        allow_max_smem(k_field_fwd<F>);
-        k_field_fwd<F><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p);
+        allow_max_smem(k_field_fwd<F, TAPS>);
+        k_field_fwd<F, TAPS><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p);
         if (int st = launch_status("field forward")) return st;
     }
     if (which & FK_MLP_BWD) {
         const bool dw = p.d_w0 != nullptr;
-        const size_t smem = bwd_smem(p.K0, dw);
+        const size_t smem = bwd_smem<TAPS>(p.K0, dw);
         if (smem > 227 * 1024) {
             set_error("field backward needs %zu B of shared memory", smem);
             return GBSDF_ERR_UNSUPPORTED;
         }
-        // d_pre0 [126 T, 256] fp16 (without d_w0) and d_enc [126 T, K0] fp32 as TMA store
-        // targets; with d_w0 the d_pre0 maps are never used and describe d_enc's memory
+        // d_pre0 [rows, 256] fp16 (without d_w0) and d_enc [rows, K0] fp32 as TMA store targets
+        // (rows = tiles x 126 or 125); with d_w0 the d_pre0 maps are never used and describe
+        // d_enc's memory.  The '30' maps are the last lane quadrant's LAST_BOX-row boxes.
         const int64_t rows = ntiles * TILE_ROWS;
         if (rows >= ((int64_t)1 << 31)) {
             set_error("%lld backward rows exceed the TMA coordinate range", (long long)rows);
@@ -1239,14 +1280,14 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
             if (int st = tensor_map_2d(&tm_pre32, false, p.d_pre0, rows, HID, HID, 64, 32,
                                        CU_TENSOR_MAP_SWIZZLE_128B, l2n, "d_pre0"))
                 return st;
-            if (int st = tensor_map_2d(&tm_pre30, false, p.d_pre0, rows, HID, HID, 64, 30,
+            if (int st = tensor_map_2d(&tm_pre30, false, p.d_pre0, rows, HID, HID, 64, LAST_BOX,
                                        CU_TENSOR_MAP_SWIZZLE_128B, l2n, "d_pre0"))
                 return st;
         }
         if (int st = tensor_map_2d(&tm_enc32, true, p.d_enc, rows, p.K0, p.K0, 16, 32, CU_TENSOR_MAP_SWIZZLE_64B, l2n,
                                    "d_enc"))
             return st;
-        if (int st = tensor_map_2d(&tm_enc30, true, p.d_enc, rows, p.K0, p.K0, 16, 30, CU_TENSOR_MAP_SWIZZLE_64B, l2n,
+        if (int st = tensor_map_2d(&tm_enc30, true, p.d_enc, rows, p.K0, p.K0, 16, LAST_BOX, CU_TENSOR_MAP_SWIZZLE_64B, l2n,
                                    "d_enc"))
             return st;
         if (dw) tm_pre32 = tm_pre30 = tm_enc32;
@@ -1254,7 +1295,7 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
             if (int st = tensor_map_2d(&tm_plo32, false, p.d_pre0_lo, rows, HID, HID, 64, 32,
                                        CU_TENSOR_MAP_SWIZZLE_128B, l2n, "d_pre0_lo"))
                 return st;
-            if (int st = tensor_map_2d(&tm_plo30, false, p.d_pre0_lo, rows, HID, HID, 64, 30,
+            if (int st = tensor_map_2d(&tm_plo30, false, p.d_pre0_lo, rows, HID, HID, 64, LAST_BOX,
                                        CU_TENSOR_MAP_SWIZZLE_128B, l2n, "d_pre0_lo"))
                 return st;
         } else {
@@ -1263,19 +1304,19 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
         int64_t grid = num_sms();
         if (grid > ntiles) grid = ntiles;
         if (dw) {
-            allow_max_smem(k_field_bwd<F, true>);
-            k_field_bwd<F, true><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30,
+            allow_max_smem(k_field_bwd<F, true, TAPS>);
+            k_field_bwd<F, true, TAPS><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30,
                                                                              tm_plo32, tm_plo30);
         } else {
-            allow_max_smem(k_field_bwd<F, false>);
-            k_field_bwd<F, false><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30,
+            allow_max_smem(k_field_bwd<F, false, TAPS>);
+            k_field_bwd<F, false, TAPS><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30,
                                                                               tm_plo32, tm_plo30);
         }
         if (int st = launch_status("field backward")) return st;
     }
     if (which & FK_SCATTER) {
         const int64_t items = p.Ns * p.active;
-        k_field_scatter<F, SCATTER_CPT><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p);
+        k_field_scatter<F, SCATTER_CPT, TAPS><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p);
         if (int st = launch_status("field scatter")) return st;
     }
     return GBSDF_OK;
@@ -1293,6 +1334,7 @@ static int check_field_weights(const FieldParams& p) {
 
 static int check_field(const FieldParams& p) {
     GBSDF_CHECK_ARG(p.Ns >= 0, "Ns < 0");
+    GBSDF_CHECK_ARG(p.taps == 0 || p.taps == 4 || p.taps == 6, "taps %d (4 or 6; 0 means 6)", p.taps);
     if (int st = check_field_weights(p)) return st;
     GBSDF_CHECK_ARG(p.S > 0 || p.sample_ray, "need S > 0 or sample_ray");
     GBSDF_CHECK_ARG(p.center && p.ray_unit && p.dists, "NULL ray pointer");
@@ -1305,12 +1347,16 @@ using namespace gbsdf;
 
 extern "C" size_t gbsdf_field_args_size(void) { return sizeof(gbsdf_field_args); }
 
-static int field_dispatch(const FieldParams& p, int which, void* stream) {
+template <int TAPS>
+static int field_dispatch_taps(const FieldParams& p, int which, void* stream) {
     switch (p.grid.n_features) {
-        case 2: return launch_field<2>(p, which, as_stream(stream));
-        case 4: return launch_field<4>(p, which, as_stream(stream));
-        default: return launch_field<8>(p, which, as_stream(stream));
+        case 2: return launch_field<2, TAPS>(p, which, as_stream(stream));
+        case 4: return launch_field<4, TAPS>(p, which, as_stream(stream));
+        default: return launch_field<8, TAPS>(p, which, as_stream(stream));
     }
+}
+static int field_dispatch(const FieldParams& p, int which, void* stream) {
+    return p.taps == 4 ? field_dispatch_taps<4>(p, which, stream) : field_dispatch_taps<6>(p, which, stream);
 }
 
 static int check_fwd(const FieldParams& p, int which) {

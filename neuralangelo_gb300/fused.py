@@ -24,6 +24,7 @@ Kernels per step (all on the current stream):
 """
 import ctypes
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -44,7 +45,8 @@ class FieldArgs(ctypes.Structure):
                 ("d_table", c_vp), ("d_pre0", c_vp), ("x0ext", c_vp), ("d_enc", c_vp), ("d_whead", c_vp),
                 ("d_bhead", c_vp),
                 ("err", c_vp), ("d_w0", c_vp), ("h0c_lo", c_vp), ("xc_lo", c_vp), ("d_pre0_lo", c_vp),
-                ("d_table_scale_dev", c_vp), ("found_inf", c_vp)]
+                ("d_table_scale_dev", c_vp), ("found_inf", c_vp),
+                ("taps", c_i32), ("pad_taps", c_i32)]
 
 
 class RenderArgs(ctypes.Structure):
@@ -202,8 +204,11 @@ class FusedField:
         self.H = cfg.sdf.mlp.hidden_dim
         if self.H != 256:
             raise ValueError("the fused field is built for SDF hidden width 256")
-        if cfg.sdf.gradient.taps != 6 or cfg.sdf.gradient.mode != "numerical":
-            raise ValueError("the fused field implements the 6-tap numerical gradient")
+        if cfg.sdf.gradient.taps not in (4, 6) or cfg.sdf.gradient.mode != "numerical":
+            raise ValueError("the fused field implements the 6- and 4-tap numerical gradients")
+        self.taps = int(cfg.sdf.gradient.taps)
+        # samples per 128-row tile and rows used: 18 x 7 (6 taps) or 25 x 5 (4 taps)
+        self.spt, self.tile_rows = (18, 126) if self.taps == 6 else (25, 125)
         if cfg.sdf.mlp.skip or cfg.sdf.mlp.num_layers != 1:
             raise ValueError("the fused field implements the one-hidden-layer SDF MLP of the reference config")
         rgb = cfg.rgb
@@ -331,7 +336,7 @@ class FusedField:
         if self.ws is not None and self.ws['key'] == key:
             return self.ws
         self.ws = None                      # release the previous shape's buffers first
-        rows0 = (Ns + 17) // 18 * 126      # layer-0 rows: 18 samples x 7 evaluations per tile
+        rows0 = (Ns + self.spt - 1) // self.spt * self.tile_rows      # layer-0 rows, tile-major
         f16, f32 = torch.float16, torch.float32
         e = lambda *s, dt=f32: torch.empty(*s, device=device, dtype=dt)  # noqa: E731
         Hc = self.Hc
@@ -456,9 +461,18 @@ class FusedField:
         fa.table, fa.w0e, fa.w0b = _p(pk['table']), _p(pk['w0e']), _p(pk['w0b'])
         fa.w0x, fa.b0, fa.whead, fa.bhead = _p(pk['w0x']), _p(pk['b0']), _p(pk['whead']), _p(pk['bhead'])
         fa.beta = float(m.cfg.sdf.mlp.activ_params.beta)
-        fa.eps = eps
-        fa.two_eps = float(torch.tensor(2 * eps, dtype=torch.float32))
-        fa.eps2 = float(torch.tensor(eps ** 2, dtype=torch.float32))
+        fa.taps = self.taps
+        if self.taps == 6:
+            fa.eps = eps
+            fa.two_eps = float(torch.tensor(2 * eps, dtype=torch.float32))
+            fa.eps2 = float(torch.tensor(eps ** 2, dtype=torch.float32))
+        else:
+            # the tetrahedral stencil's displacement and denominators as the reference forms them
+            # (modules.py:158-174): eps / sqrt(3) in double, then float32 scalars
+            e = eps / float(np.sqrt(3.0))
+            fa.eps = e
+            fa.two_eps = float(torch.tensor(4.0 * e, dtype=torch.float32))
+            fa.eps2 = float(torch.tensor(e ** 2, dtype=torch.float32))
         fa.outside_val = float(m.outside_val)
         fa.xc, fa.ldxc = _p(ws['xc']), self.Kc0
         fa.app_dim, fa.app_table = self.app_dim, _p(pk['app'])

@@ -336,9 +336,14 @@ def spherical_harmonics(d):
         _SH_C3[5] * z * (xx - yy), _SH_C3[6] * x * (xx - 3 * yy)], dim=-1).to(torch.float32).to(d.dtype)
 
 
-def neural_rgb(p, cfg, pts, normals, rays_unit, feats, app):
+def neural_rgb(p, cfg, pts, normals, rays_unit, feats, app, gates=None):
     """NeuralRGB.forward (modules.py:209-220) with MLPwithSkipConnection (nerf_util.py:187-196):
-    input [x, SH(d), n, feat, app], ReLU hidden layers, sigmoid output."""
+    input [x, SH(d), n, feat, app], ReLU hidden layers, sigmoid output.
+
+    gates (test diagnostics only): per hidden layer a {0, 1} tensor shaped like its output,
+    used in place of the ReLU's own [h > 0].  A pre-activation within rounding of zero takes
+    either side in two valid computations; feeding the gates another computation took
+    compares the rest of the arithmetic across that discontinuity."""
     st = cfg.get('fp16_storage', False)
     parts = [pts, spherical_harmonics(rays_unit), normals, feats]
     if app is not None:
@@ -349,7 +354,7 @@ def neural_rgb(p, cfg, pts, normals, rays_unit, feats, app):
         W = weight_norm(p[f'rgb.l{i}.v'], p[f'rgb.l{i}.g'])
         h = h @ W.t() + p[f'rgb.l{i}.b']
         if i != n - 1:
-            h = fp16_store(torch.relu(h), st)
+            h = fp16_store(h * gates[i].to(h.dtype) if gates is not None else torch.relu(h), st)
     return torch.sigmoid(h)
 
 
@@ -439,7 +444,10 @@ def render_step(p, cfg, layout, batch, eps, progress, w_eik, w_curv, training=Tr
     app = None
     if cfg['app_dim'] > 0:
         app = p['app'][batch['app_idx']][:, None, :].expand(R, N, cfg['app_dim'])
-    rgbs = neural_rgb(p, cfg, pts, normals, rays, feat, app)
+    gates = batch.get('rgb_gates')
+    if gates is not None:
+        gates = [g.reshape(R, N, -1) for g in gates]
+    rgbs = neural_rgb(p, cfg, pts, normals, rays, feat, app, gates)
     alphas = neus_alphas(d, sdf[..., 0], grads, dists, batch['far'], p['s_var'], progress, cfg['anneal_end'])
     rgbs_all, alphas_all = rgbs, alphas
     if cfg.get('bg_enabled') and batch.get('dists_bg') is not None:     # model.py:129-134
@@ -499,10 +507,15 @@ def render_step_ragged(p, cfg, layout, batch, eps, progress, w_eik, w_curv, mean
             continue
         idx = torch.tensor(rays)
         d = torch.stack([batch['dists'][offs[r]:offs[r + 1]] for r in rays])
+        gates = None
+        if batch.get('rgb_gates') is not None:          # flat per-sample rows -> this group's rays
+            rows = torch.cat([torch.arange(int(offs[r]), int(offs[r + 1])) for r in rays])
+            gates = [g[rows] for g in batch['rgb_gates']]
         sub = dict(center=batch['center'][idx], ray_unit=batch['ray_unit'][idx], dists=d,
                    far=batch['far'][idx], outside=batch['outside'][idx], target=batch['target'][idx],
                    app_idx=batch['app_idx'][idx] if batch.get('app_idx') is not None else None,
-                   dists_bg=batch['dists_bg'][idx] if batch.get('dists_bg') is not None else None)
+                   dists_bg=batch['dists_bg'][idx] if batch.get('dists_bg') is not None else None,
+                   rgb_gates=gates)
         out = render_step(p, cfg, layout, sub, eps, progress, w_eik, w_curv)
         ins = (~sub['outside']).to(dt).expand(len(rays), n)
         eik = ((out['grads'].norm(dim=-1) - 1.0) ** 2).nan_to_num(nan=0.0, posinf=0.0, neginf=0.0)
