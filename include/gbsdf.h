@@ -136,6 +136,8 @@ int gbsdf_composite_weights_bwd(int64_t R, int64_t N, const float* alpha, const 
  * The split pair carries a gradient through the colour MLP's input-gradient
  * chain at ~2^-22 relative precision on the fp16 tensor cores.  err:
  * optional device int set non-zero when a bounded device wait runs out. */
+/* Device workspace of gbsdf_dense: 0 bytes (the tiles are staged in shared memory). */
+size_t gbsdf_dense_workspace_size(int64_t M, int K, int N);
 int gbsdf_dense(int64_t M, int K, int N, const void* X, const void* Xlo, int ldx, const void* W,
                 const float* bias, const void* G, int ldg, void* Y, void* Ylo, int ldy, int y_f32, int epi,
                 float beta, int* err, void* stream);
@@ -218,7 +220,29 @@ typedef struct gbsdf_field_args {
                                 eps2 = eps^2.  x0ext, d_enc and d_pre0 hold ceil(Ns / samples per tile)
                                 tiles of rows. */
     int32_t pad_taps;
+    unsigned long long* d_table_fix;  /* optional int64 [entries, F]: deterministic table scatter.  Each
+                                         contribution is added as a 64-bit fixed-point integer (48
+                                         fraction bits) with integer atomics, whose sum does not depend
+                                         on the order they land in, then added into d_table: two runs
+                                         give bit-identical table gradients (|sum| < 2^15).  The call
+                                         clears the buffer itself.  NULL: FP32 vector atomics. */
 } gbsdf_field_args;
+
+/* Sizes of the caller-owned buffers of the field calls for Ns samples, K0 encoder columns, a
+ * tap count (6, 4, or 0 = 6) and the deterministic scatter (grid needed then).  The calls
+ * allocate nothing; a caller sizes x0ext, d_enc, d_w0 / d_pre0 (and d_pre0_lo) and d_table_fix
+ * from these.  The colour-input, h0c and per-sample output buffers are [Ns, ...] as declared
+ * in gbsdf_field_args. */
+typedef struct gbsdf_field_workspace {
+    int64_t rows;              /* rows of x0ext, d_enc and d_pre0: tiles x 126 (6 taps) or x 125 (4 taps) */
+    size_t x0ext_bytes;        /* fp16 [rows, 2 K0 + 16] */
+    size_t d_enc_bytes;        /* fp32 [rows, K0] */
+    size_t d_w0_bytes;         /* fp32 [256, K0 + 16] when K0 <= 64 (in-kernel layer-0 weight gradient), else 0 */
+    size_t d_pre0_bytes;       /* fp16 [rows, 256] for d_pre0 and again for d_pre0_lo when K0 > 64, else 0 */
+    size_t d_table_fix_bytes;  /* int64 [entries, F] for the deterministic scatter, else 0 */
+} gbsdf_field_workspace;
+int gbsdf_field_workspace_size(int64_t Ns, int32_t K0, int32_t taps, int32_t deterministic,
+                               const gbsdf_grid* grid, gbsdf_field_workspace* out);
 
 size_t gbsdf_field_args_size(void);
 /* Forward: hash-grid gather of the 7 evaluations into x0ext, then the MLP forward
@@ -297,6 +321,10 @@ typedef struct gbsdf_render_args {
 
 size_t gbsdf_render_args_size(void);
 int gbsdf_render_fused(const gbsdf_render_args* args, void* stream);
+/* Device workspace of gbsdf_render_fused for R rays of S samples (0: ragged) and n_bg
+ * background samples: 0 bytes -- a ray's alphas and transmittances live in its warp's shared
+ * memory (up to 512 samples), every other buffer is an argument. */
+size_t gbsdf_render_workspace_size(int64_t R, int32_t S, int32_t n_bg);
 
 /* Last colour layer (H -> 3, sigmoid) forward: rgbs = sigmoid(Y W^T + b).
  * Replaces the last Linear + sigmoid of NeuralRGB (modules.py:215, nerf_util.py:187-196).
@@ -443,6 +471,14 @@ int gbsdf_sampler_round(const gbsdf_sampler_args* args, void* stream);
  * constant 1.  err: device flag set when a bounded wait times out (may be NULL). */
 int gbsdf_wgrad(int64_t M, int N, int K, const void* dZ, const void* dZ_lo, int ldz, const void* X, int ldx,
                 float* dW, int ldw, int accumulate, int* err, void* stream);
+
+/* Self-test of the bounded waits (no counterpart in the reference): one GPU thread waits on an
+ * mbarrier with the limit timeout_ns (0 to 2 s); nothing arrives on it unless arrive_first.
+ * status [2] int32 (device): status[0] = 1 when the wait ran out, 0 when it completed;
+ * status[1] = the wait's wall time in microseconds.  Every kernel's waits on TMA, MMA and
+ * pipeline barriers end the same way: after the limit they set the caller's err flag and the
+ * kernel returns, so a stalled pipeline surfaces as a status instead of a hung GPU. */
+int gbsdf_selftest_wait(int64_t timeout_ns, int arrive_first, int* status, void* stream);
 
 #ifdef __cplusplus
 }

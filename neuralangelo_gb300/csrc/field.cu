@@ -132,6 +132,24 @@ __device__ __forceinline__ void write_tile_features(uint8_t* a_s, uint8_t* a2_s,
     write_half_row<F>(a2_s + off, lo);
 }
 
+// Deterministic mode: each contribution as a 64-bit fixed-point integer with DET_FRAC_BITS
+// fraction bits, added with integer atomics.  Integer addition is associative, so the sums
+// do not depend on the order the atomics land in: two runs give bit-identical results.
+constexpr int DET_FRAC_BITS = 48;
+template <int F>
+__device__ __forceinline__ void scatter_add_fixed(unsigned long long* dst, const float* v) {
+#pragma unroll
+    for (int f = 0; f < F; ++f)
+        if (v[f] != 0.0f) atomicAdd(dst + f, (unsigned long long)__float2ll_rn(v[f] * 0x1p48f));
+}
+
+__global__ void k_fixed_to_table(int64_t n, const unsigned long long* __restrict__ fix, float* __restrict__ d_table) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const long long q = (long long)fix[i];
+    if (q != 0) d_table[i] += (float)((double)q * 0x1p-48);
+}
+
 template <int F>
 __device__ __forceinline__ void scatter_add(float* dst, const float* v) {
     if constexpr (F == 8) {
@@ -222,7 +240,7 @@ __global__ void __launch_bounds__(256, 6) k_field_gather(FieldParams p, int64_t 
 // are read again per pass, from L1): fewer accumulator registers, more resident warps.
 constexpr int SCATTER_CPT = 2;
 
-template <int F, int CPT, int TAPS>
+template <int F, int CPT, int TAPS, bool DET>
 __global__ void __launch_bounds__(256, CPT >= 8 ? 2 : (CPT == 4 ? 3 : 4)) k_field_scatter(FieldParams p) {
     constexpr int EVALS = TapTile<TAPS>::EVALS, SPT = TapTile<TAPS>::SPT;
     const int A = p.active, K0 = p.K0;
@@ -238,6 +256,7 @@ __global__ void __launch_bounds__(256, CPT >= 8 ? 2 : (CPT == 4 ? 3 : 4)) k_fiel
     sample_point(p, s, c);
     const LevelDesc d = level_desc(p.grid, l);
     float* base = p.d_table + d.offset * F;
+    unsigned long long* fbase = DET ? p.d_table_fix + d.offset * F : nullptr;
     const float gscale = p.d_table_scale_dev ? *p.d_table_scale_dev : (p.d_table_scale != 0.0f ? p.d_table_scale : 1.0f);
     bool nonfinite = false;
     const int lane = threadIdx.x & 31;
@@ -292,7 +311,10 @@ __global__ void __launch_bounds__(256, CPT >= 8 ? 2 : (CPT == 4 ? 3 : 4)) k_fiel
                     grid_index(d, bx + (corner & 1), by + ((corner >> 1) & 1), bz + ((corner >> 2) & 1));
                 const float w = corner_weight(corner, fx, fy, fz) * gscale;
                 if (idx != pidx[cc]) {
-                    if (pidx[cc] != 0xffffffffu) scatter_add<F>(base + (uint64_t)pidx[cc] * F, pacc[cc]);
+                    if (pidx[cc] != 0xffffffffu) {
+                        if constexpr (DET) scatter_add_fixed<F>(fbase + (uint64_t)pidx[cc] * F, pacc[cc]);
+                        else scatter_add<F>(base + (uint64_t)pidx[cc] * F, pacc[cc]);
+                    }
                     pidx[cc] = idx;
 #pragma unroll
                     for (int f = 0; f < F; ++f) pacc[cc][f] = 0.0f;
@@ -322,7 +344,10 @@ __global__ void __launch_bounds__(256, CPT >= 8 ? 2 : (CPT == 4 ? 3 : 4)) k_fiel
                     }
                 }
             }
-            if (mine) scatter_add<F>(base + (uint64_t)pidx[cc] * F, pacc[cc]);
+            if (mine) {
+                if constexpr (DET) scatter_add_fixed<F>(fbase + (uint64_t)pidx[cc] * F, pacc[cc]);
+                else scatter_add<F>(base + (uint64_t)pidx[cc] * F, pacc[cc]);
+            }
         }
     }
     if (nonfinite && p.found_inf) *p.found_inf = 1.0f;     // any writer stores the same value
@@ -1316,7 +1341,19 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
     }
     if (which & FK_SCATTER) {
         const int64_t items = p.Ns * p.active;
-        k_field_scatter<F, SCATTER_CPT, TAPS><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p);
+        if (p.d_table_fix) {
+            // deterministic mode: integer accumulation into the caller's buffer, then into d_table
+            const int64_t n = (int64_t)p.grid.offset[p.grid.n_levels] * F;
+            if (cudaMemsetAsync(p.d_table_fix, 0, (size_t)n * 8, s) != cudaSuccess) {
+                set_error("clearing d_table_fix failed");
+                return GBSDF_ERR_CUDA;
+            }
+            k_field_scatter<F, SCATTER_CPT, TAPS, true><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p);
+            if (int st = launch_status("field scatter (deterministic)")) return st;
+            k_fixed_to_table<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, p.d_table_fix, p.d_table);
+        } else {
+            k_field_scatter<F, SCATTER_CPT, TAPS, false><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p);
+        }
         if (int st = launch_status("field scatter")) return st;
     }
     return GBSDF_OK;
@@ -1388,7 +1425,10 @@ static int check_bwd(const FieldParams& p, int which) {
         GBSDF_CHECK_ARG(aligned(p.d_h0c, 16), "d_h0c alignment");
         GBSDF_CHECK_ARG(!p.d_pre0_lo || aligned(p.d_pre0_lo, 16), "d_pre0_lo alignment");
     }
-    if (which & FK_SCATTER) GBSDF_CHECK_ARG(p.d_table && aligned(p.d_table, 16), "d_table missing or misaligned");
+    if (which & FK_SCATTER) {
+        GBSDF_CHECK_ARG(p.d_table && aligned(p.d_table, 16), "d_table missing or misaligned");
+        GBSDF_CHECK_ARG(!p.d_table_fix || aligned(p.d_table_fix, 16), "d_table_fix misaligned");
+    }
     return GBSDF_OK;
 }
 
@@ -1419,6 +1459,25 @@ extern "C" int gbsdf_field_mlp_bwd(const gbsdf_field_args* params, void* stream)
 }
 extern "C" int gbsdf_field_scatter(const gbsdf_field_args* params, void* stream) {
     return field_call(params, FK_SCATTER, stream);
+}
+
+extern "C" int gbsdf_field_workspace_size(int64_t Ns, int32_t K0, int32_t taps, int32_t deterministic,
+                                          const gbsdf_grid* grid, gbsdf_field_workspace* out) {
+    clear_error();
+    GBSDF_CHECK_ARG(out != nullptr && Ns >= 0, "bad arguments");
+    GBSDF_CHECK_ARG(K0 % 16 == 0 && K0 >= 16 && K0 <= 128, "K0 %d", K0);
+    GBSDF_CHECK_ARG(taps == 0 || taps == 4 || taps == 6, "taps %d", taps);
+    GBSDF_CHECK_ARG(!deterministic || grid != nullptr, "the deterministic scatter's size needs the grid");
+    const int spt = taps == 4 ? TapTile<4>::SPT : TapTile<6>::SPT;
+    const int rows_per_tile = taps == 4 ? TapTile<4>::ROWS : TapTile<6>::ROWS;
+    const int64_t rows = (Ns + spt - 1) / spt * rows_per_tile;
+    out->rows = rows;
+    out->x0ext_bytes = (size_t)rows * (2 * K0 + 16) * 2;
+    out->d_enc_bytes = (size_t)rows * K0 * 4;
+    out->d_w0_bytes = K0 <= 64 ? (size_t)HID * (K0 + 16) * 4 : 0;
+    out->d_pre0_bytes = K0 > 64 ? (size_t)rows * HID * 2 : 0;
+    out->d_table_fix_bytes = deterministic ? (size_t)grid->offset[grid->n_levels] * grid->n_features * 8 : 0;
+    return GBSDF_OK;
 }
 
 extern "C" int gbsdf_sdf_points(const gbsdf_field_args* params, int64_t M, const float* pts, const float* ax,

@@ -501,3 +501,8 @@ extern "C" int gbsdf_app_grad(int64_t R, int32_t S, const int64_t* ray_offsets, 
         R, S, ray_offsets, app_idx, (const float*)d_xc, ld_dxc, col0, app_dim, d_app);
     return launch_status("app_grad");
 }
+
+extern "C" size_t gbsdf_render_workspace_size(int64_t R, int32_t S, int32_t n_bg) {
+    (void)R; (void)S; (void)n_bg;
+    return 0;
+}

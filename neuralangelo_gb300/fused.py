@@ -46,7 +46,13 @@ class FieldArgs(ctypes.Structure):
                 ("d_bhead", c_vp),
                 ("err", c_vp), ("d_w0", c_vp), ("h0c_lo", c_vp), ("xc_lo", c_vp), ("d_pre0_lo", c_vp),
                 ("d_table_scale_dev", c_vp), ("found_inf", c_vp),
-                ("taps", c_i32), ("pad_taps", c_i32)]
+                ("taps", c_i32), ("pad_taps", c_i32), ("d_table_fix", c_vp)]
+
+
+class FieldWorkspace(ctypes.Structure):
+    _fields_ = [("rows", c_i64), ("x0ext_bytes", ctypes.c_size_t), ("d_enc_bytes", ctypes.c_size_t),
+                ("d_w0_bytes", ctypes.c_size_t), ("d_pre0_bytes", ctypes.c_size_t),
+                ("d_table_fix_bytes", ctypes.c_size_t)]
 
 
 class RenderArgs(ctypes.Structure):
@@ -68,6 +74,7 @@ for _name in ("gbsdf_field_fwd", "gbsdf_field_bwd", "gbsdf_field_encode", "gbsdf
               "gbsdf_field_mlp_bwd", "gbsdf_field_scatter"):
     _lib.register(_name, [c_vp, c_vp])
 _lib.register("gbsdf_render_fused", [c_vp, c_vp])
+_lib.register("gbsdf_field_workspace_size", [c_i64, c_i32, c_i32, c_i32, c_vp, c_vp])
 _lib.register("gbsdf_rgb_head_fwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp])
 _lib.register("gbsdf_rgb_head_bwd", [c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
                                      c_vp])
@@ -175,9 +182,12 @@ class FusedField:
     """Fused FP16 forward+backward over a FieldModel's FP32 master parameters."""
 
     def __init__(self, model, loss_scale=2.0 ** 15, split_colour_grads=False, fused_w0_grad=True,
-                 activation_pairs=True, dynamic_loss_scale=True, growth_interval=2000):
+                 activation_pairs=True, dynamic_loss_scale=True, growth_interval=2000, deterministic_table=False):
         check_struct_sizes()
         self.model = model
+        # the table gradient through the order-independent fixed-point scatter (bit-identical
+        # across runs; an int64 buffer of the table's size besides the FP32 gradient)
+        self.deterministic = bool(deterministic_table)
         # dynamic loss scaling: the scale, the schedule scalars and the overflow flag in one device
         # buffer (created at the first step): [0] loss scale, [1] anneal, [2] curvature weight,
         # [3] 1 / loss scale, [4] found_inf; an int32 growth tracker beside it
@@ -332,11 +342,17 @@ class FusedField:
         return self.fused_w0_grad and self.K0 <= 64
 
     def _workspace(self, R, S, Ns, device):
-        key = (R, S, Ns, self.K0, self.bg, self.pairs)
+        key = (R, S, Ns, self.K0, self.bg, self.pairs, self.deterministic)
         if self.ws is not None and self.ws['key'] == key:
             return self.ws
         self.ws = None                      # release the previous shape's buffers first
-        rows0 = (Ns + self.spt - 1) // self.spt * self.tile_rows      # layer-0 rows, tile-major
+        # the caller-owned buffers of the field calls, sized by the library
+        wsz = FieldWorkspace()
+        lay = self.model.neural_sdf.tcnn_encoding.layout
+        _lib.call("gbsdf_field_workspace_size", Ns, self.K0, self.taps, 1 if self.deterministic else 0,
+                  ctypes.byref(lay.struct), ctypes.byref(wsz))
+        rows0 = int(wsz.rows)                                        # layer-0 rows, tile-major
+        assert rows0 == (Ns + self.spt - 1) // self.spt * self.tile_rows
         f16, f32 = torch.float16, torch.float32
         e = lambda *s, dt=f32: torch.empty(*s, device=device, dtype=dt)  # noqa: E731
         Hc = self.Hc
@@ -358,7 +374,9 @@ class FusedField:
                   x0ext=e(rows0, 2 * self.K0 + 16, dt=f16), d_enc=e(rows0, self.K0),
                   d_whead=torch.zeros(256, device=device),
                   d_bhead=torch.zeros(1, device=device), d_bl=torch.zeros(3, device=device),
-                  err=torch.zeros(1, device=device, dtype=torch.int32))
+                  err=torch.zeros(1, device=device, dtype=torch.int32),
+                  d_table_fix=(torch.empty(wsz.d_table_fix_bytes // 8, device=device, dtype=torch.int64)
+                               if self.deterministic else None))
         if self.pairs:
             # low halves, with the row strides of their hi buffers (the constant-1 column's lo is 0)
             ws.update(h0c_lo=e(Ns, 264, dt=f16).zero_(), xc_lo=e(Ns, self.Kc0, dt=f16),
@@ -609,6 +627,7 @@ class FusedField:
         fa.d_h0c = _p(ws['d_h0c'])
         fa.d_table, fa.d_pre0, fa.d_enc = _p(d_table), _p(ws['d_pre0']), _p(ws['d_enc'])
         fa.d_pre0_lo = _p(ws['d_pre0_lo'])
+        fa.d_table_fix = _p(ws['d_table_fix'])
         fa.d_whead, fa.d_bhead = _p(ws['d_whead']), _p(ws['d_bhead'])
         if ws['d_w0'] is not None:
             ws['d_w0'].zero_()

@@ -101,3 +101,28 @@ def test_field_backward_weight_gradient_arguments_without_gpu(lib):
     a.d_pre0 = 8                                   # misaligned
     assert lib.gbsdf_field_mlp_bwd(ctypes.byref(a), None) == 1
     assert b"d_pre0" in lib.gbsdf_last_error()
+
+
+def test_workspace_size_queries(lib):
+    """The field calls' caller-owned buffers are sized by the library: rows are whole tiles of
+    18 samples x 7 evaluations (6 taps) or 25 x 5 (4 taps); render and dense need none."""
+    from neuralangelo_gb300.encoding import GridLayout
+    from neuralangelo_gb300.fused import FieldWorkspace
+    lay = GridLayout(8, 4, 16, 16, 1.5)
+    for taps, rows in ((6, 6 * 126), (0, 6 * 126), (4, 4 * 125)):
+        w = FieldWorkspace()
+        assert lib.gbsdf_field_workspace_size(ctypes.c_int64(100), 32, taps, 1, ctypes.byref(lay.struct),
+                                              ctypes.byref(w)) == 0
+        assert w.rows == rows
+        assert w.x0ext_bytes == rows * (2 * 32 + 16) * 2 and w.d_enc_bytes == rows * 32 * 4
+        assert w.d_w0_bytes == 256 * 48 * 4 and w.d_pre0_bytes == 0
+        assert w.d_table_fix_bytes == int(lay.struct.offset[8]) * 4 * 8
+    w = FieldWorkspace()
+    assert lib.gbsdf_field_workspace_size(ctypes.c_int64(1000), 80, 6, 0, None, ctypes.byref(w)) == 0
+    assert w.d_w0_bytes == 0 and w.d_pre0_bytes == w.rows * 256 * 2 and w.d_table_fix_bytes == 0
+    assert lib.gbsdf_field_workspace_size(ctypes.c_int64(10), 32, 5, 0, None, ctypes.byref(w)) == 1
+    assert b"taps" in lib.gbsdf_last_error()
+    lib.gbsdf_render_workspace_size.restype = ctypes.c_size_t
+    lib.gbsdf_dense_workspace_size.restype = ctypes.c_size_t
+    assert lib.gbsdf_render_workspace_size(ctypes.c_int64(16384), 128, 32) == 0
+    assert lib.gbsdf_dense_workspace_size(ctypes.c_int64(1 << 21), 256, 256) == 0

@@ -595,3 +595,21 @@ def test_fused_4_taps_matches_plain():
     assert abs(res['loss'] - ref_loss) < 2e-3 * abs(ref_loss)
     for k in ('table', 'sdf.l0.v', 'sdf.l1.v', 'rgb.l0.v', 's_var'):
         assert rel(mine[k], ref[k]) < 2e-2, k
+
+
+def test_deterministic_table_scatter():
+    """The fixed-point table scatter: two runs give bit-identical table gradients, and they
+    agree with the FP32-atomics path up to its summation order."""
+    model = build()
+    batch = make_rays(64, 32, seed=2, miss_frac=0.1, n_images=10, device=DEV)
+    tabs = []
+    for det in (True, True, False):
+        ff = FusedField(model, deterministic_table=det)
+        model.zero_grad(set_to_none=True)
+        ff.step(batch)
+        torch.cuda.synchronize()
+        tabs.append(model.neural_sdf.tcnn_encoding.params.grad.clone())
+    assert torch.equal(tabs[0], tabs[1])
+    e = rel(tabs[0].cpu(), tabs[2].cpu())
+    print(f"\ndeterministic vs atomics: {e:.1e}")
+    assert e < 1e-6
