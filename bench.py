@@ -77,15 +77,20 @@ GATHER_SCATTER = ("gbsdf_field_encode", "gbsdf_field_scatter")
 def bench_ragged(model, device, steps, warmup, rays=65536, seed=0):
     """Ragged batching: 65536 rays, 30% culled to zero samples, the rest 16..256 samples
     (6.2M samples), the fused step captured in one CUDA graph; against the same rays in
-    the reference's dense layout padded to 128 samples (8.4M samples, misses computed)."""
+    the reference's dense layout padded to 128 samples (8.4M samples, misses computed); and
+    the ragged step again with the launch shapes autotune.StepTuner chose for it."""
     import torch
     from neuralangelo_gb300.fused import CapturedStep, FusedField
     from neuralangelo_gb300.workloads import make_ragged_rays, padded
     rag = make_ragged_rays(rays, seed=seed, n_images=100, device=device)
     useful = int(rag['dists'].numel())
     out = dict(rays=rays, useful_samples=useful)
-    for name, b in (("padded_128", padded(rag, 128, seed=seed)), ("ragged", rag)):
+    tuned = None
+    for name, b in (("padded_128", padded(rag, 128, seed=seed)), ("ragged", rag), ("ragged_tuned", rag)):
         ff = FusedField(model)
+        if name == "ragged_tuned":
+            from neuralangelo_gb300.autotune import StepTuner
+            tuned = StepTuner(ff, reps=3).tune(b)
         ns = int(b['dists'].numel())
         if name == "ragged":   # eager launches, for the graph's benefit
             ms_e = time_steps(lambda: ff.step(b, compute_loss=False), steps, warmup, lambda: None)
@@ -99,6 +104,8 @@ def bench_ragged(model, device, steps, warmup, rays=65536, seed=0):
         ff.release()
         torch.cuda.empty_cache()
     out["speedup_vs_padded"] = round(out["padded_128"]["ms_per_step"] / out["ragged"]["ms_per_step"], 3)
+    out["tuning"] = tuned                      # autotune.StepTuner's launch shapes for this workload
+    out["tuned_vs_default"] = round(out["ragged"]["ms_per_step"] / out["ragged_tuned"]["ms_per_step"], 3)
     return out
 
 

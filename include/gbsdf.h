@@ -136,6 +136,11 @@ int gbsdf_composite_weights_bwd(int64_t R, int64_t N, const float* alpha, const 
  * The split pair carries a gradient through the colour MLP's input-gradient
  * chain at ~2^-22 relative precision on the fp16 tensor cores.  err:
  * optional device int set non-zero when a bounded device wait runs out. */
+/* Launch shape of gbsdf_dense for layers of K input and N output columns (a tuning choice;
+ * results are unchanged): n_tile output columns per CTA (64, 128 or 256; 0 = the built-in
+ * rule) and ring slots of the A pipeline (3 to 6, capped by shared memory; 0 = as many as fit).
+ * A small process-wide table (32 shapes); set it before launches that should use it. */
+int gbsdf_dense_tune(int K, int N, int n_tile, int nslots);
 /* Device workspace of gbsdf_dense: 0 bytes (the tiles are staged in shared memory). */
 size_t gbsdf_dense_workspace_size(int64_t M, int K, int N);
 int gbsdf_dense(int64_t M, int K, int N, const void* X, const void* Xlo, int ldx, const void* W,
@@ -226,6 +231,9 @@ typedef struct gbsdf_field_args {
                                          on the order they land in, then added into d_table: two runs
                                          give bit-identical table gradients (|sum| < 2^15).  The call
                                          clears the buffer itself.  NULL: FP32 vector atomics. */
+    /* Launch shapes (tuning choices, results unchanged; 0 = the built-in default): */
+    int32_t scatter_cpt;     /* table corners per pass of the scatter for 8-feature fields: 2, 4 or 8 */
+    int32_t fwd_ctas;        /* CTAs per SM launched for the MLP forward: 1 or 2 */
 } gbsdf_field_args;
 
 /* Sizes of the caller-owned buffers of the field calls for Ns samples, K0 encoder columns, a

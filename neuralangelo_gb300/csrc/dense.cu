@@ -42,6 +42,7 @@ struct DenseParams {
     float beta;
     int* err;
     int nslots;          // A-chunk slots of the shared-memory ring
+    int nslots_req;      // tuning: requested slots (0 = as many as fit)
     int tma_store;       // fp16 output written back through shared memory and TMA
 };
 
@@ -352,6 +353,7 @@ static int launch_dense(DenseParams p, cudaStream_t s) {
     p.tma_store = (N_TILE / 4 >= 32 && aligned(p.Y, 16) && p.ldy % (p.y_f32 ? 4 : 8) == 0 &&
                    dense_smem_slots(N_TILE, p.K, MIN_SLOTS, true) <= DENSE_SMEM_MAX) ? 1 : 0;
     p.nslots = dense_slots(N_TILE, p.K, p.tma_store != 0);
+    if (p.nslots_req >= MIN_SLOTS && p.nslots_req < p.nslots) p.nslots = p.nslots_req;
     const size_t smem = dense_smem_slots(N_TILE, p.K, p.nslots, p.tma_store != 0);
     if (smem > DENSE_SMEM_MAX) {
         set_error("dense layer K=%d N_TILE=%d needs %zu B of shared memory", p.K, N_TILE, smem);
@@ -401,7 +403,37 @@ int dense_launch(const DenseParams& p, int n_tile, cudaStream_t s) {
 
 }  // namespace gbsdf
 
+namespace gbsdf {
+// launch shapes chosen by a tuner, per (K, N); read by gbsdf_dense
+struct DenseTune {
+    int K, N, n_tile, nslots;
+};
+static DenseTune g_dense_tune[32];
+static int g_dense_tune_n = 0;
+static const DenseTune* dense_tune_find(int K, int N) {
+    for (int i = 0; i < g_dense_tune_n; ++i)
+        if (g_dense_tune[i].K == K && g_dense_tune[i].N == N) return &g_dense_tune[i];
+    return nullptr;
+}
+}  // namespace gbsdf
+
 using namespace gbsdf;
+
+extern "C" int gbsdf_dense_tune(int K, int N, int n_tile, int nslots) {
+    clear_error();
+    GBSDF_CHECK_ARG(n_tile == 0 || n_tile == 64 || n_tile == 128 || n_tile == 256, "n_tile %d", n_tile);
+    GBSDF_CHECK_ARG(nslots == 0 || (nslots >= MIN_SLOTS && nslots <= MAX_SLOTS), "nslots %d", nslots);
+    for (int i = 0; i < g_dense_tune_n; ++i) {
+        if (g_dense_tune[i].K == K && g_dense_tune[i].N == N) {
+            g_dense_tune[i].n_tile = n_tile;
+            g_dense_tune[i].nslots = nslots;
+            return GBSDF_OK;
+        }
+    }
+    GBSDF_CHECK_ARG(g_dense_tune_n < 32, "dense tuning table full");
+    g_dense_tune[g_dense_tune_n++] = DenseTune{K, N, n_tile, nslots};
+    return GBSDF_OK;
+}
 
 // Y[:, 0:N] = epi(X[:, 0:K] * W^T + b ; G), fp16 in/out, fp32 accumulate.
 // K multiple of 16 (<= 320), N multiple of 64; leading dimensions multiples of 8.
@@ -434,6 +466,12 @@ extern "C" int gbsdf_dense(int64_t M, int K, int N, const void* X, const void* X
     int n_tile = 128;
     while (n_tile > 64 && (dense_smem(n_tile, K, Xlo != nullptr) > DENSE_SMEM_MAX || N % n_tile != 0))
         n_tile >>= 1;
+    p.nslots_req = 0;
+    if (const DenseTune* t = dense_tune_find(K, N)) {
+        if (t->n_tile > 0 && N % t->n_tile == 0 && dense_smem(t->n_tile, K, Xlo != nullptr) <= DENSE_SMEM_MAX)
+            n_tile = t->n_tile;
+        p.nslots_req = t->nslots;
+    }
     p.n_split = N / n_tile;
     return dense_launch(p, n_tile, as_stream(stream));
 }

@@ -1278,7 +1278,8 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
             set_error("field forward needs %zu B of shared memory", smem);
             return GBSDF_ERR_UNSUPPORTED;
         }
-        int64_t grid = num_sms() * FWD_CTAS_PER_SM;
+        // p.fwd_ctas (a tuning choice): resident CTAs per SM to launch, 1 or 2 (0 = 2)
+        int64_t grid = num_sms() * (p.fwd_ctas == 1 ? 1 : FWD_CTAS_PER_SM);
         if (grid > ntiles) grid = ntiles;
         allow_max_smem(k_field_fwd<F, TAPS>);
         k_field_fwd<F, TAPS><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p);
@@ -1352,7 +1353,14 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
             if (int st = launch_status("field scatter (deterministic)")) return st;
             k_fixed_to_table<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, p.d_table_fix, p.d_table);
         } else {
-            k_field_scatter<F, SCATTER_CPT, TAPS, false><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(p);
+            // p.scatter_cpt (a tuning choice, 8-feature fields): table corners per pass, 2, 4 or 8 (0 = 2)
+            const unsigned blocks = (unsigned)((items + 255) / 256);
+            if (F == 8 && p.scatter_cpt == 4)
+                k_field_scatter<F, 4, TAPS, false><<<blocks, 256, 0, s>>>(p);
+            else if (F == 8 && p.scatter_cpt == 8)
+                k_field_scatter<F, 8, TAPS, false><<<blocks, 256, 0, s>>>(p);
+            else
+                k_field_scatter<F, SCATTER_CPT, TAPS, false><<<blocks, 256, 0, s>>>(p);
         }
         if (int st = launch_status("field scatter")) return st;
     }
@@ -1372,6 +1380,9 @@ static int check_field_weights(const FieldParams& p) {
 static int check_field(const FieldParams& p) {
     GBSDF_CHECK_ARG(p.Ns >= 0, "Ns < 0");
     GBSDF_CHECK_ARG(p.taps == 0 || p.taps == 4 || p.taps == 6, "taps %d (4 or 6; 0 means 6)", p.taps);
+    GBSDF_CHECK_ARG(p.scatter_cpt == 0 || p.scatter_cpt == 2 || p.scatter_cpt == 4 || p.scatter_cpt == 8,
+                    "scatter_cpt %d (2, 4 or 8; 0 = 2)", p.scatter_cpt);
+    GBSDF_CHECK_ARG(p.fwd_ctas >= 0 && p.fwd_ctas <= 2, "fwd_ctas %d (1 or 2; 0 = 2)", p.fwd_ctas);
     if (int st = check_field_weights(p)) return st;
     GBSDF_CHECK_ARG(p.S > 0 || p.sample_ray, "need S > 0 or sample_ray");
     GBSDF_CHECK_ARG(p.center && p.ray_unit && p.dists, "NULL ray pointer");

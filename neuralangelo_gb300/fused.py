@@ -46,7 +46,8 @@ class FieldArgs(ctypes.Structure):
                 ("d_bhead", c_vp),
                 ("err", c_vp), ("d_w0", c_vp), ("h0c_lo", c_vp), ("xc_lo", c_vp), ("d_pre0_lo", c_vp),
                 ("d_table_scale_dev", c_vp), ("found_inf", c_vp),
-                ("taps", c_i32), ("pad_taps", c_i32), ("d_table_fix", c_vp)]
+                ("taps", c_i32), ("pad_taps", c_i32), ("d_table_fix", c_vp), ("scatter_cpt", c_i32),
+                ("fwd_ctas", c_i32)]
 
 
 class FieldWorkspace(ctypes.Structure):
@@ -105,15 +106,22 @@ def _round16(n):
     return (n + 15) // 16 * 16
 
 
+# dense-layer calls of a step, recorded for the launch-shape tuner (autotune.py) when a list
+DENSE_CALLS = None
+
+
 def _dense(X, Wt, N, K, out, bias=None, epi=EPI_IDENTITY, beta=100.0, G=None, err=None, X_lo=None, out_lo=None):
     """out[:, :N] = epi((X + X_lo)[:, :K] @ Wt[:N, :K].T + bias ; G) on the tcgen05 kernel."""
     M = X.shape[0]
     _lib.TIMER.count_bytes("gbsdf_dense", M * (K * 2 * (2 if X_lo is not None else 1) + (N * 2 if G is not None else 0)
                                                + N * out.element_size() * (2 if out_lo is not None else 1)))
-    _lib.call("gbsdf_dense", X.shape[0], K, N, c_vp(X.data_ptr()), c_vp(_p(X_lo)), X.stride(0),
-              c_vp(Wt.data_ptr()), c_vp(_p(bias)), c_vp(_p(G)), G.stride(0) if G is not None else 0,
-              c_vp(out.data_ptr()), c_vp(_p(out_lo)), out.stride(0), 1 if out.dtype == torch.float32 else 0,
-              int(epi), float(beta), c_vp(_p(err)), _lib.stream_ptr(X.device))
+    args = (X.shape[0], K, N, c_vp(X.data_ptr()), c_vp(_p(X_lo)), X.stride(0),
+            c_vp(Wt.data_ptr()), c_vp(_p(bias)), c_vp(_p(G)), G.stride(0) if G is not None else 0,
+            c_vp(out.data_ptr()), c_vp(_p(out_lo)), out.stride(0), 1 if out.dtype == torch.float32 else 0,
+            int(epi), float(beta), c_vp(_p(err)), _lib.stream_ptr(X.device))
+    if DENSE_CALLS is not None:
+        DENSE_CALLS.append(args)
+    _lib.call("gbsdf_dense", *args)
 
 
 def _wgrad(dZ, X, N, K, dW, accumulate=False, dZ_lo=None, err=None):
@@ -188,6 +196,8 @@ class FusedField:
         # the table gradient through the order-independent fixed-point scatter (bit-identical
         # across runs; an int64 buffer of the table's size besides the FP32 gradient)
         self.deterministic = bool(deterministic_table)
+        # launch shapes chosen by autotune.StepTuner (results unchanged): scatter_cpt, fwd_ctas
+        self.tuning = {}
         # dynamic loss scaling: the scale, the schedule scalars and the overflow flag in one device
         # buffer (created at the first step): [0] loss scale, [1] anneal, [2] curvature weight,
         # [3] 1 / loss scale, [4] found_inf; an int32 growth tracker beside it
@@ -499,6 +509,9 @@ class FusedField:
         fa.h0c_lo, fa.xc_lo = _p(ws['h0c_lo']), _p(ws['xc_lo'])
         fa.x0ext = _p(ws['x0ext'])
         fa.err = _p(ws['err'])
+        fa.scatter_cpt = int(self.tuning.get('scatter_cpt', 0))
+        fa.fwd_ctas = int(self.tuning.get('fwd_ctas', 0))
+        self._fa = fa                      # the field calls' arguments of the last step (the tuner re-issues them)
         # ---------------- forward ----------------
         _lib.call("gbsdf_field_encode", ctypes.byref(fa), stream)     # = gbsdf_field_fwd in two calls
         _lib.call("gbsdf_field_mlp_fwd", ctypes.byref(fa), stream)
