@@ -407,6 +407,9 @@ static unsigned head_blocks(int64_t Ns) {
 }
 
 // d_app[img(r)] += sum over ray r's samples of d_xc[s, col0:col0+D]; one warp per ray
+// D <= 32: lane = (row offset, dimension) with Dp = D rounded up to a power of two, so a
+// warp load covers 32 / Dp consecutive rows' D contiguous columns (coalesced); the row
+// lanes are then summed with shuffles.  Wider codes loop over the dimensions.
 __global__ void k_app_grad(int64_t R, int S, const int64_t* __restrict__ offs, const int* __restrict__ app_idx,
                            const float* __restrict__ d_xc, int ld, int col0, int D, float* __restrict__ d_app) {
     const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -414,6 +417,25 @@ __global__ void k_app_grad(int64_t R, int S, const int64_t* __restrict__ offs, c
     if (r >= R) return;
     const int64_t beg = S > 0 ? r * S : offs[r];
     const int64_t end = S > 0 ? beg + S : offs[r + 1];
+    if (D <= 32) {
+        int Dp = 1;
+        while (Dp < D) Dp <<= 1;
+        const int per = 32 / Dp, d = lane % Dp, ro = lane / Dp;
+        float acc0 = 0.0f, acc1 = 0.0f;
+        if (d < D) {
+            const float* col = d_xc + col0 + d;
+            int64_t s = beg + ro;
+            for (; s + per < end; s += 2 * per) {
+                acc0 += col[s * ld];
+                acc1 += col[(s + per) * ld];
+            }
+            if (s < end) acc0 += col[s * ld];
+        }
+        float acc = acc0 + acc1;
+        for (int off = Dp; off < 32; off <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+        if (ro == 0 && d < D && acc != 0.0f) atomicAdd(&d_app[(int64_t)app_idx[r] * D + d], acc);
+        return;
+    }
     for (int d = 0; d < D; ++d) {
         float acc = 0.0f;
         for (int64_t s = beg + lane; s < end; s += 32) acc += d_xc[s * ld + col0 + d];
