@@ -64,7 +64,7 @@ def profiled_traffic(kernel):
     return float(c["dram_bytes_per_sample"]), f"{c.get('kernel', kernel)}: {c['source']}", c.get("l2_throughput_pct")
 
 
-# kernels of this library launched by one call of each entry point (cuBLAS excluded)
+# kernels of this library launched by one call of each entry point
 KERNELS_PER_CALL = {"gbsdf_field_fwd": 2, "gbsdf_field_bwd": 2}   # others: 1
 
 

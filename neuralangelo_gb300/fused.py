@@ -781,7 +781,7 @@ class FusedField:
         dW0 = torch.zeros_like(l0.weight_v)
         gx = g['w0ext']      # columns: features hi | x,y,z hi, 1, x,y,z lo, 0 [| features lo]
         dW0[:, 3:3 + A * F] = gx[:, :A * F]
-        if gx.shape[1] > K0 + 16:                      # the GEMM path keeps the lo columns apart
+        if gx.shape[1] > K0 + 16:                      # the k_wgrad path keeps the lo columns apart
             dW0[:, 3:3 + A * F] += gx[:, K0 + 16:K0 + 16 + A * F]
         dW0[:, :3] = gx[:, K0:K0 + 3] + gx[:, K0 + 4:K0 + 7]
         db0 = gx[:, K0 + 3]

@@ -414,7 +414,7 @@ def test_c2_accuracy_report_512_rays():
 
 def test_in_kernel_layer0_weight_gradient_matches_gemm_path():
     """K0 <= 64: the backward kernel's own dW0 (TMEM accumulators, per-CTA atomics) against the
-    d_pre0 rows + GEMM path on the same step; every other gradient must agree as well."""
+    d_pre0 rows + k_wgrad path on the same step; every other gradient must agree as well."""
     model = build(seed=5)
     batch = make_rays(96, 64, seed=12, miss_frac=0.2, n_images=10, device=DEV)
     grads = []
