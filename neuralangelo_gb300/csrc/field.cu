@@ -687,6 +687,10 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     const uint32_t idesc1 = umma::idesc_f16(TILE_M, HID);
     const uint32_t idesc2 = umma::idesc_f16_bmn(TILE_M, K0);
     const uint32_t w_addr = umma::smem_u32(w_s);
+    // MMA2's and dW0's descriptors are built once per tile: a K = 16 step only moves the start
+    // address (bits 0-13, in 16-byte units, below 2^14 for any shared-memory address), so each
+    // MMA adds a multiple of a per-tile step
+    auto desc_step = [](uint32_t bytes) { return (uint64_t)(bytes >> 4); };
     // feature buffer b (0, or 1 with DW): selects, not arrays, which would go to local memory
     auto a_buf = [&](int b) { return b ? a_s1 : a_s0; };
     auto a3_buf = [&](int b) { return b ? a3_s1 : a3_s0; };
@@ -701,18 +705,23 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     float dbh = 0.0f;
     bool ok = true;
 
+    // the prologue runs on warp 1 (lane = sample of the tile), apart from warp 0's MMA issuer
+    static_assert(TapTile<TAPS>::SPT <= 32, "the prologue's samples fit one warp");
+    const int pl = tid - 32;
+    const bool pl_on = pl >= 0 && pl < SPT;
     // per-sample output gradients -> d f of each evaluation (modules.py:144-156), for
     // the next tile while this one is in flight, in three steps that keep the global
-    // loads off the tile's critical path: the per-sample loads at the top of the tile,
-    // the per-ray `outside` flag before MMA2, the arithmetic into df_s[buf] at the end
+    // loads and the arithmetic off the tile's critical path: the per-sample loads at the
+    // top of the tile, then, while MMA2 runs, the per-ray `outside` flag and the arithmetic
+    // into df_s[buf]
     struct PrologueIn {
         float g[3], dg[3], dh[3], n[3], dsdf;
         int r;
         bool out;
     };
     auto prologue_load = [&](int64_t tt, PrologueIn& in) {
-        const int64_t s = tt * SPT + tid;
-        if (tid < SPT && s < p.Ns) {
+        const int64_t s = tt * SPT + pl;
+        if (pl_on && s < p.Ns) {
             in.r = ray_of(p, s);
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
@@ -727,12 +736,12 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         }
     };
     auto prologue_ray = [&](int64_t tt, PrologueIn& in) {
-        const int64_t s = tt * SPT + tid;
-        if (tid < SPT && s < p.Ns) in.out = p.outside && p.outside[in.r];
+        const int64_t s = tt * SPT + pl;
+        if (pl_on && s < p.Ns) in.out = p.outside && p.outside[in.r];
     };
     auto prologue_finish = [&](int64_t tt, const PrologueIn& in, int buf) {
-        if (tid < SPT) {
-            const int64_t s = tt * SPT + tid;
+        if (pl_on) {
+            const int64_t s = tt * SPT + pl;
             float* dfb = df_s + buf * (EVALS * SPT);
             float df[EVALS];
 #pragma unroll
@@ -777,7 +786,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
             }
 #pragma unroll
             for (int e = 0; e < EVALS; ++e) {
-                dfb[e * SPT + tid] = df[e];
+                dfb[e * SPT + pl] = df[e];
                 dbh += df[e];
             }
         }
@@ -804,12 +813,15 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         }
         cp_async_commit();
     };
-    auto issue1 = [&](int buf) {
-        if (tid == 0) {
-            umma::fence_after_sync();
-            issue_tile_mma_strided(tmem, a3_addr(buf), KL, w_addr, KB, K0, idesc1);   // residuals first
-            issue_tile_mma(tmem, a_addr(buf), w_addr, KB, idesc1, true);
-            umma::mma_commit(mbar);
+    auto issue1 = [&](int buf) {                   // warp 0 converged: every call follows a CTA barrier
+        if (warp == 0) {
+            if (umma::elect_one()) {
+                umma::fence_after_sync();
+                issue_tile_mma_strided(tmem, a3_addr(buf), KL, w_addr, KB, K0, idesc1);   // residuals first
+                issue_tile_mma(tmem, a_addr(buf), w_addr, KB, idesc1, true);
+                umma::mma_commit(mbar);
+            }
+            __syncwarp();
         }
     };
     int64_t t = blockIdx.x;
@@ -826,10 +838,12 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     __syncthreads();
     if (t < ntiles) issue1(0);
     int it = 0;
+    // MMA completions: one thread polls the mbarrier and the CTA barrier (a lane shuffle for the
+    // per-warp lo wait) hands on its result
     for (; t < ntiles && ok; t += gridDim.x, ++it) {
         const int64_t s0 = t * SPT;
         cp_async_wait_group<0>();                    // this tile's d_h0c rows
-        ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
+        ok = __syncthreads_and(tid == 0 ? umma::mbar_wait(mbar, phase) : true);   // one poller
         phase ^= 1u;
         if (!ok) {
             flag_timeout(p.err, 1);
@@ -949,50 +963,52 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         // (3) d_enc = d_pre * W0e  (MMA2: A = d_pre [128 x 256] in TMEM; B = W0e read
         // MN-major from MMA1's w0b tile: the core matrix of hidden rows 8g..8g+7 and
         // feature columns 8c..8c+7 sits at g * KB * 16 + c * 128 bytes)
-        if (tid == 0) {
-            umma::fence_after_sync();
-            if constexpr (DW) {
-                // dW0[h] += d_pre^T [x hi | tail], then += d_pre^T [x lo | 0].
-                // A (hidden half h = staging parts 2h, 2h + 1): atoms of 64 units x 8 rows, next
-                // 64 units 16 KB on, next 8 rows 1 KB on; B (the tile's rows, MN-major): next 8
-                // rows KB*16 bytes on, next 8 features 128 bytes on.
-                const uint32_t st = umma::smem_u32(stage_s);
-                const uint32_t id_b = umma::idesc_f16_mn(TILE_M, KB);
-                for (int h = 0; h < 2; ++h) {
-                    const uint32_t d = t_dw + (uint32_t)(h * KB);
-                    for (int ks = 0; ks < TILE_M / 16; ++ks) {
-                        const uint64_t ad = umma::make_desc_sw128_mn(st + h * 32768u + ks * 2048u, 16384u, 1024u);
-                        const uint64_t bd = umma::make_desc(a_addr(cb) + ks * 2u * KB * 16u, KB * 16u, 128u);
-                        umma::mma_f16(d, ad, bd, id_b, (dw_first && ks == 0) ? 0u : 1u);
-                    }
-                    for (int ks = 0; ks < TILE_M / 16; ++ks) {
-                        const uint64_t ad = umma::make_desc_sw128_mn(st + h * 32768u + ks * 2048u, 16384u, 1024u);
-                        const uint64_t bd = umma::make_desc(a3_addr(cb) + ks * 2u * KB * 16u, KB * 16u, 128u);
-                        umma::mma_f16(d, ad, bd, id_b, 1u);
+        {
+            // descriptor bases from converged code (warp-uniform values); the elected lane adds
+            // constant multiples of row_step per MMA
+            const uint64_t row_step = desc_step(2u * KB * 16u);   // 16 rows (dW0's B) / 16 hidden units (MMA2's B)
+            const uint64_t d_stage = umma::make_desc_sw128_mn(umma::smem_u32(stage_s), 16384u, 1024u);
+            const uint32_t id_dw = umma::idesc_f16_mn(TILE_M, KB);
+            const uint64_t d_w = umma::make_desc(w_addr, (uint32_t)KB * 16u, 128u);
+            const uint64_t bx = umma::make_desc(a_addr(cb), KB * 16u, 128u);
+            const uint64_t bx3 = umma::make_desc(a3_addr(cb), KB * 16u, 128u);
+            if (warp == 0 && umma::elect_one()) {      // (warp 0 reconverges below)
+                // MMA2 and (DW) the two dW0 hidden halves go out in turn, each accumulator in its own order
+                umma::fence_after_sync();
+#pragma unroll
+                for (int i = 0; i < 2 * (HID / 16); ++i) {   // d_pre lo chunks first (smaller addends), then hi
+                    const int ks = i & (HID / 16 - 1);
+                    umma::mma_f16_ta(t_enc, i < HID / 16 ? t_lo(ks) : t_hi(ks), d_w + ks * row_step, idesc2,
+                                     i > 0 ? 1u : 0u);
+                    if (DW && i < 2 * (TILE_M / 16)) {
+                        // dW0[h] += d_pre^T [x hi | tail] (i < 8), then += d_pre^T [x lo | 0].
+                        // A (hidden half h = staging parts 2h, 2h + 1): atoms of 64 units x 8 rows, next
+                        // 64 units 16 KB on, next 8 rows 1 KB on; B (the tile's rows, MN-major): next 8
+                        // rows KB*16 bytes on, next 8 features 128 bytes on.
+                        const int k8 = i & (TILE_M / 16 - 1);
+                        const uint64_t bd = (i < TILE_M / 16 ? bx : bx3) + k8 * row_step;
+                        const uint32_t acc0 = (dw_first && i == 0) ? 0u : 1u;
+#pragma unroll
+                        for (int h = 0; h < 2; ++h)
+                            umma::mma_f16(t_dw + (uint32_t)(h * KB), d_stage + desc_step(h * 32768 + k8 * 2048), bd,
+                                          id_dw, acc0);
                     }
                 }
+                umma::mma_commit(mbar);
             }
-            const uint32_t lbo = (uint32_t)KB * 16u;          // next 8 hidden units (K)
-            for (int ks = 0; ks < HID / 16; ++ks) {          // the lo half first (smaller addends)
-                const uint64_t bd = umma::make_desc(w_addr + ks * 2u * lbo, lbo, 128u);
-                umma::mma_f16_ta(t_enc, t_lo(ks), bd, idesc2, ks > 0 ? 1u : 0u);
-            }
-            for (int ks = 0; ks < HID / 16; ++ks) {
-                const uint64_t bd = umma::make_desc(w_addr + ks * 2u * lbo, lbo, 128u);
-                umma::mma_f16_ta(t_enc, t_hi(ks), bd, idesc2, 1u);
-            }
-            umma::mma_commit(mbar);
         }
+        if (warp == 0) __syncwarp();                 // the issuing lane rejoins its warp before the barrier
         if constexpr (DW) dw_first = false;
         if (tn < ntiles) {
             stage_dh0(tn);                           // every warp has read this tile's d_h0c rows
             prologue_ray(tn, pin);
+            prologue_finish(tn, pin, (it + 1) & 1);  // the other df buffer, under the MMAs
         }
         if (DW && tn < ntiles) {
             cp_async_wait_group<1>();                // tile tn's A tile (its d_h0c group may still be in flight)
             umma::fence_proxy_async_smem();
         }
-        ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
+        ok = __syncthreads_and(tid == 0 ? umma::mbar_wait(mbar, phase) : true);   // one poller
         phase ^= 1u;
         if (!ok) {
             flag_timeout(p.err, 1);
@@ -1019,20 +1035,21 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
             umma::fence_proxy_async_smem();
             umma::fence_before_sync();
             __syncthreads();
-            if (tid == 0) {
+            const uint64_t row_step = desc_step(2u * KB * 16u);
+            const uint64_t d_stage = umma::make_desc_sw128_mn(umma::smem_u32(stage_s), 16384u, 1024u);
+            const uint32_t id_dw = umma::idesc_f16_mn(TILE_M, KB);
+            const uint64_t bx = umma::make_desc(a_addr(cb), KB * 16u, 128u);
+            if (warp == 0 && umma::elect_one()) {
                 umma::fence_after_sync();
-                const uint32_t st = umma::smem_u32(stage_s);
-                const uint32_t id_b = umma::idesc_f16_mn(TILE_M, KB);
-                for (int h = 0; h < 2; ++h) {
-                    const uint32_t d = t_dw + (uint32_t)(h * KB);
-                    for (int ks = 0; ks < TILE_M / 16; ++ks) {
-                        const uint64_t ad = umma::make_desc_sw128_mn(st + h * 32768u + ks * 2048u, 16384u, 1024u);
-                        const uint64_t bd = umma::make_desc(a_addr(cb) + ks * 2u * KB * 16u, KB * 16u, 128u);
-                        umma::mma_f16(d, ad, bd, id_b, 1u);
-                    }
-                }
+#pragma unroll
+                for (int ks = 0; ks < TILE_M / 16; ++ks)     // the two hidden halves' chains in turn
+#pragma unroll
+                    for (int h = 0; h < 2; ++h)
+                        umma::mma_f16(t_dw + (uint32_t)(h * KB), d_stage + desc_step(h * 32768 + ks * 2048),
+                                      bx + ks * row_step, id_dw, 1u);
                 umma::mma_commit(mbar_lo);
             }
+            if (warp == 0) __syncwarp();
         }
         if (DW && tn < ntiles) issue1(nb);           // D1 is free: MMA2 has read d_pre
         // (4) d_enc rows to global for k_field_scatter: 16-column chunks dealt in turn
@@ -1042,7 +1059,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         if constexpr (DW) {
             // the lo dW0 MMAs read the staging rows: wait for them before d_enc goes through
             // (a timed-out wait skips this warp's stores; the tile's closing barrier ends the loop)
-            ok = __all_sync(0xffffffffu, umma::mbar_wait(mbar_lo, phase_lo));
+            ok = __shfl_sync(0xffffffffu, lane == 0 ? (int)umma::mbar_wait(mbar_lo, phase_lo) : 0, 0) != 0;
             phase_lo ^= 1u;
             if (!ok && lane == 0) flag_timeout(p.err, 1);
         }
@@ -1063,12 +1080,9 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
             }
         }
         umma::fence_before_sync();
-        if (tn < ntiles) {
-            prologue_finish(tn, pin, (it + 1) & 1);  // the other df buffer
-            if (!DW) {
-                cp_async_wait_group<1>();            // tile tn's A tile (its d_h0c group may still be in flight)
-                umma::fence_proxy_async_smem();
-            }
+        if (!DW && tn < ntiles) {
+            cp_async_wait_group<1>();                // tile tn's A tile (its d_h0c group may still be in flight)
+            umma::fence_proxy_async_smem();
         }
         ok = __syncthreads_and(ok);   // the TMEM accumulator of tile t read; tile tn's A tile and d f in place
         if (ok && !DW && tn < ntiles) issue1(nb);
