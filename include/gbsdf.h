@@ -480,6 +480,31 @@ int gbsdf_sampler_round(const gbsdf_sampler_args* args, void* stream);
 int gbsdf_wgrad(int64_t M, int N, int K, const void* dZ, const void* dZ_lo, int ldz, const void* X, int ldx,
                 float* dW, int ldw, int accumulate, int* err, void* stream);
 
+/* Gradients of weight-normalised linears (torch.nn.utils.weight_norm, dim 0: W = g v / ||v||
+ * per output row; projects/neuralangelo/utils/mlp.py:55-69, projects/nerf/utils/nerf_util.py:
+ * 187-196) from the gradient of the effective weight, with the loss scale taken off; replaces
+ * autograd's per-layer weight-norm backward.  An entry with v == NULL is plain: the weight's
+ * gradient gets s dW and the bias's s db (s = *scale_dev when scale_dev is not NULL, else scale).
+ * Gradient tensors (dv, dg, dbias) are contiguous; acc_* = 1 adds into them, 0 overwrites.
+ * Up to GBSDF_WN_MAX_LAYERS entries per call, one launch. */
+#define GBSDF_WN_MAX_LAYERS 16
+typedef struct gbsdf_weightnorm_layer {
+    int64_t rows, cols;
+    const float* dW;      /* effective-weight gradient [rows, cols], row stride ld_dw */
+    int64_t ld_dw;
+    const float* db;      /* bias gradient [rows], element stride ld_db, or NULL */
+    int64_t ld_db;
+    const float* v;       /* weight_v [rows, cols] contiguous, or NULL for a plain entry */
+    const float* g;       /* weight_g [rows] */
+    float* dv;            /* weight_v.grad (plain: weight.grad) [rows, cols] */
+    float* dg;            /* weight_g.grad [rows] */
+    float* dbias;         /* bias.grad [rows], or NULL */
+    int32_t acc_v, acc_g, acc_b, pad;
+} gbsdf_weightnorm_layer;
+int gbsdf_weightnorm_bwd(int32_t n, const gbsdf_weightnorm_layer* layers, const float* scale_dev, float scale,
+                         void* stream);
+size_t gbsdf_weightnorm_layer_size(void);   /* sizeof(gbsdf_weightnorm_layer), for binding checks */
+
 /* Self-test of the bounded waits (no counterpart in the reference): one GPU thread waits on an
  * mbarrier with the limit timeout_ns (0 to 2 s); nothing arrives on it unless arrive_first.
  * status [2] int32 (device): status[0] = 1 when the wait ran out, 0 when it completed;

@@ -132,9 +132,89 @@ def _wgrad(dZ, X, N, K, dW, accumulate=False, dZ_lo=None, err=None):
               c_vp(_p(err)), _lib.stream_ptr(dZ.device))
 
 
-def pack_sdf(sdf):
+class WeightNormLayer(ctypes.Structure):
+    """gbsdf_weightnorm_layer (include/gbsdf.h)."""
+    _fields_ = [("rows", c_i64), ("cols", c_i64), ("dW", c_vp), ("ld_dw", c_i64), ("db", c_vp), ("ld_db", c_i64),
+                ("v", c_vp), ("g", c_vp), ("dv", c_vp), ("dg", c_vp), ("dbias", c_vp),
+                ("acc_v", c_i32), ("acc_g", c_i32), ("acc_b", c_i32), ("pad", c_i32)]
+
+
+WN_MAX_LAYERS = 16
+_lib.register("gbsdf_weightnorm_bwd", [c_i32, c_vp, c_vp, c_f32, c_vp])
+
+
+class _GradSink:
+    """The masters' .grad tensors that gbsdf_weightnorm_bwd writes: an absent one is created
+    uninitialised and overwritten (as autograd sets a fresh .grad), a present one is added into."""
+
+    def __init__(self):
+        self.seen = {}
+
+    def __call__(self, param):
+        key = id(param)
+        if key not in self.seen:
+            if param.grad is None:
+                param.grad = torch.empty_like(param, memory_format=torch.contiguous_format)
+                acc = 0
+            else:
+                if not param.grad.is_contiguous():
+                    raise ValueError("gbsdf_weightnorm_bwd writes contiguous gradients")
+                acc = 1
+            self.seen[key] = (param.grad, acc)
+        return self.seen[key]
+
+
+def _wn_entry(sink, dW, db=None, weight=None, bias=None, v=None, g=None, rows=None):
+    """One gbsdf_weightnorm_layer: the weight-norm parameters v, g (weight-norm entry) or the
+    plain weight (plain entry), the bias, and the row range ``rows`` (a slice of the
+    destination's rows, for gradients assembled from row blocks)."""
+    if dW.dim() == 1:
+        dW = dW.reshape(1, -1)
+    assert dW.stride(1) == 1 and dW.dtype == torch.float32
+    e = WeightNormLayer()
+    e.rows, e.cols = dW.shape
+    e.dW, e.ld_dw = dW.data_ptr(), dW.stride(0)
+    sl = rows if rows is not None else slice(0, dW.shape[0])
+    if v is not None:
+        dv, e.acc_v = sink(v)
+        dg, e.acc_g = sink(g)
+        e.v, e.g = v.detach()[sl].data_ptr(), g.detach().reshape(-1)[sl].data_ptr()
+        e.dv, e.dg = dv[sl].data_ptr(), dg.reshape(-1)[sl].data_ptr()
+    else:
+        dv, e.acc_v = sink(weight)
+        e.dv = dv.reshape(-1, e.cols)[sl].data_ptr()
+    if db is not None and bias is not None:
+        db = db.reshape(-1)
+        assert db.dtype == torch.float32
+        dbias, e.acc_b = sink(bias)
+        e.db, e.ld_db = db.data_ptr(), db.stride(0)
+        e.dbias = dbias.reshape(-1)[sl].data_ptr()
+    return e
+
+
+def _weightnorm_bwd(entries, scale, device):
+    """All entries in launches of up to WN_MAX_LAYERS; scale a device scalar or a float."""
+    sdev = scale.data_ptr() if torch.is_tensor(scale) else None
+    sval = 0.0 if torch.is_tensor(scale) else float(scale)
+    for i in range(0, len(entries), WN_MAX_LAYERS):
+        chunk = entries[i:i + WN_MAX_LAYERS]
+        arr = (WeightNormLayer * len(chunk))(*chunk)
+        _lib.call("gbsdf_weightnorm_bwd", len(chunk), ctypes.cast(arr, c_vp), c_vp(sdev), sval,
+                  _lib.stream_ptr(device))
+
+
+def active_table_params(sdf):
+    """Number of table parameters in the active levels: the levels are stored level-major, so
+    the active ones are a prefix of the table, and no kernel reads or writes past it."""
+    layout = sdf.tcnn_encoding.layout
+    return int(layout.offset[sdf.active_levels]) * layout.n_features
+
+
+def pack_sdf(sdf, table16=None):
     """FP16 working copies of a NeuralSDF's hash table and layer-0 weights (weight norm
-    applied) plus the FP32 position columns, bias and head; returns (pk, active, K0)."""
+    applied) plus the FP32 position columns, bias and head; returns (pk, active, K0).
+    An FP32 table is converted over its active levels only, into ``table16`` when given (a
+    persistent buffer of the table's size; the inactive levels are left as they are)."""
     A = sdf.active_levels
     F = sdf.tcnn_encoding.layout.n_features
     K0 = max(16, _round16(A * F))
@@ -145,8 +225,16 @@ def pack_sdf(sdf):
         w0e[:, :A * F] = W0[:, 3:3 + A * F]
         w0x = W0[:, :3].contiguous().float()
         b0 = sdf.mlp.linears[0].bias.detach().float()
+        params = sdf.tcnn_encoding.params.detach()
+        if params.dtype == torch.float16:
+            table = params
+        else:
+            n = active_table_params(sdf)
+            table = table16 if table16 is not None else torch.empty(max(n, 1), device=params.device,
+                                                                    dtype=torch.float16)
+            table[:n].copy_(params[:n])
         pk = dict(
-            table=sdf.tcnn_encoding.params.detach().half(),
+            table=table,
             w0e=w0e, w0b=w0_with_tail(w0e, w0x, b0),
             w0x=w0x, b0=b0,
             whead=sdf.mlp.linear_sdf.weight.detach()[0].contiguous().float(),
@@ -260,13 +348,18 @@ class FusedField:
             self.Kr0 = 256 + _round16(16 + self.app_dim + 1)   # [feat | SH 16, app, 1 | 0]
         self.ws = None
         self.err = None
+        self._table16 = None          # persistent fp16 working copy of an FP32 table
 
     # ------------------------------------------------------------------ parameters
     def _pack(self):
         """FP16 working copies of the FP32 masters (weight norm applied) for this step."""
         m = self.model
         sdf = m.neural_sdf
-        pk, self.A, self.K0 = pack_sdf(sdf)
+        params = sdf.tcnn_encoding.params
+        if params.dtype != torch.float16 and (self._table16 is None or self._table16.numel() != params.numel()
+                                               or self._table16.device != params.device):
+            self._table16 = torch.zeros(params.numel(), device=params.device, dtype=torch.float16)
+        pk, self.A, self.K0 = pack_sdf(sdf, self._table16)
         with torch.no_grad():
             W0 = sdf.mlp.linears[0].weight
             W1 = sdf.mlp.linears[1].weight
@@ -769,8 +862,9 @@ class FusedField:
 
     # ------------------------------------------------------------------ gradients -> masters
     def _scatter_grads(self, g):
-        """Unscale, map effective-weight gradients onto the weight-norm parameters
-        (W = g v / ||v||) with autograd, and accumulate into the masters' .grad."""
+        """Map the effective-weight gradients onto the weight-norm parameters (W = g v / ||v||),
+        take the loss scale off and accumulate into the masters' .grad: gbsdf_weightnorm_bwd,
+        one launch for every layer and plain parameter of the field and the colour MLP."""
         m = self.model
         inv = self._scal[3:4] if self.dynamic else 1.0 / self.loss_scale
         sdf = m.neural_sdf
@@ -800,28 +894,29 @@ class FusedField:
             eff.append((lins[i], g[f'wc{i}'], g[f'bc{i}']))
         eff.append((lins[-1], g['wl'], g['bl']))
         names = ['sdf.l0', 'sdf.l1'] + [f'rgb.l{i}' for i in range(len(eff) - 2)]
-        self.eff_grads = {n: (dW * inv, db * inv) for n, (_, dW, db) in zip(names, eff)}
-        for lin, dW, db in eff:
-            with torch.enable_grad():
-                v = lin.weight_v.detach().requires_grad_(True)
-                gg = lin.weight_g.detach().requires_grad_(True)
-                W = v * (gg / v.norm(dim=1, keepdim=True))
-                dv, dg = torch.autograd.grad(W, (v, gg), grad_outputs=dW * inv)
-            _acc(lin.weight_v, dv)
-            _acc(lin.weight_g, dg)
-            _acc(lin.bias, db * inv)
-        _acc(sdf.mlp.linear_sdf.weight, (self.ws['d_whead'] * inv).reshape(1, -1))
-        _acc(sdf.mlp.linear_sdf.bias, self.ws['d_bhead'] * inv)
+        self._eff = (names, [(dW, db) for _, dW, db in eff], inv)
+        sink = _GradSink()
+        ents = [_wn_entry(sink, dW, db, bias=lin.bias, v=lin.weight_v, g=lin.weight_g) for lin, dW, db in eff]
+        head = sdf.mlp.linear_sdf
+        ents.append(_wn_entry(sink, self.ws['d_whead'], self.ws['d_bhead'], weight=head.weight, bias=head.bias))
+        ents.append(_wn_entry(sink, self.ws['d_s_var'].reshape(1, 1), weight=m.s_var))
+        if self.app_dim:
+            ents.append(_wn_entry(sink, g['app'], weight=m.appear_embed.weight))
+        if self.bg:
+            ents += self._scatter_background(g['bg'], inv, sink)
+        _weightnorm_bwd(ents, inv, dW0.device)
         if not self._table_in_place:
             _acc(sdf.tcnn_encoding.params, g['table'].to(sdf.tcnn_encoding.params.dtype))
-        _acc(m.s_var, (self.ws['d_s_var'] * inv).reshape(()))
-        if self.app_dim:
-            _acc(m.appear_embed.weight, g['app'] * inv)
-        if self.bg:
-            self._scatter_background(g['bg'], inv)
 
-    def _scatter_background(self, g, inv):
-        """Background NeRF gradients (plain linears) from the packed layouts into .grad."""
+    @property
+    def eff_grads(self):
+        """Unscaled gradients of the effective weights and biases of the last step, per layer."""
+        names, eff, inv = self._eff
+        return {n: (dW * inv, db * inv) for n, (dW, db) in zip(names, eff)}
+
+    def _scatter_background(self, g, inv, sink):
+        """Background NeRF gradients (plain linears) from the packed layouts: entries of the
+        gradient launch."""
         bgm = self.model.background_nerf
         L, Lr = bgm.mlp_feat.linears, bgm.mlp_rgb.linears
         eff = {}
@@ -829,20 +924,32 @@ class FusedField:
         for i in (1, 2, 3, 5, 6):
             eff[f'bg.l{i}'] = (g[i][:, :256], g[i][:, 256])
         eff['bg.l4'] = (g[4][:, :340], g[4][:, 340])
-        g7 = g[7]
-        eff['bg.l7'] = (torch.cat([g7[256:257, :256], g7[:256, :256]], dim=0),
-                        torch.cat([g7[256:257, 256], g7[:256, 256]], dim=0))
         nin = 256 + 16 + self.app_dim
         eff['bg.rgb.l0'] = (g['r0'][:, :nin], g['r0'][:, nin])
         eff['bg.rgb.l1'] = (g['r1'], self.ws['bg_d_bl'])
         lins = {f'bg.l{i}': L[i] for i in range(8)}
         lins.update({'bg.rgb.l0': Lr[0], 'bg.rgb.l1': Lr[1]})
-        self.bg_grads = {k: (dW * inv, db * inv) for k, (dW, db) in eff.items()}
-        for k, (dW, db) in self.bg_grads.items():
-            _acc(lins[k].weight, dW)
-            _acc(lins[k].bias, db)
+        # layer 7's rows come packed as [256 feature rows | density row]; the layer's order is
+        # [density | features]
+        g7 = g[7]
+        self._bg_eff = (eff, g7, inv)
+        ents = [_wn_entry(sink, dW, db, weight=lins[k].weight, bias=lins[k].bias) for k, (dW, db) in eff.items()]
+        ents.append(_wn_entry(sink, g7[256:257, :256], g7[256:257, 256], weight=L[7].weight, bias=L[7].bias,
+                              rows=slice(0, 1)))
+        ents.append(_wn_entry(sink, g7[:256, :256], g7[:256, 256], weight=L[7].weight, bias=L[7].bias,
+                              rows=slice(1, 257)))
         if self.app_dim:
-            _acc(self.model.appear_embed_outside.weight, g['app'] * inv)
+            ents.append(_wn_entry(sink, g['app'], weight=self.model.appear_embed_outside.weight))
+        return ents
+
+    @property
+    def bg_grads(self):
+        """Unscaled gradients of the background NeRF's weights and biases of the last step."""
+        eff, g7, inv = self._bg_eff
+        out = {k: (dW * inv, db * inv) for k, (dW, db) in eff.items()}
+        out['bg.l7'] = (torch.cat([g7[256:257, :256], g7[:256, :256]], dim=0) * inv,
+                        torch.cat([g7[256:257, 256], g7[:256, 256]], dim=0) * inv)
+        return out
 
     # ------------------------------------------------------------------ dynamic loss scaling
     def _scalars(self, device):
@@ -906,7 +1013,9 @@ def _acc(param, grad):
 class CapturedStep:
     """One training step of a FusedField -- zero the master gradients, forward,
     backward (and, with dynamic loss scaling, the overflow check and the scale update) --
-    captured in a CUDA graph and replayed.
+    captured in a CUDA graph and replayed.  A replay clears the hash table's gradient over the
+    active levels only; the inactive levels stay as the capture left them (zero), so code that
+    writes into that gradient between replays must keep them zero.
 
     The batch is copied into static device buffers at capture time; ``replay(batch)``
     copies a new batch of the same shapes into them (host tensors are copied from
@@ -950,9 +1059,17 @@ class CapturedStep:
         fused.refresh_scalars()
         self.key = fused.schedule_key()
         self.graph = torch.cuda.CUDAGraph()
+        # the table gradient is cleared over the active levels only: the warm-up above zeroed
+        # all of it, the step writes nothing past the active prefix, and a change of the active
+        # levels captures the step again
+        table = model.neural_sdf.tcnn_encoding.params
+        n_act = active_table_params(model.neural_sdf)
         with torch.cuda.graph(self.graph):
             for p in self.params:
-                p.grad.zero_()
+                if p is table:
+                    p.grad[:n_act].zero_()
+                else:
+                    p.grad.zero_()
             self.out = fused.step(self.static, compute_loss=False, _refresh=False)
 
     def replay(self, batch=None):

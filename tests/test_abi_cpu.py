@@ -126,3 +126,24 @@ def test_workspace_size_queries(lib):
     lib.gbsdf_dense_workspace_size.restype = ctypes.c_size_t
     assert lib.gbsdf_render_workspace_size(ctypes.c_int64(16384), 128, 32) == 0
     assert lib.gbsdf_dense_workspace_size(ctypes.c_int64(1 << 21), 256, 256) == 0
+
+
+def test_weightnorm_arguments_without_gpu(lib):
+    """gbsdf_weightnorm_bwd: the binding's struct layout, and the argument checks that return
+    before any launch."""
+    from neuralangelo_gb300 import fused
+    lib.gbsdf_weightnorm_layer_size.restype = ctypes.c_size_t
+    assert lib.gbsdf_weightnorm_layer_size() == ctypes.sizeof(fused.WeightNormLayer)
+    one = ctypes.c_float(1.0)
+    assert lib.gbsdf_weightnorm_bwd(fused.WN_MAX_LAYERS + 1, None, None, one, None) == 1
+    assert b"entries" in lib.gbsdf_last_error()
+    arr = (fused.WeightNormLayer * 1)()
+    arr[0].rows, arr[0].cols = 4, 8
+    ptr = ctypes.cast(arr, ctypes.c_void_p)
+    assert lib.gbsdf_weightnorm_bwd(1, ptr, None, one, None) == 1
+    assert b"NULL dW" in lib.gbsdf_last_error()
+    arr[0].dW, arr[0].dv, arr[0].ld_dw = 16, 16, 8
+    arr[0].v = 16                                   # weight norm without g / dg
+    assert lib.gbsdf_weightnorm_bwd(1, ptr, None, one, None) == 1
+    assert b"needs g and dg" in lib.gbsdf_last_error()
+    assert lib.gbsdf_weightnorm_bwd(0, None, None, one, None) == 0
