@@ -505,6 +505,30 @@ int gbsdf_weightnorm_bwd(int32_t n, const gbsdf_weightnorm_layer* layers, const 
                          void* stream);
 size_t gbsdf_weightnorm_layer_size(void);   /* sizeof(gbsdf_weightnorm_layer), for binding checks */
 
+/* Working copies of weight-normalised (or plain) weights for the fused step: per entry, rows of
+ * W = g v / ||v|| (the norm over all `cols` of each source row; g == NULL: W = v), columns
+ * [col0, col0 + ncols), written to any of: dst16 (fp16, row stride ld16, the segment's first
+ * column at dst16), dst16_lo (fp16 residual W - fp16(W), dst16's layout), dst16T (fp16
+ * transposed: element (r, j) at dst16T[j * ldT + r]), dst32 (FP32, row stride ld32).  Replaces
+ * the weight-norm forward of each linear (the reference's weight property) and the casts,
+ * transposes and column reorders of the packing.  Up to GBSDF_WN_MAX_LAYERS entries, one launch. */
+typedef struct gbsdf_weightnorm_pack {
+    int64_t rows, cols;
+    const float* v;       /* weight_v or the plain weight, [rows, ld_src] */
+    int64_t ld_src;
+    const float* g;       /* weight_g [rows], or NULL for a plain weight */
+    int64_t col0, ncols;
+    void* dst16;
+    int64_t ld16;
+    void* dst16_lo;
+    void* dst16T;
+    int64_t ldT;
+    float* dst32;
+    int64_t ld32;
+} gbsdf_weightnorm_pack;
+int gbsdf_weightnorm_fwd(int32_t n, const gbsdf_weightnorm_pack* entries, void* stream);
+size_t gbsdf_weightnorm_pack_size(void);
+
 /* Self-test of the bounded waits (no counterpart in the reference): one GPU thread waits on an
  * mbarrier with the limit timeout_ns (0 to 2 s); nothing arrives on it unless arrive_first.
  * status [2] int32 (device): status[0] = 1 when the wait ran out, 0 when it completed;

@@ -13,7 +13,9 @@
 //
 // One warp per output row: two warp sums (||v_r||^2 and dW_r . v_r), then one pass writing
 // dv_r.  Replaces the per-layer autograd graphs (norm, quotient, product and their backward)
-// and the separate unscale and accumulate kernels.
+// and the separate unscale and accumulate kernels.  gbsdf_weightnorm_fwd below forms the
+// weights' working copies the same way, in place of the per-layer weight-norm forward, cast,
+// transpose and reorder kernels.
 #include "common.cuh"
 
 namespace gbsdf {
@@ -75,10 +77,80 @@ __global__ void __launch_bounds__(256) k_weightnorm_bwd(const __grid_constant__ 
     }
 }
 
+// ---------------------------------------------------------------------------
+// The forward counterpart: the fp16 (and fp32) working copies of the effective weights that the
+// fused step's kernels read, W = g v / ||v|| (or a plain weight), one column segment per entry,
+// written row-major, as an fp16 hi + lo pair, transposed, or in FP32.  The product is formed as
+// torch's weight norm forms it: v * (g / ||v||).
+struct WnPackParams {
+    gbsdf_weightnorm_pack E[GBSDF_WN_MAX_LAYERS];
+    int64_t row0[GBSDF_WN_MAX_LAYERS + 1];
+    int n;
+};
+
+__global__ void __launch_bounds__(256) k_weightnorm_fwd(const __grid_constant__ WnPackParams p) {
+    const int64_t grow = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (grow >= p.row0[p.n]) return;
+    int l = 0;
+    while (grow >= p.row0[l + 1]) ++l;
+    const gbsdf_weightnorm_pack& E = p.E[l];
+    const int64_t r = grow - p.row0[l];
+    const float* v = E.v + r * E.ld_src;
+    float scale = 1.0f;
+    if (E.g) {
+        float n2 = 0.0f;
+        for (int64_t j = lane; j < E.cols; j += 32) n2 = fmaf(v[j], v[j], n2);
+        scale = E.g[r] / sqrtf(wn_warp_sum(n2));
+    }
+    __half* d16 = reinterpret_cast<__half*>(E.dst16);
+    __half* d16lo = reinterpret_cast<__half*>(E.dst16_lo);
+    __half* d16t = reinterpret_cast<__half*>(E.dst16T);
+    for (int64_t j = lane; j < E.ncols; j += 32) {
+        const float w = v[E.col0 + j] * scale;
+        const __half h = __float2half_rn(w);
+        if (d16) d16[r * E.ld16 + j] = h;
+        if (d16lo) d16lo[r * E.ld16 + j] = __float2half_rn(w - __half2float(h));
+        if (d16t) d16t[j * E.ldT + r] = h;
+        if (E.dst32) E.dst32[r * E.ld32 + j] = w;
+    }
+}
+
 }  // namespace
 }  // namespace gbsdf
 
 using namespace gbsdf;
+
+extern "C" int gbsdf_weightnorm_fwd(int32_t n, const gbsdf_weightnorm_pack* entries, void* stream) {
+    clear_error();
+    GBSDF_CHECK_ARG(n >= 0 && n <= GBSDF_WN_MAX_LAYERS, "n %d (0 to %d entries)", n, GBSDF_WN_MAX_LAYERS);
+    GBSDF_CHECK_ARG(n == 0 || entries != nullptr, "NULL entries");
+    WnPackParams p{};
+    p.n = n;
+    int64_t rows = 0;
+    for (int i = 0; i < n; ++i) {
+        const gbsdf_weightnorm_pack& E = entries[i];
+        GBSDF_CHECK_ARG(E.rows >= 0 && E.cols > 0 && E.col0 >= 0 && E.ncols >= 0 && E.col0 + E.ncols <= E.cols,
+                        "entry %d: rows %lld, cols %lld, segment [%lld, %lld)", i, (long long)E.rows,
+                        (long long)E.cols, (long long)E.col0, (long long)(E.col0 + E.ncols));
+        GBSDF_CHECK_ARG(E.v, "entry %d: NULL v", i);
+        GBSDF_CHECK_ARG(E.ld_src >= E.cols || E.rows <= 1, "entry %d: ld_src %lld < cols", i, (long long)E.ld_src);
+        GBSDF_CHECK_ARG(E.dst16 || E.dst16T || E.dst32, "entry %d: no destination", i);
+        GBSDF_CHECK_ARG(!E.dst16_lo || E.dst16, "entry %d: dst16_lo needs dst16", i);
+        GBSDF_CHECK_ARG(!E.dst16 || E.ld16 >= E.ncols || E.rows <= 1, "entry %d: ld16", i);
+        GBSDF_CHECK_ARG(!E.dst16T || E.ldT >= E.rows, "entry %d: ldT %lld < rows", i, (long long)E.ldT);
+        GBSDF_CHECK_ARG(!E.dst32 || E.ld32 >= E.ncols || E.rows <= 1, "entry %d: ld32", i);
+        p.E[i] = E;
+        p.row0[i] = rows;
+        rows += E.rows;
+    }
+    p.row0[n] = rows;
+    if (rows == 0) return GBSDF_OK;
+    k_weightnorm_fwd<<<(unsigned)((rows + 7) / 8), 256, 0, as_stream(stream)>>>(p);
+    return launch_status("weightnorm_fwd");
+}
+
+extern "C" size_t gbsdf_weightnorm_pack_size(void) { return sizeof(gbsdf_weightnorm_pack); }
 
 extern "C" int gbsdf_weightnorm_bwd(int32_t n, const gbsdf_weightnorm_layer* layers, const float* scale_dev,
                                     float scale, void* stream) {

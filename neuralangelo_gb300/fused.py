@@ -192,6 +192,64 @@ def _wn_entry(sink, dW, db=None, weight=None, bias=None, v=None, g=None, rows=No
     return e
 
 
+class WeightNormPack(ctypes.Structure):
+    """gbsdf_weightnorm_pack (include/gbsdf.h)."""
+    _fields_ = [("rows", c_i64), ("cols", c_i64), ("v", c_vp), ("ld_src", c_i64), ("g", c_vp),
+                ("col0", c_i64), ("ncols", c_i64), ("dst16", c_vp), ("ld16", c_i64), ("dst16_lo", c_vp),
+                ("dst16T", c_vp), ("ldT", c_i64), ("dst32", c_vp), ("ld32", c_i64)]
+
+
+_lib.register("gbsdf_weightnorm_fwd", [c_i32, c_vp, c_vp])
+
+
+def _wsrc(lin):
+    """(v, g) of a weight-normalised linear, (weight, None) of a plain one."""
+    if hasattr(lin, 'weight_v'):
+        return lin.weight_v.detach(), lin.weight_g.detach().reshape(-1)
+    return lin.weight.detach(), None
+
+
+def _pk_entry(src, g=None, col0=0, ncols=None, rows=None, dst16=None, dst16_lo=None, dst16T=None, dst32=None):
+    """One gbsdf_weightnorm_pack entry: rows ``rows`` (a slice) of W = g v / ||v|| (src = v; or
+    W = src when g is None), columns [col0, col0 + ncols).  Each destination is a view whose
+    element (0, 0) takes (first row, col0): dst16 / dst16_lo / dst32 row-major [rows, ncols] (a
+    1-D view for one column), dst16T [ncols, rows]."""
+    if src.dim() == 1:
+        src = src.reshape(-1, 1)
+    sl = rows if rows is not None else slice(0, src.shape[0])
+    part = src[sl]
+    assert src.dtype == torch.float32 and src.stride(1) == 1
+    e = WeightNormPack()
+    e.rows, e.cols = part.shape[0], src.shape[1]
+    e.v, e.ld_src = part.data_ptr(), src.stride(0)
+    e.g = g[sl].data_ptr() if g is not None else None
+    e.col0 = col0
+    e.ncols = ncols if ncols is not None else src.shape[1] - col0
+
+    def rowmajor(t, dt):
+        assert t.dtype == dt and (t.dim() == 1 or t.stride(1) == 1)
+        return t.data_ptr(), t.stride(0)
+    if dst16 is not None:
+        e.dst16, e.ld16 = rowmajor(dst16, torch.float16)
+        if dst16_lo is not None:
+            ptr, ld = rowmajor(dst16_lo, torch.float16)
+            assert ld == e.ld16
+            e.dst16_lo = ptr
+    if dst16T is not None:
+        e.dst16T, e.ldT = rowmajor(dst16T, torch.float16)
+    if dst32 is not None:
+        e.dst32, e.ld32 = rowmajor(dst32, torch.float32)
+    return e
+
+
+def _weightnorm_fwd(entries, device):
+    """All pack entries in launches of up to WN_MAX_LAYERS."""
+    for i in range(0, len(entries), WN_MAX_LAYERS):
+        chunk = entries[i:i + WN_MAX_LAYERS]
+        arr = (WeightNormPack * len(chunk))(*chunk)
+        _lib.call("gbsdf_weightnorm_fwd", len(chunk), ctypes.cast(arr, c_vp), _lib.stream_ptr(device))
+
+
 def _weightnorm_bwd(entries, scale, device):
     """All entries in launches of up to WN_MAX_LAYERS; scale a device scalar or a float."""
     sdev = scale.data_ptr() if torch.is_tensor(scale) else None
@@ -210,56 +268,53 @@ def active_table_params(sdf):
     return int(layout.offset[sdf.active_levels]) * layout.n_features
 
 
-def pack_sdf(sdf, table16=None):
+def pack_sdf(sdf, table16=None, bufs=None, entries=None):
     """FP16 working copies of a NeuralSDF's hash table and layer-0 weights (weight norm
     applied) plus the FP32 position columns, bias and head; returns (pk, active, K0).
     An FP32 table is converted over its active levels only, into ``table16`` when given (a
-    persistent buffer of the table's size; the inactive levels are left as they are)."""
+    persistent buffer of the table's size; the inactive levels are left as they are).
+    The layer-0 copies are written by gbsdf_weightnorm_fwd into ``bufs`` (zero-initialised
+    buffers kept by the caller for this active-level count; fresh ones when None); with
+    ``entries`` (a list) the pack entries are appended there for the caller's launch."""
     A = sdf.active_levels
     F = sdf.tcnn_encoding.layout.n_features
     K0 = max(16, _round16(A * F))
     H = sdf.cfg_sdf.mlp.hidden_dim
-    with torch.no_grad():
-        W0 = sdf.mlp.linears[0].weight                           # [256, 3 + L F]
-        w0e = torch.zeros(H, K0, device=W0.device, dtype=torch.float16)
-        w0e[:, :A * F] = W0[:, 3:3 + A * F]
-        w0x = W0[:, :3].contiguous().float()
-        b0 = sdf.mlp.linears[0].bias.detach().float()
-        params = sdf.tcnn_encoding.params.detach()
-        if params.dtype == torch.float16:
-            table = params
-        else:
-            n = active_table_params(sdf)
-            table = table16 if table16 is not None else torch.empty(max(n, 1), device=params.device,
-                                                                    dtype=torch.float16)
-            table[:n].copy_(params[:n])
-        pk = dict(
-            table=table,
-            w0e=w0e, w0b=w0_with_tail(w0e, w0x, b0),
-            w0x=w0x, b0=b0,
-            whead=sdf.mlp.linear_sdf.weight.detach()[0].contiguous().float(),
-            bhead=sdf.mlp.linear_sdf.bias.detach().float())
+    l0 = sdf.mlp.linears[0]
+    dev = l0.bias.device
+    if bufs is None:
+        bufs = {}
+    if 'w0e' not in bufs:
+        bufs['w0e'] = torch.zeros(H, K0, device=dev, dtype=torch.float16)
+        bufs['w0b'] = torch.zeros(H, K0 + 16, device=dev, dtype=torch.float16)
+        bufs['w0x'] = torch.zeros(H, 3, device=dev, dtype=torch.float32)
+    w0e, w0b, w0x = bufs['w0e'], bufs['w0b'], bufs['w0x']
+    b0 = l0.bias.detach()
+    # w0b: the fp16 encoding columns, then the position columns and bias as fp16 hi/lo pairs
+    # matched to the x0ext tail (x hi, 1, x lo, 1, x hi): w hi, b hi, w hi, b lo, w lo.  The
+    # products sum to w0x x + b0 to ~2^-20 relative, so the pre-activation keeps FP32 accuracy.
+    v, g = _wsrc(l0)
+    ents = [_pk_entry(v, g, col0=3, ncols=A * F, dst16=w0e),
+            _pk_entry(v, g, col0=3, ncols=A * F, dst16=w0b),
+            _pk_entry(v, g, col0=0, ncols=3, dst16=w0b[:, K0:], dst16_lo=w0b[:, K0 + 8:], dst32=w0x),
+            _pk_entry(v, g, col0=0, ncols=3, dst16=w0b[:, K0 + 4:]),
+            _pk_entry(b0, None, dst16=w0b[:, K0 + 3], dst16_lo=w0b[:, K0 + 7])]
+    if entries is not None:
+        entries += ents
+    else:
+        _weightnorm_fwd(ents, dev)
+    params = sdf.tcnn_encoding.params.detach()
+    if params.dtype == torch.float16:
+        table = params
+    else:
+        n = active_table_params(sdf)
+        table = table16 if table16 is not None else torch.empty(max(n, 1), device=params.device,
+                                                                dtype=torch.float16)
+        table[:n].copy_(params[:n])
+    pk = dict(table=table, w0e=w0e, w0b=w0b, w0x=w0x, b0=b0,
+              whead=sdf.mlp.linear_sdf.weight.detach()[0],
+              bhead=sdf.mlp.linear_sdf.bias.detach())
     return pk, A, K0
-
-
-def w0_with_tail(w0e, w0x, b0):
-    """B operand [256, K0 + 16] of the forward field MMA: the fp16 encoding columns, then
-    the position columns and bias as fp16 hi/lo pairs matched to the x0ext tail
-    (x hi, 1, x lo, 1, x hi): w hi, b hi, w hi, b lo, w lo.  The products sum to
-    w0x x + b0 to ~2^-20 relative, so the pre-activation keeps FP32 accuracy."""
-    H, K0 = w0e.shape
-    hi = w0x.half()
-    lo = (w0x - hi.float()).half()
-    bh = b0.half()
-    bl = (b0 - bh.float()).half()
-    t = torch.zeros(H, K0 + 16, device=w0e.device, dtype=torch.float16)
-    t[:, :K0] = w0e
-    t[:, K0:K0 + 3] = hi
-    t[:, K0 + 3] = bh
-    t[:, K0 + 4:K0 + 7] = hi
-    t[:, K0 + 7] = bl
-    t[:, K0 + 8:K0 + 11] = lo
-    return t
 
 
 def sdf_weight_args(sdf, pk, A, K0, err=None):
@@ -349,96 +404,110 @@ class FusedField:
         self.ws = None
         self.err = None
         self._table16 = None          # persistent fp16 working copy of an FP32 table
+        self._pkbuf = None            # persistent weight copies (per active-level count)
 
     # ------------------------------------------------------------------ parameters
     def _pack(self):
-        """FP16 working copies of the FP32 masters (weight norm applied) for this step."""
+        """Working copies of the FP32 masters (weight norm applied) for this step: the fp16
+        table over the active levels, and every MLP weight copy (fp16, transposed, reordered)
+        from gbsdf_weightnorm_fwd into buffers kept across steps."""
         m = self.model
         sdf = m.neural_sdf
         params = sdf.tcnn_encoding.params
         if params.dtype != torch.float16 and (self._table16 is None or self._table16.numel() != params.numel()
                                                or self._table16.device != params.device):
             self._table16 = torch.zeros(params.numel(), device=params.device, dtype=torch.float16)
-        pk, self.A, self.K0 = pack_sdf(sdf, self._table16)
-        with torch.no_grad():
-            W0 = sdf.mlp.linears[0].weight
-            W1 = sdf.mlp.linears[1].weight
-            pk['w1'] = W1.half().contiguous()
-            pk['w1T'] = W1.t().half().contiguous()
-            pk['b1'] = sdf.mlp.linears[1].bias.detach().float()
-            lins = m.neural_rgb.mlp.linears
-            # colour layer 0 columns reordered to [feat 256 | x 3, SH 16, n 3, app | 0]
-            Wc0 = lins[0].weight
-            sh = 16
-            tail_src = torch.cat([Wc0[:, 0:3], Wc0[:, 3:3 + sh], Wc0[:, 3 + sh:6 + sh],
-                                  Wc0[:, 6 + sh + 256:6 + sh + 256 + self.app_dim]], dim=1)
-            wc0 = torch.zeros(self.Hc, self.Kc0, device=W0.device, dtype=torch.float16)
-            wc0[:, :256] = Wc0[:, 6 + sh:6 + sh + 256]
-            wc0[:, 256:256 + self.tail] = tail_src
-            pk['wc'] = [wc0.contiguous()]
-            pk['bc'] = [lins[0].bias.detach().float()]
-            for i in range(1, self.n_rgb_hidden):
-                pk['wc'].append(lins[i].weight.half().contiguous())
-                pk['bc'].append(lins[i].bias.detach().float())
-            # transposes for the input-gradient GEMMs
-            pk['wcT'] = [None] + [w.t().contiguous() for w in pk['wc'][1:]]
-            pk['wc0T_feat'] = wc0[:, :256].t().contiguous()           # [256, Hc]
-            t = torch.zeros(64, self.Hc, device=W0.device, dtype=torch.float16)
-            t[:self.Kc0 - 256] = wc0[:, 256:].t()
-            pk['wc0T_tail'] = t                                        # [64, Hc]
-            pk['wl'] = lins[-1].weight.detach().float().contiguous()  # [3, Hc]
-            pk['bl'] = lins[-1].bias.detach().float().contiguous()
-            pk['s_var'] = m.s_var.detach().reshape(1).float().contiguous()
-            pk['app'] = m.appear_embed.weight.detach().float().contiguous() if self.app_dim else None
-            if self.bg:
-                self._pack_background(pk)
+        key = (sdf.active_levels, params.device)
+        if self._pkbuf is None or self._pkbuf['key'] != key:
+            self._pkbuf = dict(key=key)            # zero-initialised: padding columns stay zero
+        bufs = self._pkbuf
+        ents = []
+        pk, self.A, self.K0 = pack_sdf(sdf, self._table16, bufs, ents)
+        dev = params.device
+        f16 = torch.float16
+        z = lambda *sh: torch.zeros(*sh, device=dev, dtype=f16)  # noqa: E731
+        lins = m.neural_rgb.mlp.linears
+        l1 = sdf.mlp.linears[1]
+        Hc, n_hid = self.Hc, self.n_rgb_hidden
+        if 'w1' not in bufs:
+            bufs['w1'], bufs['w1T'] = z(*l1.bias.shape, l1.in_features), z(l1.in_features, *l1.bias.shape)
+            bufs['wc'] = [z(Hc, self.Kc0)] + [z(Hc, Hc) for _ in range(1, n_hid)]
+            bufs['wcT'] = [None] + [z(Hc, Hc) for _ in range(1, n_hid)]
+            bufs['wc0T_feat'], bufs['wc0T_tail'] = z(256, Hc), z(64, Hc)
+            bufs['wl'] = torch.zeros(lins[-1].bias.shape[0], Hc, device=dev, dtype=torch.float32)
+        v, g = _wsrc(l1)
+        ents.append(_pk_entry(v, g, dst16=bufs['w1'], dst16T=bufs['w1T']))
+        # colour layer 0 columns reordered to [feat 256 | x 3, SH 16, n 3, app | 0] from the
+        # reference's [x 3 | SH 16 | n 3 | feat 256 | app]
+        sh = 16
+        wc0, t_tail = bufs['wc'][0], bufs['wc0T_tail']
+        v, g = _wsrc(lins[0])
+        ents.append(_pk_entry(v, g, col0=6 + sh, ncols=256, dst16=wc0[:, :256], dst16T=bufs['wc0T_feat']))
+        ents.append(_pk_entry(v, g, col0=0, ncols=6 + sh, dst16=wc0[:, 256:256 + 6 + sh], dst16T=t_tail[:6 + sh]))
+        if self.app_dim:
+            ents.append(_pk_entry(v, g, col0=6 + sh + 256, ncols=self.app_dim,
+                                  dst16=wc0[:, 256 + 6 + sh:256 + 6 + sh + self.app_dim],
+                                  dst16T=t_tail[6 + sh:6 + sh + self.app_dim]))
+        for i in range(1, n_hid):
+            v, g = _wsrc(lins[i])
+            ents.append(_pk_entry(v, g, dst16=bufs['wc'][i], dst16T=bufs['wcT'][i]))
+        v, g = _wsrc(lins[-1])
+        ents.append(_pk_entry(v, g, dst32=bufs['wl']))
+        pk['w1'], pk['w1T'], pk['b1'] = bufs['w1'], bufs['w1T'], l1.bias.detach()
+        pk['wc'], pk['wcT'] = bufs['wc'], bufs['wcT']
+        pk['bc'] = [lins[i].bias.detach() for i in range(n_hid)]
+        pk['wc0T_feat'], pk['wc0T_tail'] = bufs['wc0T_feat'], t_tail          # [256, Hc], [64, Hc]
+        pk['wl'], pk['bl'] = bufs['wl'], lins[-1].bias.detach()
+        pk['s_var'] = m.s_var.detach().reshape(1)
+        pk['app'] = m.appear_embed.weight.detach() if self.app_dim else None
+        if self.bg:
+            self._pack_background(pk, bufs, ents)
+        _weightnorm_fwd(ents, dev)
         self.pk = pk
 
-    def _pack_background(self, pk):
-        """FP16 working copies of the background NeRF (no weight norm), laid out for the
-        dense kernel: layer 0 padded to the 96-column input, the skip layer over
-        [h4 | input], the last layer split into its 256 feature rows and the density row
-        (modules.py:258-264)."""
+    def _pack_background(self, pk, bufs, ents):
+        """Working copies of the background NeRF (no weight norm), laid out for the dense
+        kernel: layer 0 padded to the 96-column input, the skip layer over [h4 | input], the
+        last layer split into its 256 feature rows and the density row (modules.py:258-264);
+        pack entries appended to ``ents``."""
         bgm = self.model.background_nerf
         L, Lr = bgm.mlp_feat.linears, bgm.mlp_rgb.linears
         dev = L[0].weight.device
-        f16 = torch.float16
-        h = lambda x: x.detach().to(f16).contiguous()                      # noqa: E731
-        b = [None] * 8
-        w = [None] * 8
-        w[0] = torch.zeros(256, BG_X_COLS, device=dev, dtype=f16)
-        w[0][:, :84] = L[0].weight.detach()
-        for i in (1, 2, 3, 5, 6):
-            w[i] = h(L[i].weight)
-        w[4] = torch.zeros(256, BG_S_COLS, device=dev, dtype=f16)
-        w[4][:, :340] = L[4].weight.detach()
-        W7 = L[7].weight.detach()
-        w[7] = h(W7[1:])
-        for i in range(7):
-            b[i] = L[i].bias.detach().float().contiguous()
-        b[7] = L[7].bias.detach()[1:].float().contiguous()
-        pk['bw'], pk['bb'] = w, b
-        pk['bw7d'] = W7[0].float().contiguous()
-        pk['bb7d'] = L[7].bias.detach()[:1].float().contiguous()
-        # input-gradient operands (the dense kernel takes W^T)
-        pk['bwT'] = [None] + [w[i].t().contiguous() if i != 4 else w[4][:, :256].t().contiguous()
-                              for i in range(1, 7)]
-        w7ext = torch.zeros(272, 256, device=dev, dtype=f16)
-        w7ext[:256] = W7[1:]
-        w7ext[256] = W7[0]
-        pk['bw7extT'] = w7ext.t().contiguous()                              # [256, 272]
         Hbr, Kr0 = self.Hbr, self.Kr0
-        wr0 = torch.zeros(Hbr, Kr0, device=dev, dtype=f16)
-        wr0[:, :256 + 16 + self.app_dim] = Lr[0].weight.detach()            # [feat | SH | app]: same order
-        pk['bwr0'], pk['bbr0'] = wr0, Lr[0].bias.detach().float().contiguous()
-        pk['bwr0T_feat'] = wr0[:, :256].t().contiguous()                    # [256, Hbr]
-        t = torch.zeros(64, Hbr, device=dev, dtype=f16)
-        t[:Kr0 - 256] = wr0[:, 256:].t()
-        pk['bwr0T_tail'] = t                                                # [64, Hbr]
-        pk['bwr1'] = Lr[1].weight.detach().float().contiguous()            # [3, Hbr]
-        pk['bbr1'] = Lr[1].bias.detach().float().contiguous()
+        nin = 256 + 16 + self.app_dim
+        z = lambda *sh: torch.zeros(*sh, device=dev, dtype=torch.float16)  # noqa: E731
+        if 'bw' not in bufs:
+            bufs['bw'] = [z(256, BG_X_COLS)] + [z(256, 256) for _ in range(3)] + [z(256, BG_S_COLS)] + \
+                         [z(256, 256) for _ in range(3)]
+            bufs['bwT'] = [None] + [z(256, 256) for _ in range(6)]
+            bufs['bw7extT'] = z(256, 272)
+            bufs['bwr0'], bufs['bwr0T_feat'], bufs['bwr0T_tail'] = z(Hbr, Kr0), z(256, Hbr), z(64, Hbr)
+        w, wT = bufs['bw'], bufs['bwT']
+        W = lambda i: L[i].weight.detach()  # noqa: E731
+        ents.append(_pk_entry(W(0), ncols=84, dst16=w[0][:, :84]))
+        for i in (1, 2, 3, 5, 6):
+            ents.append(_pk_entry(W(i), dst16=w[i], dst16T=wT[i]))
+        ents.append(_pk_entry(W(4), ncols=340, dst16=w[4][:, :340]))
+        ents.append(_pk_entry(W(4), ncols=256, dst16T=wT[4]))
+        # layer 7: feature rows 1-256 (row-major and transposed), the density row transposed only
+        ents.append(_pk_entry(W(7), rows=slice(1, 257), dst16=w[7], dst16T=bufs['bw7extT'][:, :256]))
+        ents.append(_pk_entry(W(7), rows=slice(0, 1), dst16T=bufs['bw7extT'][:, 256:257]))
+        Wr0 = Lr[0].weight.detach()                                       # [feat | SH | app]: same order
+        ents.append(_pk_entry(Wr0, ncols=256, dst16=bufs['bwr0'][:, :256], dst16T=bufs['bwr0T_feat']))
+        ents.append(_pk_entry(Wr0, col0=256, ncols=nin - 256, dst16=bufs['bwr0'][:, 256:nin],
+                              dst16T=bufs['bwr0T_tail'][:nin - 256]))
+        b = [L[i].bias.detach() for i in range(7)] + [L[7].bias.detach()[1:]]
+        pk['bw'], pk['bb'] = w, b
+        pk['bw7d'] = W(7)[0]
+        pk['bb7d'] = L[7].bias.detach()[:1]
+        pk['bwT'] = wT                                                     # input-gradient operands (W^T)
+        pk['bw7extT'] = bufs['bw7extT']                                    # [256, 272]
+        pk['bwr0'], pk['bbr0'] = bufs['bwr0'], Lr[0].bias.detach()
+        pk['bwr0T_feat'], pk['bwr0T_tail'] = bufs['bwr0T_feat'], bufs['bwr0T_tail']   # [256, Hbr], [64, Hbr]
+        pk['bwr1'] = Lr[1].weight.detach()                                 # [3, Hbr]
+        pk['bbr1'] = Lr[1].bias.detach()
         ae = self.model.appear_embed_outside
-        pk['app_bg'] = ae.weight.detach().float().contiguous() if ae is not None else None
+        pk['app_bg'] = ae.weight.detach() if ae is not None else None
 
     # ------------------------------------------------------------------ workspace
     def _in_kernel_w0_grad(self):

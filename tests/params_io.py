@@ -83,13 +83,46 @@ def batch_to(batch, device, dtype=torch.float32):
     return out
 
 
+def step_weight_copies(model):
+    """The MLP weight copies exactly as the fused step forms them from the FP32 masters (weight
+    norm and rounding in gbsdf_weightnorm_fwd, a deterministic kernel), or None when the model
+    is not on a GPU or not a configuration the fused step takes."""
+    if not next(model.parameters()).is_cuda:
+        return None
+    from neuralangelo_gb300.fused import FusedField
+    try:
+        ff = FusedField(model)
+    except (ValueError, NotImplementedError):
+        return None
+    ff._pack()
+    return ff.pk
+
+
+class torch_rounded_weights:
+    """Within this block, model_to_oracle rounds torch's own FP32 weights to fp16 instead of
+    taking the step's copies: the other of two equally valid roundings of the same masters."""
+
+    def __enter__(self):
+        global step_weight_copies
+        self._saved, step_weight_copies = step_weight_copies, (lambda model: None)
+        return self
+
+    def __exit__(self, *exc):
+        global step_weight_copies
+        step_weight_copies = self._saved
+        return False
+
+
 def model_to_oracle(model, fp16_weights=False, effective=False):
     """FieldModel parameters -> the oracle's float64 dict.  With fp16_weights the
     table and the MLP weight matrices are first rounded to fp16 the way the fused
     step uses them (weight norm applied in fp32, then rounded; biases, SDF head,
-    s_var and the appearance table stay fp32)."""
+    s_var and the appearance table stay fp32): on a GPU the step's own copies, since
+    an FP32 weight one bit off rounds to a neighbouring fp16 value now and then, and a
+    ReLU gate can follow it."""
     s = model.neural_sdf
     p = {}
+    pk = step_weight_copies(model) if fp16_weights else None
 
     def q(t):
         return t.detach().half().double().cpu() if fp16_weights else t.detach().double().cpu()
@@ -107,8 +140,12 @@ def model_to_oracle(model, fp16_weights=False, effective=False):
         W = lin.weight.detach()
         if fp16_weights and i == 0:
             W = torch.cat([W[:, :3], W[:, 3:].half().float()], dim=1)    # position columns stay fp32
+            if pk is not None:                  # the step's copies over the active columns
+                n = s.active_levels * s.tcnn_encoding.layout.n_features
+                W[:, :3] = pk['w0x']
+                W[:, 3:3 + n] = pk['w0e'][:, :n].float()
         elif fp16_weights:
-            W = W.half().float()
+            W = pk['w1'].float() if pk is not None else W.half().float()
         p[f'sdf.l{i}.v'], p[f'sdf.l{i}.g'] = vg(lin, W)
         p[f'sdf.l{i}.b'] = lin.bias.detach().double().cpu()
     p['sdf.head.w'] = s.mlp.linear_sdf.weight.detach().double().cpu()
@@ -116,7 +153,15 @@ def model_to_oracle(model, fp16_weights=False, effective=False):
     lins = model.neural_rgb.mlp.linears
     for i, lin in enumerate(lins):
         W = lin.weight.detach()
-        if fp16_weights and i != len(lins) - 1:
+        if fp16_weights and pk is not None:
+            if i == 0:                          # undo the step's column order [feat | x, SH, n, app | 0]
+                wc0, sh, nt = pk['wc'][0].float(), 16, W.shape[1] - 256
+                W = torch.cat([wc0[:, 256:256 + 6 + sh], wc0[:, :256], wc0[:, 256 + 6 + sh:256 + nt]], dim=1)
+            elif i == len(lins) - 1:
+                W = pk['wl'].clone()
+            else:
+                W = pk['wc'][i].float()
+        elif fp16_weights and i != len(lins) - 1:
             W = W.half().float()
         p[f'rgb.l{i}.v'], p[f'rgb.l{i}.g'] = vg(lin, W)
         p[f'rgb.l{i}.b'] = lin.bias.detach().double().cpu()

@@ -147,3 +147,22 @@ def test_weightnorm_arguments_without_gpu(lib):
     assert lib.gbsdf_weightnorm_bwd(1, ptr, None, one, None) == 1
     assert b"needs g and dg" in lib.gbsdf_last_error()
     assert lib.gbsdf_weightnorm_bwd(0, None, None, one, None) == 0
+
+
+def test_weightnorm_pack_arguments_without_gpu(lib):
+    """gbsdf_weightnorm_fwd: the binding's struct layout and the checks that return before any
+    launch (segment past the row, no destination)."""
+    from neuralangelo_gb300 import fused
+    lib.gbsdf_weightnorm_pack_size.restype = ctypes.c_size_t
+    assert lib.gbsdf_weightnorm_pack_size() == ctypes.sizeof(fused.WeightNormPack)
+    arr = (fused.WeightNormPack * 1)()
+    e = arr[0]
+    e.rows, e.cols, e.v, e.ld_src, e.col0, e.ncols = 4, 8, 16, 8, 6, 4
+    ptr = ctypes.cast(arr, ctypes.c_void_p)
+    assert lib.gbsdf_weightnorm_fwd(1, ptr, None) == 1
+    assert b"segment" in lib.gbsdf_last_error()
+    e.col0 = 0
+    assert lib.gbsdf_weightnorm_fwd(1, ptr, None) == 1
+    assert b"no destination" in lib.gbsdf_last_error()
+    assert lib.gbsdf_weightnorm_fwd(fused.WN_MAX_LAYERS + 1, None, None) == 1
+    assert lib.gbsdf_weightnorm_fwd(0, None, None) == 0

