@@ -45,11 +45,13 @@ __device__ __forceinline__ int ray_of(const FieldParams& p, int64_t s) {
 }
 
 // float32 centre point c + d t (camera.py:314-320: one multiply, one add)
-__device__ __forceinline__ void sample_point(const FieldParams& p, int64_t s, float* x) {
-    const int r = ray_of(p, s);
+__device__ __forceinline__ void sample_point_of_ray(const FieldParams& p, int64_t s, int r, float* x) {
     const float t = p.dists[s];
 #pragma unroll
     for (int i = 0; i < 3; ++i) x[i] = __fadd_rn(p.center[3 * r + i], __fmul_rn(p.ray_unit[3 * r + i], t));
+}
+__device__ __forceinline__ void sample_point(const FieldParams& p, int64_t s, float* x) {
+    sample_point_of_ray(p, s, ray_of(p, s), x);
 }
 
 // evaluation position: the reference adds a float32 tap vector to the point.
@@ -362,6 +364,20 @@ __global__ void __launch_bounds__(256, CPT >= 8 ? 2 : (CPT == 4 ? 3 : 4)) k_fiel
 // bias columns], so the epilogue reads W0x x + b0 + W0e f from TMEM and adds
 // nothing; the fp16 residual of the features is a second MMA over the W0e prefix.
 constexpr int FWD_CTAS_PER_SM = 2;
+constexpr int FWD_APP_MAX = 28;        // appearance-code columns the forward's prefetch holds
+// One sample's per-ray inputs of the forward's per-sample phase, prefetched into a ring of
+// four tiles in shared memory (see k_field_fwd)
+struct FwdSample {
+    int r;                       // ray; -1 past the last sample
+    int out;                     // the ray's `outside` flag
+    int appi;                    // appearance-code row
+    float c[3];                  // sample point c + d t
+    float dv[3];                 // ray direction
+    float app[FWD_APP_MAX];      // appearance code
+};
+constexpr int FWD_RING = 4;
+// the colour-input tail is at most 48 columns with 23 fixed ones (check_fwd): app_dim <= 25
+static_assert(FWD_APP_MAX >= 48 - 23, "the prefetch record holds every appearance column");
 
 template <int F, int TAPS>
 __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(FieldParams p) {
@@ -380,6 +396,7 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
     // (125 or 126 evaluation rows + padding)
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sdf_s + FWD_SDF_FLOATS);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+    FwdSample* ring = reinterpret_cast<FwdSample*>(mbar + 2);  // [FWD_RING][SPT]
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     stage_rows_kmajor(w_s, (const __half*)p.w0b, 0, HID, KB, KB, tid, FIELD_THREADS, HID);
@@ -424,6 +441,59 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
             umma::mma_commit(mbar);
         }
     };
+    // The per-sample phase reads per-ray inputs (flags, direction, centre, appearance code)
+    // behind one or two dependent global loads.  They are prefetched into a ring of FWD_RING
+    // tiles by the threads that have no sample of their own in that phase, one load level per
+    // tile: the ray index three tiles ahead, the per-ray values two tiles ahead, the appearance
+    // row one tile ahead; each level lands before the next reads it (a CTA barrier apart).
+    const bool want_xc = p.xc != nullptr;
+    const bool want_app = want_xc && p.app_table && p.app_dim > 0;
+    auto slot = [&](int k) { return ring + (k & (FWD_RING - 1)) * SPT; };
+    auto tile_of = [&](int k) { return (int64_t)blockIdx.x + (int64_t)k * gridDim.x; };
+    auto pre_ray = [&](int k, int js) {
+        const int64_t tk = tile_of(k), ss = tk * SPT + js;
+        slot(k)[js].r = (tk < ntiles && ss < p.Ns) ? ray_of(p, ss) : -1;
+    };
+    auto pre_vals = [&](int k, int js) {
+        FwdSample& e = slot(k)[js];
+        const int r = e.r;
+        if (r < 0) return;
+        e.out = p.outside && p.outside[r];
+        if (want_xc) {
+            const int64_t ss = tile_of(k) * SPT + js;
+            sample_point_of_ray(p, ss, r, e.c);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) e.dv[i] = p.ray_unit[3 * r + i];
+        }
+        if (want_app) e.appi = p.app_idx[r];
+    };
+    auto pre_app = [&](int k, int js) {
+        FwdSample& e = slot(k)[js];
+        if (e.r < 0 || !want_app) return;
+        const float* a = p.app_table + (int64_t)e.appi * p.app_dim;
+        for (int i0 = 0; i0 < p.app_dim; i0 += 8) {
+            float v[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) v[j] = i0 + j < p.app_dim ? a[i0 + j] : 0.0f;
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (i0 + j < p.app_dim) e.app[i0 + j] = v[j];
+        }
+    };
+    constexpr int LD0 = (SPT * 6 + 31) / 32 * 32;    // first loader thread
+    static_assert(LD0 + 3 * SPT <= FIELD_THREADS, "the forward's prefetch loaders fit the CTA");
+    if (tid < SPT) {
+        pre_ray(0, tid);
+        pre_ray(1, tid);
+        pre_ray(2, tid);
+    }
+    __syncthreads();
+    if (tid < SPT) {
+        pre_vals(0, tid);
+        pre_vals(1, tid);
+    }
+    __syncthreads();
+    if (tid < SPT) pre_app(0, tid);
     int64_t t = blockIdx.x;
     if (t < ntiles) {
         stage(t);
@@ -432,7 +502,7 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
     }
     __syncthreads();
     if (t < ntiles) issue();
-    for (; t < ntiles; t += gridDim.x) {
+    for (int it = 0; t < ntiles; t += gridDim.x, ++it) {
         const int64_t s0 = t * SPT;
         const bool ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
         phase ^= 1u;
@@ -480,12 +550,19 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
         // per-sample: gradient, Hessian diagonal, outside overwrite, colour-input columns;
         // six threads per sample, each storing one 8-column chunk of the colour-input tail
         // (the first of them also the SDF, gradient and Hessian)
+        if (tid >= LD0 && tid < LD0 + 3 * SPT) {
+            const int li = tid - LD0, st = li / SPT, js = li - st * SPT;
+            if (st == 0) pre_ray(it + 3, js);
+            else if (st == 1) pre_vals(it + 2, js);
+            else pre_app(it + 1, js);
+        }
         if (tid < SPT * 6) {
             const int js = tid / 6, kc8 = tid - 6 * js;
             const int64_t ss = s0 + js;
+            const FwdSample& e = slot(it)[js];
             if (ss < p.Ns) {
-                const int r = ray_of(p, ss);
-                const bool out = p.outside && p.outside[r];
+                const int r = e.r;
+                const bool out = e.out != 0;
                 const float fc = out ? p.outside_val : sdf_s[js];
                 float g[3], hh[3];
                 if constexpr (TAPS == 6) {
@@ -521,10 +598,8 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
                 }
                 if (p.xc && 8 * kc8 < p.ldxc - HID) {
                     // NeuralRGB input tail (modules.py:209-213): x, SH(d), normalize(g), app
-                    float c[3];
-                    sample_point(p, ss, c);
-                    const float* dv = p.ray_unit + 3 * r;
-                    const float dx = dv[0], dy = dv[1], dz = dv[2];
+                    const float* c = e.c;
+                    const float dx = e.dv[0], dy = e.dv[1], dz = e.dv[2];
                     const float xx = dx * dx, yy = dy * dy, zz = dz * dz;
                     float col[22];
                     col[0] = c[0]; col[1] = c[1]; col[2] = c[2];
@@ -551,9 +626,8 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
                     // compile-time indices (col[] stays in registers), the appearance code read
                     // straight from the table, and the last (padding) column a constant 1: the
                     // colour layer-0 weight gradient dZ^T xc then carries the bias gradient there
-                    const float* a = (p.app_table && p.app_dim > 0)
-                                         ? p.app_table + (int64_t)p.app_idx[r] * p.app_dim
-                                         : nullptr;
+                    const float* a = want_app ? e.app : nullptr;
+                    (void)r;
                     __half* dst = (__half*)p.xc + ss * (int64_t)p.ldxc + HID;
                     const int ncol = p.ldxc - HID;
                     float o8[8];
@@ -1253,7 +1327,8 @@ template <int TAPS>
 static size_t fwd_smem(int K0) {
     const size_t KB = (size_t)K0 + 16;
     return (size_t)HID * KB * 2 + (size_t)TILE_M * (KB + K0) * 2 +
-           (HID + 2 * TILE_M + FWD_SDF_FLOATS) * 4 + 16;
+           (HID + 2 * TILE_M + FWD_SDF_FLOATS) * 4 + 16 +
+           (size_t)FWD_RING * TapTile<TAPS>::SPT * sizeof(FwdSample);
 }
 template <int TAPS>
 static size_t bwd_smem(int K0, bool dw) {
