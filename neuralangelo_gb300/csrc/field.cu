@@ -926,10 +926,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         const int64_t tn = t + gridDim.x;
         const int cb = DW ? (it & 1) : 0, nb = DW ? ((it + 1) & 1) : 0;   // this tile's / the next tile's A
         umma::fence_after_sync();
-        if (tn < ntiles) {
-            stage_a(tn, nb);                         // free: MMA1 of tile t completed (DW: the other buffer)
-            prologue_load(tn, pin);                  // consumed at the end of the tile
-        }
+        if (tn < ntiles) prologue_load(tn, pin);     // consumed under MMA2
         // (2) d_pre = (d f * w_head + [centre] d_h0c) * softplus'(pre) -> TMEM (hi, lo) and d_pre0
         uint8_t* stg = stage_s + warp * BWD_STAGE_BYTES;
         const CUtensorMap* tm_pre = q == 3 ? &tm_pre30 : &tm_pre32;
@@ -1074,13 +1071,15 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         if (warp == 0) __syncwarp();                 // the issuing lane rejoins its warp before the barrier
         if constexpr (DW) dw_first = false;
         if (tn < ntiles) {
+            // the next tile's A tile and d_h0c rows, issued while every thread waits for MMA2: the
+            // ~3,500 16-byte copies cost the issuing threads ~2k clocks wherever they go, and under the
+            // d_pre epilogue they stretched it by a fifth.  A is free: MMA1 of tile t has completed,
+            // and with DW it goes to the other buffer, whose last readers (the previous tile's lo dW0
+            // MMAs) completed before that tile's d_enc epilogue
+            stage_a(tn, nb);
             stage_dh0(tn);                           // every warp has read this tile's d_h0c rows
             prologue_ray(tn, pin);
             prologue_finish(tn, pin, (it + 1) & 1);  // the other df buffer, under the MMAs
-        }
-        if (DW && tn < ntiles) {
-            cp_async_wait_group<1>();                // tile tn's A tile (its d_h0c group may still be in flight)
-            umma::fence_proxy_async_smem();
         }
         ok = __syncthreads_and(tid == 0 ? umma::mbar_wait(mbar, phase) : true);   // one poller
         phase ^= 1u;
@@ -1106,6 +1105,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
                     make_uint4(__float_as_uint(f[4]), __float_as_uint(f[5]), __float_as_uint(f[6]),
                                __float_as_uint(f[7]));
             }
+            if (tn < ntiles) cp_async_wait_group<1>();   // tile tn's A tile, before MMA1(tn) below
             umma::fence_proxy_async_smem();
             umma::fence_before_sync();
             __syncthreads();
