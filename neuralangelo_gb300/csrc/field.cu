@@ -380,7 +380,9 @@ constexpr int FWD_RING = 4;
 static_assert(FWD_APP_MAX >= 48 - 23, "the prefetch record holds every appearance column");
 
 template <int F, int TAPS>
-__global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(FieldParams p) {
+__global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(FieldParams p,
+                                                                             const __grid_constant__ CUtensorMap tm_xhi,
+                                                                             const __grid_constant__ CUtensorMap tm_xlo) {
     constexpr int EVALS = TapTile<TAPS>::EVALS, SPT = TapTile<TAPS>::SPT;
     extern __shared__ __align__(1024) uint8_t smem[];
     const int K0 = p.K0;
@@ -395,14 +397,16 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
     // the mbarrier 8-byte aligned whatever the tile's row count: 128 floats past sdf_s
     // (125 or 126 evaluation rows + padding)
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sdf_s + FWD_SDF_FLOATS);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
-    FwdSample* ring = reinterpret_cast<FwdSample*>(mbar + 2);  // [FWD_RING][SPT]
+    uint64_t* mbar_a = mbar + 1;                                // the A tile's TMA loads
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
+    FwdSample* ring = reinterpret_cast<FwdSample*>(mbar + 3);  // [FWD_RING][SPT]
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     stage_rows_kmajor(w_s, (const __half*)p.w0b, 0, HID, KB, KB, tid, FIELD_THREADS, HID);
     for (int i = tid; i < HID; i += FIELD_THREADS) wh_s[i] = p.whead[i];
     if (tid == 0) {
         umma::mbar_init(mbar, 1);
+        umma::mbar_init(mbar_a, 1);
         umma::fence_mbar_init();
     }
     if (warp == 0) {
@@ -422,16 +426,24 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
     const int e_row = row / SPT, sl_row = row % SPT;
     uint32_t phase = 0;
 
-    // features of a tile, gathered by k_field_gather into x0ext; the next tile's
-    // load overlaps this tile's epilogue (A is free once its MMAs completed)
-    const int64_t xrows = ntiles * (int64_t)(SPT * EVALS);
-    auto stage = [&](int64_t tt) {
-        const __half* xb = (const __half*)p.x0ext;
-        stage_rows_kmajor(a_s, xb, tt * (SPT * EVALS), xrows, KX, KB, tid, FIELD_THREADS);
-        stage_rows_kmajor(a2_s, xb + K0 + 16, tt * (SPT * EVALS), xrows, KX, K0, tid, FIELD_THREADS);
+    // features of a tile, gathered by k_field_gather into x0ext, loaded by TMA (thread 0, one
+    // box per 8-row group and part, straight into the core-matrix layout; rows past the end
+    // arrive as zeros); the next tile's load overlaps this tile's epilogue (A is free once its
+    // MMAs completed)
+    // (a timed-out tile ends the loop at its top, before its load_a: no load is left in flight)
+    (void)KX;
+    auto load_a = [&](int64_t tt) {
+        umma::mbar_arrive_expect_tx(mbar_a, (uint32_t)(TILE_M * (KB + K0) * 2));
+        const int row0 = (int)(tt * (SPT * EVALS));
+#pragma unroll 1
+        for (int g = 0; g < TILE_M / 8; ++g) {
+            umma::tma_load_3d(a_s + g * KB * 16, &tm_xhi, 0, row0 + 8 * g, 0, mbar_a);
+            umma::tma_load_3d(a2_s + g * K0 * 16, &tm_xlo, 0, row0 + 8 * g, 0, mbar_a);
+        }
     };
-    auto issue = [&]() {
+    auto issue = [&](uint32_t phase_a) {           // the k-th call waits for the k-th load: phase k & 1
         if (tid == 0) {
+            if (!umma::mbar_wait(mbar_a, phase_a)) flag_timeout(p.err, 1);   // the A tile's TMA loads
             umma::fence_after_sync();
             // smallest terms first: the tensor core's FP32 accumulation drops low
             // bits of addends much smaller than the running sum, so the fp16
@@ -495,13 +507,9 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
     __syncthreads();
     if (tid < SPT) pre_app(0, tid);
     int64_t t = blockIdx.x;
-    if (t < ntiles) {
-        stage(t);
-        cp_async_wait_all();
-        umma::fence_proxy_async_smem();
-    }
+    if (t < ntiles && tid == 0) load_a(t);
     __syncthreads();
-    if (t < ntiles) issue();
+    if (t < ntiles) issue(0u);
     for (int it = 0; t < ntiles; t += gridDim.x, ++it) {
         const int64_t s0 = t * SPT;
         const bool ok = __syncthreads_and(umma::mbar_wait(mbar, phase));
@@ -512,7 +520,7 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
         }
         umma::fence_after_sync();
         const int64_t tn = t + gridDim.x;
-        if (tn < ntiles) stage(tn);
+        if (tn < ntiles && tid == 0) load_a(tn);
         // epilogue: h = softplus(pre) ; partial head dot ; centre rows keep h in h0c
         const int64_t s = s0 + sl_row;
         const bool keep = row < SPT * EVALS && s < p.Ns && e_row == 0;
@@ -647,12 +655,8 @@ __global__ void __launch_bounds__(FIELD_THREADS, FWD_CTAS_PER_SM) k_field_fwd(Fi
                 }
             }
         }
-        if (tn < ntiles) {
-            cp_async_wait_all();
-            umma::fence_proxy_async_smem();
-        }
         __syncthreads();
-        if (tn < ntiles) issue();
+        if (tn < ntiles) issue((uint32_t)(it + 1) & 1u);
     }
     umma::fence_before_sync();
     __syncthreads();
@@ -705,12 +709,13 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
                                                              const __grid_constant__ CUtensorMap tm_enc32,
                                                              const __grid_constant__ CUtensorMap tm_enc30,
                                                              const __grid_constant__ CUtensorMap tm_plo32,
-                                                             const __grid_constant__ CUtensorMap tm_plo30) {
+                                                             const __grid_constant__ CUtensorMap tm_plo30,
+                                                             const __grid_constant__ CUtensorMap tm_xhi,
+                                                             const __grid_constant__ CUtensorMap tm_xlo) {
     constexpr int EVALS = TapTile<TAPS>::EVALS, SPT = TapTile<TAPS>::SPT, TILE_ROWS = TapTile<TAPS>::ROWS;
     extern __shared__ __align__(1024) uint8_t smem[];
     const int K0 = p.K0;
     const int KB = K0 + 16;                                     // features hi + tail
-    const int KX = 2 * K0 + 16;                                 // x0ext row width
     uint8_t* stage_s = smem;                                    // [16 warps][4 KB] TMA store staging
     uint8_t* w_s = stage_s + (BWD_THREADS / 32) * BWD_STAGE_BYTES;   // [256 x KB]  w0b: B of MMA1
     uint8_t* a_s0 = w_s + HID * KB * 2;                         // [128 x KB]  features hi | tail
@@ -724,7 +729,8 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     float* dh0_s = df_s + TapTile<TAPS>::DF_FLOATS;              // [SPT][DH0_LD] d_h0c of the tile's samples
     uint64_t* mbar = reinterpret_cast<uint64_t*>(dh0_s + SPT * DH0_LD);
     uint64_t* mbar_lo = mbar + 1;                               // DW: the lo-half dW0 MMAs of a tile
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
+    uint64_t* mbar_a = mbar + 2;                                // the A tile's TMA loads
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 3);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     stage_rows_kmajor(w_s, (const __half*)p.w0b, 0, HID, KB, KB, tid, BWD_THREADS, HID);
@@ -743,6 +749,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     if (tid == 0) {
         umma::mbar_init(mbar, 1);
         umma::mbar_init(mbar_lo, 1);
+        umma::mbar_init(mbar_a, 1);
         umma::fence_mbar_init();
     }
     if (warp == 0) {
@@ -867,16 +874,21 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     };
     // encoder features of a tile, streamed back from the forward's x0ext rows (rows
     // 126-127 of a tile read the next tile's first rows or zeros; their MMA results
-    // are never used), and the d_h0c rows of its 18 samples; the next tile's load
-    // overlaps this tile's epilogue
-    const int64_t xrows = ntiles * (int64_t)(SPT * EVALS);
-    auto stage_a = [&](int64_t tt, int buf) {      // one cp.async group
-        const __half* xb = (const __half*)p.x0ext;
-        stage_rows_kmajor(a_buf(buf), xb, tt * (SPT * EVALS), xrows, KX, KB, tid, BWD_THREADS);
-        stage_rows_kmajor(a3_buf(buf), xb + K0 + 16, tt * (SPT * EVALS), xrows, KX, K0, tid, BWD_THREADS, TILE_M,
-                          KL);
-        cp_async_commit();
+    // are never used) by TMA: one thread, one box per 8-row group and part, straight into
+    // the core-matrix layout (rows past the end, and the lo part's zero columns, arrive
+    // as zeros); 512 threads' cp.async copies of the same bytes cost them ~2k clocks a tile
+    bool a_pending = false;                         // (thread 0, which issues and waits for these loads)
+    auto load_a = [&](int64_t tt, int buf) {
+        a_pending = true;
+        umma::mbar_arrive_expect_tx(mbar_a, (uint32_t)(TILE_M * (KB + KL) * 2));
+        const int row0 = (int)(tt * (SPT * EVALS));
+#pragma unroll 1
+        for (int g = 0; g < TILE_M / 8; ++g) {
+            umma::tma_load_3d(a_buf(buf) + g * KB * 16, &tm_xhi, 0, row0 + 8 * g, 0, mbar_a);
+            umma::tma_load_3d(a3_buf(buf) + g * KL * 16, &tm_xlo, 0, row0 + 8 * g, 0, mbar_a);
+        }
     };
+    uint32_t phase_a = 0;
     auto stage_dh0 = [&](int64_t tt) {             // one cp.async group
         for (int c = tid; c < SPT * (HID / 4); c += BWD_THREADS) {
             const int js = c / (HID / 4), k4 = c - js * (HID / 4);
@@ -890,12 +902,15 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
     auto issue1 = [&](int buf) {                   // warp 0 converged: every call follows a CTA barrier
         if (warp == 0) {
             if (umma::elect_one()) {
+                if (!umma::mbar_wait(mbar_a, phase_a)) flag_timeout(p.err, 1);   // the A tile's TMA loads
+                a_pending = false;
                 umma::fence_after_sync();
                 issue_tile_mma_strided(tmem, a3_addr(buf), KL, w_addr, KB, K0, idesc1);   // residuals first
                 issue_tile_mma(tmem, a_addr(buf), w_addr, KB, idesc1, true);
                 umma::mma_commit(mbar);
             }
             __syncwarp();
+            phase_a ^= 1u;
         }
     };
     int64_t t = blockIdx.x;
@@ -904,7 +919,7 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         prologue_load(t, pin);
         prologue_ray(t, pin);
         prologue_finish(t, pin, 0);
-        stage_a(t, 0);
+        if (tid == 0) load_a(t, 0);
         stage_dh0(t);
         cp_async_wait_all();
         umma::fence_proxy_async_smem();
@@ -926,6 +941,11 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         const int64_t tn = t + gridDim.x;
         const int cb = DW ? (it & 1) : 0, nb = DW ? ((it + 1) & 1) : 0;   // this tile's / the next tile's A
         umma::fence_after_sync();
+        // the next tile's A tile, under the d_pre epilogue: MMA1 of tile t has completed, and with DW
+        // it goes to the other buffer, whose last readers (the previous tile's lo dW0 MMAs) completed
+        // before MMA1(t).  (Issued after MMA2 instead, its writes slowed the shared-memory-bound dW0
+        // MMAs.)
+        if (tn < ntiles && tid == 0) load_a(tn, nb);
         if (tn < ntiles) prologue_load(tn, pin);     // consumed under MMA2
         // (2) d_pre = (d f * w_head + [centre] d_h0c) * softplus'(pre) -> TMEM (hi, lo) and d_pre0
         uint8_t* stg = stage_s + warp * BWD_STAGE_BYTES;
@@ -1071,12 +1091,8 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
         if (warp == 0) __syncwarp();                 // the issuing lane rejoins its warp before the barrier
         if constexpr (DW) dw_first = false;
         if (tn < ntiles) {
-            // the next tile's A tile and d_h0c rows, issued while every thread waits for MMA2: the
-            // ~3,500 16-byte copies cost the issuing threads ~2k clocks wherever they go, and under the
-            // d_pre epilogue they stretched it by a fifth.  A is free: MMA1 of tile t has completed,
-            // and with DW it goes to the other buffer, whose last readers (the previous tile's lo dW0
-            // MMAs) completed before that tile's d_enc epilogue
-            stage_a(tn, nb);
+            // the next tile's d_h0c rows, issued while every thread waits for MMA2 (copies landing
+            // under the d_pre epilogue stretch it)
             stage_dh0(tn);                           // every warp has read this tile's d_h0c rows
             prologue_ray(tn, pin);
             prologue_finish(tn, pin, (it + 1) & 1);  // the other df buffer, under the MMAs
@@ -1105,7 +1121,6 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
                     make_uint4(__float_as_uint(f[4]), __float_as_uint(f[5]), __float_as_uint(f[6]),
                                __float_as_uint(f[7]));
             }
-            if (tn < ntiles) cp_async_wait_group<1>();   // tile tn's A tile, before MMA1(tn) below
             umma::fence_proxy_async_smem();
             umma::fence_before_sync();
             __syncthreads();
@@ -1154,14 +1169,11 @@ __global__ void __launch_bounds__(BWD_THREADS, 1) k_field_bwd(FieldParams p,
             }
         }
         umma::fence_before_sync();
-        if (!DW && tn < ntiles) {
-            cp_async_wait_group<1>();                // tile tn's A tile (its d_h0c group may still be in flight)
-            umma::fence_proxy_async_smem();
-        }
         ok = __syncthreads_and(ok);   // the TMEM accumulator of tile t read; tile tn's A tile and d f in place
         if (ok && !DW && tn < ntiles) issue1(nb);
     }
     cp_async_wait_all();
+    if (tid == 0 && a_pending && !umma::mbar_wait(mbar_a, phase_a)) flag_timeout(p.err, 1);   // a load left in flight
     if (lane == 0) umma::bulk_wait0();               // this warp's TMA stores have completed
     umma::fence_before_sync();
     __syncthreads();
@@ -1327,7 +1339,7 @@ template <int TAPS>
 static size_t fwd_smem(int K0) {
     const size_t KB = (size_t)K0 + 16;
     return (size_t)HID * KB * 2 + (size_t)TILE_M * (KB + K0) * 2 +
-           (HID + 2 * TILE_M + FWD_SDF_FLOATS) * 4 + 16 +
+           (HID + 2 * TILE_M + FWD_SDF_FLOATS) * 4 + 24 +
            (size_t)FWD_RING * TapTile<TAPS>::SPT * sizeof(FwdSample);
 }
 template <int TAPS>
@@ -1335,13 +1347,25 @@ static size_t bwd_smem(int K0, bool dw) {
     const size_t KB = (size_t)K0 + 16;
     const size_t need = (size_t)(BWD_THREADS / 32) * BWD_STAGE_BYTES + (size_t)HID * KB * 2 +
                         (size_t)TILE_M * (KB + (dw ? KB : K0)) * 2 * (dw ? 2 : 1) +
-                        (2 * HID + TapTile<TAPS>::DF_FLOATS + TapTile<TAPS>::SPT * DH0_LD) * 4 + 24;
+                        (2 * HID + TapTile<TAPS>::DF_FLOATS + TapTile<TAPS>::SPT * DH0_LD) * 4 + 32;
     return need > BWD_SMEM_FLOOR ? need : BWD_SMEM_FLOOR;
 }
 
 // The field's four kernels, in step order.  `which`: bit 0 the hash-grid gather,
 // bit 1 the MLP forward, bit 2 the MLP backward, bit 3 the table-gradient scatter.
 enum FieldKernels : int { FK_GATHER = 1, FK_MLP_FWD = 2, FK_MLP_BWD = 4, FK_SCATTER = 8 };
+
+// TMA maps of the x0ext rows as the field MLP's A tiles (8-row groups in the core-matrix layout):
+// features hi | tail (K0 + 16 columns), and features lo into a tile lo_cols wide (K0, or K0 + 16
+// whose last two chunks lie past the tensor and arrive as zeros)
+static int x0ext_maps(const FieldParams& p, int64_t rows, int lo_cols, CUtensorMap* hi, CUtensorMap* lo) {
+    const int KX = 2 * p.K0 + 16;
+    if (rows <= 0) rows = 1;                          // (no tile is loaded)
+    if (int st = tensor_map_kmajor_groups(hi, p.x0ext, rows, (p.K0 + 16) / 8, KX, (p.K0 + 16) / 8, "x0ext hi"))
+        return st;
+    return tensor_map_kmajor_groups(lo, (const __half*)p.x0ext + p.K0 + 16, rows, p.K0 / 8, KX, lo_cols / 8,
+                                    "x0ext lo");
+}
 
 template <int F, int TAPS>
 static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
@@ -1370,8 +1394,10 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
         // p.fwd_ctas (a tuning choice): resident CTAs per SM to launch, 1 or 2 (0 = 2)
         int64_t grid = num_sms() * (p.fwd_ctas == 1 ? 1 : FWD_CTAS_PER_SM);
         if (grid > ntiles) grid = ntiles;
+        CUtensorMap tm_xhi, tm_xlo;
+        if (int st = x0ext_maps(p, ntiles * TILE_ROWS, p.K0, &tm_xhi, &tm_xlo)) return st;
         allow_max_smem(k_field_fwd<F, TAPS>);
-        k_field_fwd<F, TAPS><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p);
+        k_field_fwd<F, TAPS><<<(unsigned)grid, FIELD_THREADS, smem, s>>>(p, tm_xhi, tm_xlo);
         if (int st = launch_status("field forward")) return st;
     }
     if (which & FK_MLP_BWD) {
@@ -1416,16 +1442,18 @@ static int launch_field(const FieldParams& p, int which, cudaStream_t s) {
         } else {
             tm_plo32 = tm_plo30 = tm_pre32;              // unused
         }
+        CUtensorMap tm_xhi, tm_xlo;
+        if (int st = x0ext_maps(p, rows, dw ? p.K0 + 16 : p.K0, &tm_xhi, &tm_xlo)) return st;
         int64_t grid = num_sms();
         if (grid > ntiles) grid = ntiles;
         if (dw) {
             allow_max_smem(k_field_bwd<F, true, TAPS>);
             k_field_bwd<F, true, TAPS><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30,
-                                                                             tm_plo32, tm_plo30);
+                                                                             tm_plo32, tm_plo30, tm_xhi, tm_xlo);
         } else {
             allow_max_smem(k_field_bwd<F, false, TAPS>);
             k_field_bwd<F, false, TAPS><<<(unsigned)grid, BWD_THREADS, smem, s>>>(p, tm_pre32, tm_pre30, tm_enc32, tm_enc30,
-                                                                              tm_plo32, tm_plo30);
+                                                                              tm_plo32, tm_plo30, tm_xhi, tm_xlo);
         }
         if (int st = launch_status("field backward")) return st;
     }

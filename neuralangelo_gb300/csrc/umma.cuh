@@ -173,6 +173,13 @@ __device__ __forceinline__ void tma_load_2d(void* smem_dst, const void* tmap, in
 }
 
 // 2D TMA tile store shared -> global (bulk group); elements past the tensor are not written
+// 3D tiled load (coordinates innermost first) completing on an mbarrier's transaction count
+__device__ __forceinline__ void tma_load_3d(void* smem_dst, const void* tmap, int x, int y, int z, uint64_t* mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(smem_u32(smem_dst)), "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_u32(mbar))
+        : "memory");
+}
 __device__ __forceinline__ void tma_store_2d(const void* tmap, int x, int y, const void* smem_src) {
     asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
                      reinterpret_cast<uint64_t>(tmap)),
