@@ -481,8 +481,8 @@ int gbsdf_wgrad(int64_t M, int N, int K, const void* dZ, const void* dZ_lo, int 
                 float* dW, int ldw, int accumulate, int* err, void* stream);
 
 /* Gradients of weight-normalised linears (torch.nn.utils.weight_norm, dim 0: W = g v / ||v||
- * per output row; projects/neuralangelo/utils/mlp.py:55-69, projects/nerf/utils/nerf_util.py:
- * 187-196) from the gradient of the effective weight, with the loss scale taken off; replaces
+ * per output row; applied at projects/neuralangelo/utils/mlp.py:42-43 and
+ * projects/nerf/utils/nerf_util.py:177-178) from the gradient of the effective weight, with the loss scale taken off; replaces
  * autograd's per-layer weight-norm backward.  An entry with v == NULL is plain: the weight's
  * gradient gets s dW and the bias's s db (s = *scale_dev when scale_dev is not NULL, else scale).
  * Gradient tensors (dv, dg, dbias) are contiguous; acc_* = 1 adds into them, 0 overwrites.

@@ -2,7 +2,7 @@
 // loss scale taken off, in one launch for a whole list of layers.
 //
 // The reference wraps the SDF and colour MLP linears in torch.nn.utils.weight_norm (dim 0;
-// projects/neuralangelo/utils/mlp.py:55-69, projects/nerf/utils/nerf_util.py:187-196):
+// projects/neuralangelo/utils/mlp.py:42-43, projects/nerf/utils/nerf_util.py:177-178):
 // W = g v / ||v||, the norm taken over each output row.  The fused step yields the gradient of
 // the effective weight W (times the loss scale); autograd through the weight norm is, for
 // output row r with n = ||v_r|| and s = 1 / loss scale,

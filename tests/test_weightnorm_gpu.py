@@ -1,6 +1,6 @@
 """Weight-norm backward kernel (gbsdf_weightnorm_bwd) against torch autograd through
 torch.nn.utils.weight_norm (dim 0), the parametrisation of the reference's MLP linears
-(projects/neuralangelo/utils/mlp.py:55-69): the gradients of v, g and the bias from the
+(projects/neuralangelo/utils/mlp.py:42-43): the gradients of v, g and the bias from the
 effective-weight gradient, with the loss scale taken off, written or accumulated."""
 import pytest
 import torch
