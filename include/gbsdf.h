@@ -199,7 +199,8 @@ typedef struct gbsdf_field_args {
     void* d_pre0;            /* fp16 [126 T, 256], T = ceil(Ns / 18) tiles, tile-major rows (backward) */
     void* x0ext;             /* fp16 [126 T, 2 K0 + 16] tile-major rows: features hi | x,y,z hi, 1,
                                 x,y,z lo, 1, x,y,z hi, 0 x 5 | features lo; written by the forward,
-                                read by the backward */
+                                read by the backward; 16-byte aligned (the MLP kernels load its rows
+                                by TMA) */
     float* d_enc;            /* [126 T, K0] gradient of the encoder features (backward workspace) */
     float* d_whead;          /* [256] accumulated */
     float* d_bhead;          /* [1] accumulated */

@@ -1526,7 +1526,7 @@ static int field_dispatch(const FieldParams& p, int which, void* stream) {
 
 static int check_fwd(const FieldParams& p, int which) {
     if (int st = check_field(p)) return st;
-    GBSDF_CHECK_ARG(p.x0ext, "NULL x0ext");
+    GBSDF_CHECK_ARG(p.x0ext && aligned(p.x0ext, 16), "x0ext missing or misaligned (16 bytes: its rows are loaded by TMA)");
     if (which & FK_MLP_FWD) {
         GBSDF_CHECK_ARG(p.sdf && p.grad && p.hess && p.h0c, "NULL output");
         GBSDF_CHECK_ARG(p.w0b && aligned(p.w0b, 16), "w0b (fp16 [256, K0 + 16]) missing or misaligned");
@@ -1552,6 +1552,7 @@ static int check_bwd(const FieldParams& p, int which) {
         GBSDF_CHECK_ARG(!p.d_w0 || p.K0 <= 64, "d_w0 needs K0 <= 64 (K0 %d): pass d_pre0 instead", p.K0);
         GBSDF_CHECK_ARG(aligned(p.d_h0c, 16), "d_h0c alignment");
         GBSDF_CHECK_ARG(!p.d_pre0_lo || aligned(p.d_pre0_lo, 16), "d_pre0_lo alignment");
+        GBSDF_CHECK_ARG(aligned(p.x0ext, 16), "x0ext misaligned (16 bytes: its rows are loaded by TMA)");
     }
     if (which & FK_SCATTER) {
         GBSDF_CHECK_ARG(p.d_table && aligned(p.d_table, 16), "d_table missing or misaligned");

@@ -103,6 +103,24 @@ def test_field_backward_weight_gradient_arguments_without_gpu(lib):
     assert b"d_pre0" in lib.gbsdf_last_error()
 
 
+def test_x0ext_alignment_rejected_without_gpu(lib):
+    """The field MLP kernels load x0ext rows by TMA: a base off 16 bytes is an argument error."""
+    from neuralangelo_gb300.fused import FieldArgs
+    a = FieldArgs()
+    assert lib.gbsdf_grid_init(ctypes.byref(a.grid), 16, 8, 14, 32, ctypes.c_float(1.3195079)) == 0
+    a.Ns, a.S = 100, 10
+    for f in ("center", "ray_unit", "dists", "table", "w0e", "w0b", "w0x", "b0", "whead", "bhead", "grad",
+              "d_sdf", "d_grad", "d_hess", "d_xc", "d_h0c", "d_enc", "d_whead", "d_bhead", "d_w0"):
+        setattr(a, f, 256)
+    a.active, a.K0 = 8, 64
+    a.x0ext = 264                                  # 8 bytes past a 16-byte boundary
+    assert lib.gbsdf_field_mlp_bwd(ctypes.byref(a), None) == 1
+    assert b"x0ext" in lib.gbsdf_last_error()
+    a.sdf, a.hess, a.h0c = 256, 256, 256
+    assert lib.gbsdf_field_mlp_fwd(ctypes.byref(a), None) == 1
+    assert b"x0ext" in lib.gbsdf_last_error()
+
+
 def test_workspace_size_queries(lib):
     """The field calls' caller-owned buffers are sized by the library: rows are whole tiles of
     18 samples x 7 evaluations (6 taps) or 25 x 5 (4 taps); render and dense need none."""
