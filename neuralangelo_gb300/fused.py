@@ -355,7 +355,7 @@ class FusedField:
         # halves only (that costs <= 2e-4).  False: single fp16 storage (faster, less accurate).
         self.pairs = bool(activation_pairs)
         # the layer-0 weight gradient: accumulated by the backward kernel itself (K0 <= 64), or
-        # (False, or K0 > 64) from the kernel's fp16 d_pre0 rows by a separate GEMM
+        # (False, or K0 > 64) from the kernel's fp16 d_pre0 rows by the separate weight-gradient kernel (k_wgrad)
         self.fused_w0_grad = bool(fused_w0_grad)
         # carry the colour MLP's input gradients as fp16 hi+lo pairs (costs ~9% of the step and
         # leaves the weight-gradient error unchanged: that comes from fp16 storage of the
@@ -539,7 +539,7 @@ class FusedField:
                   dzs_lo=[e(Ns, Hc, dt=f16) for _ in range(2)] if self.split else None,
                   dzfeat=e(Ns, 256, dt=f16), dzfeat_lo=e(Ns, 256, dt=f16) if self.split else None,
                   dxc_tail=e(Ns, 64), d_h0c=e(Ns, 256),
-                  # K0 <= 64: the backward kernel accumulates dW0 itself; otherwise d_pre0 -> GEMM
+                  # K0 <= 64: the backward kernel accumulates dW0 itself; otherwise d_pre0 -> k_wgrad
                   d_pre0=None if self._in_kernel_w0_grad() else e(rows0, 256, dt=f16),
                   d_pre0_lo=None if self._in_kernel_w0_grad() else e(rows0, 256, dt=f16),
                   d_w0=e(256, self.K0 + 16) if self._in_kernel_w0_grad() else None,
