@@ -355,7 +355,7 @@ class FusedField:
         # halves only (that costs <= 2e-4).  False: single fp16 storage (faster, less accurate).
         self.pairs = bool(activation_pairs)
         # the layer-0 weight gradient: accumulated by the backward kernel itself (K0 <= 64), or
-        # (False, or K0 > 64) from the kernel's fp16 d_pre0 rows by the separate weight-gradient kernel (k_wgrad)
+        # (False, or K0 > 64) from the kernel's fp16 d_pre0 rows by the weight-gradient kernel
         self.fused_w0_grad = bool(fused_w0_grad)
         # carry the colour MLP's input gradients as fp16 hi+lo pairs (costs ~9% of the step and
         # leaves the weight-gradient error unchanged: that comes from fp16 storage of the
