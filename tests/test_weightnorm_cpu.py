@@ -61,3 +61,25 @@ def test_pack_entries_describe_segments_and_destinations():
     t7 = torch.zeros(6, 9, dtype=torch.float16)
     er = fused._pk_entry(w7, rows=slice(1, 5), dst16T=t7[:, :4])
     assert er.rows == 4 and er.v == w7.data_ptr() + 6 * 4 and er.ldT == 9
+
+
+def test_active_table_prefix_follows_the_level_layout():
+    """The fp16 working copy and the captured step's gradient clearing cover the active levels
+    only: a level-major prefix of offset[active] entries x F features, growing with the schedule."""
+    from neuralangelo_gb300.config import field_config
+    from neuralangelo_gb300.model import FieldModel
+    from neuralangelo_gb300.workloads import full_field_iteration
+    cfg = field_config("full")
+    cfg.sdf.encoding.hashgrid.dict_size = 14
+    model = FieldModel(cfg)
+    sdf = model.neural_sdf
+    layout = sdf.tcnn_encoding.layout
+    F = layout.n_features
+    seen = []
+    for active in (4, 8, 12, layout.n_levels):
+        model.schedule(full_field_iteration(active))
+        assert sdf.active_levels == active
+        n = fused.active_table_params(sdf)
+        assert n == int(layout.offset[active]) * F
+        seen.append(n)
+    assert seen == sorted(seen) and seen[-1] == sdf.tcnn_encoding.params.numel()
